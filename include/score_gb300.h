@@ -1,0 +1,225 @@
+/*
+ * score_gb300 — C ABI of the GB300-native recrystallization (RX) growth step.
+ *
+ * This boundary replaces the C++ member-function interface that SCORE's growth
+ * machine calls inside one OpenMP region (caHdl::solve_RXGROWTH,
+ * src/SCORE_Kernel.cpp:6497-6792).  Plain C types only; every function returns
+ * an int status (SCORE_OK = 0, negative on error) and never aborts.  Inputs are
+ * HOST buffers that the library copies; the context owns all device memory.
+ * One context = one domain = one CUDA stream; single-threaded caller.
+ *
+ * Sequence (mirrors SIMULATE_myCAs, src/SCORE_Kernel.cpp:1693-1756):
+ *   score_uds_read -> score_create -> score_load_domain -> score_place_nuclei
+ *   -> score_step ... (or score_run_until) -> score_export_labels -> score_destroy
+ */
+#ifndef SCORE_GB300_H
+#define SCORE_GB300_H
+
+#include <stdint.h>
+#include <stddef.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define SCORE_ABI_VERSION 1
+
+/* status codes */
+#define SCORE_OK                     0
+#define SCORE_ERR_ARG               -1  /* bad argument / inconsistent sizes */
+#define SCORE_ERR_CUDA              -2  /* CUDA runtime error (message in score_last_error) */
+#define SCORE_ERR_NOMEM             -3  /* device or host allocation failed */
+#define SCORE_ERR_CAPACITY          -4  /* a front list would exceed its device capacity */
+#define SCORE_ERR_BORDER_CAPACITY   -5  /* Border list exceeded 2(xy+xz+yz); the reference writes out of bounds here */
+#define SCORE_ERR_TIMEOUT           -6  /* a bounded device wait gave up (error flag set by a kernel) */
+#define SCORE_ERR_STATE             -7  /* call out of sequence */
+#define SCORE_ERR_IO                -8  /* .uds file missing or malformed */
+#define SCORE_ERR_KEYLIMIT          -9  /* more infection attempts in one step than the 32-bit claim key can order */
+#define SCORE_ERR_NOT_BUILT        -10  /* CUDA path unavailable (no device) */
+
+#define SCORE_MAX_TABLE 256        /* max rows of the time tables (annealing, drag) and X logpoint lists */
+
+/* mobility models, src/SCORE_Defs_Functionality.h:280-281 (values as read from "MobilityModel") */
+#define SCORE_MOBILITY_SEBALD_GOTTSTEIN 1
+#define SCORE_MOBILITY_ROLLETT_HOLM     2
+/* recovery models, "RecoveryConsider" 0..3; SCORE_RECOVERY_HYPERBOLIC is this library's rho0/(1+k t) law */
+#define SCORE_RECOVERY_NONE             0
+#define SCORE_RECOVERY_NES_VACCOREDIFF  1
+#define SCORE_RECOVERY_NES_SOLUTEDRAG   2
+#define SCORE_RECOVERY_MICHALAKPAXTON   3
+#define SCORE_RECOVERY_HYPERBOLIC      10
+/* Zener drag, "ZenerConsider" 0..2 */
+#define SCORE_ZENER_NONE     0
+#define SCORE_ZENER_CONSTANT 1
+#define SCORE_ZENER_TIMEDEP  2
+/* boundary handling of the domain */
+#define SCORE_BOUNDARY_REFERENCE 0  /* x,y periodic, z open: SCORE_Kernel.cpp:4362-4377 */
+#define SCORE_BOUNDARY_PERIODIC  1  /* x,y,z periodic */
+/* fill arithmetic */
+#define SCORE_PRECISION_FP64        0  /* bit-exact with the reference */
+#define SCORE_PRECISION_FP32_KAHAN  1  /* FP32 fill with Kahan compensation; FP64 dt/P */
+/* Border-list overflow policy */
+#define SCORE_BORDER_REFERENCE_LIMIT 0 /* fail with SCORE_ERR_BORDER_CAPACITY where the reference overruns */
+#define SCORE_BORDER_GROW            1 /* keep appending (slot order unchanged) */
+
+/*
+ * Growth parameters in SI units, exactly as the reference holds them after
+ * ensembleHdl::init_parameter (src/SCORE_Kernel.cpp:262-960): activation
+ * enthalpies already multiplied by echarge, temperatures in K (C + 273.15),
+ * cell size in m.  Table rows (annealing schedule, drag) keep the reference's
+ * float truncation of "*(ff)" columns (src/SCORE_Io.h:119).
+ */
+typedef struct score_params {
+    uint32_t nx, ny, nz;              /* 3DCAEdgeLengthInCells RD/TD/ND */
+    double cellsize;                  /* CellSize [um] * 1e-6 */
+    double xmax;                      /* XMAX */
+    double tmax;                      /* TIMEMAX [s] */
+    uint32_t nmax;                    /* NMAX */
+    double maxfillperstep;            /* MAXFILLPERSTEP */
+    double initial_cache;             /* InitialCacheSizeRXCells (sets recycle-list caps) */
+    double recache;                   /* ReCacheSizeRXCells */
+    int32_t defragmentation;          /* OnTheFlyDefragmentation */
+    uint32_t n_defrag;                /* HeuristicRXFrontListDefragmentation X points (sorted) */
+    double defrag_x[SCORE_MAX_TABLE];
+    /* MaterialProperties */
+    double G0, dGdt, bZeroCelsius, Tmelt;
+    /* BoundaryMobilityModel */
+    int32_t mobility_model;
+    double LAGBm0, LAGBHact, HAGBm0, HAGBHact, GSm0, GSHact;
+    double RH_HAGBm0, RH_HAGBHact, RH_cut, RH_trans, RH_exponent;
+    /* RecoveryParameter */
+    int32_t recovery_model;
+    double VacancyDiffD0, VacancyDiffHact, SoluteDiffD0, SoluteDiffHact, SoluteLsPropFactor, SoluteConcentration;
+    double NesAlpha3, NesKappa2, NesC3, NesC4, NesC5;
+    double recovery_k;                /* k [1/s] of rho(t)=rho0/(1+k t) (SCORE_RECOVERY_HYPERBOLIC) */
+    /* DragParameter / EvoMicrochemistry */
+    int32_t zener_model;
+    double zener_alpha, zener_gamma;
+    uint32_t n_zener;
+    double zener_time[SCORE_MAX_TABLE], zener_fr[SCORE_MAX_TABLE];
+    /* AnnealingSchedule (K) */
+    uint32_t n_schedule;
+    double sched_time[SCORE_MAX_TABLE], sched_temp[SCORE_MAX_TABLE];
+    /* GB300 build options (no .uds keyword) */
+    int32_t boundary;                 /* SCORE_BOUNDARY_* */
+    int32_t precision;                /* SCORE_PRECISION_* */
+    int32_t border_policy;            /* SCORE_BORDER_* */
+    int32_t reserved;
+} score_params;
+
+/* per-step scalars (the master block of solve_RXGROWTH, SCORE_Kernel.cpp:6688-6740) */
+typedef struct score_step_stats {
+    uint32_t step;        /* steps completed so far */
+    uint32_t n_nuclei;    /* nuclei placed before this step (time-dependent nucleation) */
+    double t;             /* time after this step [s] (t += dt) */
+    double dt;            /* dt for the NEXT step */
+    double dt_used;       /* dt this step integrated with */
+    double Xcells;        /* fully recrystallized cells */
+    double X;             /* Xcells / N */
+    uint64_t Sv;          /* ACTIVE front cells updated this step (Inside + Border) */
+    uint64_t n_full;      /* cells that completed this step and infected their neighbours */
+    uint64_t n_new;       /* cells newly infected this step */
+    double Pmax;          /* running max mobility weight P */
+    double rhomax;        /* max rho over deformed grains with cells left */
+    double dXstep;        /* sum of fill increments (observation; order differs from the reference) */
+    uint32_t next_never[2];  /* Inside, Border: slots ever used */
+    uint32_t n_recycled[2];  /* Inside, Border: recycle-list lengths this step */
+    uint32_t p_misses;       /* mobility weights computed on the host this step */
+    uint32_t reserved;
+} score_step_stats;
+
+/* library */
+int  score_abi_version(void);
+const char* score_status_string(int status);
+
+/* .uds input file -> params (ensembleHdl::init_parameter, src/SCORE_Kernel.cpp:1542-1625) */
+int  score_params_default(score_params* out);
+int  score_uds_read(const char* path, score_params* out);
+
+/* context: caHdl + its caregionMemHdl fronts (src/SCORE_Kernel.h:1008-1347, 1403-1584) */
+typedef struct score_ctx score_ctx;
+int  score_create(score_ctx** out, const score_params* p, int device);
+void score_destroy(score_ctx* ctx);
+const char* score_last_error(const score_ctx* ctx);
+
+/*
+ * Load one domain (replaces solve_SYNTHESIZE_DEFORMATIONSTRUCTURE + nucleation
+ * modelling + solve_REPLACE_CA_STRUCTURE, src/SCORE_Kernel.cpp:6142,6321,6353):
+ *   grid       nx*ny*nz deformed-grain ids (x fastest), each < ndefg
+ *   defg_quat  ndefg x 4 unit quaternions (q0,q1,q2,q3), defg_rho0 ndefg [1/m^2]
+ *   rxg_quat   nrxg x 4, rxg_site nrxg linear sites x+y*nx+z*nx*ny, rxg_tincub nrxg [s] (NULL = all 0)
+ *   ptable     optional nrxg*ndefg mobility weights P(rxg,defg) (row = rxg); NULL = computed on the
+ *              host in FP64 on first use (caregionMemHdl::reg_calc_mobilityweight, SCORE_Kernel.cpp:2460)
+ */
+int  score_load_domain(score_ctx* ctx, const uint32_t* grid, const double* defg_quat, const double* defg_rho0,
+                       uint32_t ndefg, const double* rxg_quat, const uint32_t* rxg_site, const double* rxg_tincub,
+                       uint32_t nrxg, const double* ptable);
+
+/* site-saturated placement of every nucleus with tincub <= t, in rxg order
+ * (caHdl::ompshar_sim_myCA_sitesaturatedNucleation, src/SCORE_GrowthMachine.cpp:50-189) */
+int  score_place_nuclei(score_ctx* ctx, uint32_t* n_placed);
+
+/* one growth step: grow -> infect -> reduce -> t+=dt -> physics -> dt
+ * (loop body of solve_RXGROWTH, src/SCORE_Kernel.cpp:6617-6743) */
+int  score_step(score_ctx* ctx, score_step_stats* out);
+
+/* whole step loop until the reference's stop rule (SCORE_Kernel.cpp:6619):
+ * Xcells>=N || X>x_target || step>NMAX || t>t_end || t>TIMEMAX.  x_target<0 uses params.xmax.
+ * trace (may be NULL) receives up to trace_cap rows; *n_steps the number of steps run. */
+int  score_run_until(score_ctx* ctx, double x_target, score_step_stats* trace, uint32_t trace_cap, uint32_t* n_steps);
+
+/* current scalars (step, t, dt, X, ...) without advancing */
+int  score_get_stats(score_ctx* ctx, score_step_stats* out);
+
+/* final grain labels by the clarify rule (ompcrit_clarify_status_infectedcells,
+ * src/SCORE_Io_Characterization.cpp:925-1000): deformed id, or ndefg+rxg for
+ * recrystallized cells and front cells with fill >= 0.5 */
+int  score_export_labels(score_ctx* ctx, uint32_t* labels);
+
+/* per-grain cell counts (caHdl::synchronize_*_counts, SCORE_Kernel.cpp:5983-6028) */
+int  score_grain_counts(score_ctx* ctx, uint32_t* rxg_counts, uint32_t* defg_counts);
+
+/* device-side timing of the last run_until: kernel-only ms, ms of the dominant
+ * (grow) kernel, its launches, and the algorithmic bytes those launches moved */
+typedef struct score_timing {
+    double total_ms, grow_ms, claim_ms, commit_ms, host_ms;
+    uint64_t grow_launches;
+    double grow_bytes;      /* algorithmic bytes of all grow launches */
+    double step_bytes;      /* algorithmic bytes of all kernels */
+    uint64_t kernel_launches;
+} score_timing;
+int  score_get_timing(score_ctx* ctx, score_timing* out);
+
+/* FP64 mobility weight P(rxg,defg) on the host, the reference's formula
+ * (SCORE_Kernel.cpp:2460-2527, SCORE_Math.cpp:558-622,1067-1130) */
+int  score_mobility_weight(const score_params* p, const double* rxg_q, const double* defg_q, double* P);
+
+/*
+ * Deterministic synthetic domain (identical bits on x86-64 and aarch64): periodic
+ * Voronoi deformed grains (optionally anisotropic "pancake" metric), uniform or
+ * texture-clustered orientations, lognormal or bimodal rho, distinct nucleation
+ * sites (uniform or grain-boundary biased), Poisson incubation times.
+ */
+typedef struct score_gen_params {
+    uint32_t nx, ny, nz;
+    uint32_t ngrains, nnuclei;
+    uint64_t seed;
+    double rho_mean, rho_sigma;        /* lognormal: mean and sigma of ln(rho) */
+    int32_t rho_mode;                  /* 0 lognormal, 1 bimodal (rho_lo/rho_hi, 50/50) */
+    double rho_lo, rho_hi;
+    double aspect[3];                  /* Voronoi metric scale per axis (1,1,1 = isotropic) */
+    int32_t ori_mode;                  /* 0 uniform, 1 clustered around ncomp components */
+    uint32_t ncomp;
+    double scatter_deg;                /* Gaussian scatter around components */
+    int32_t site_mode;                 /* 0 uniform, 1 grain-boundary biased */
+    double gb_fraction;                /* fraction of nuclei forced onto boundary cells (site_mode 1) */
+    double nucleation_rate;            /* >0: Poisson incubation times at this rate [1/s]; 0: all 0 */
+} score_gen_params;
+int  score_gen_default(score_gen_params* out);
+int  score_generate_domain(const score_gen_params* g, uint32_t* grid, double* defg_quat, double* defg_rho0,
+                           double* rxg_quat, uint32_t* rxg_site, double* rxg_tincub);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

@@ -1,0 +1,148 @@
+"""CPU oracle of the SCORE growth step — TEST INFRASTRUCTURE ONLY.
+
+Two checkers live here; only tests/, __graft_entry__.smoke() and bench.py's CPU
+baseline use them, and never as the thing measured or shipped:
+
+* ``run`` — the plain-C restatement in score_oracle.c (single-threaded FP64).
+* ``run_ref`` — the SCORE reference itself, compiled from its own sources by
+  oracle/ref/Makefile into oracle/_ref/ (only where the reference sources exist),
+  driven by oracle/ref/score_ref_driver.cpp.
+
+The restatement is pinned against the reference run here and against the
+golden fixtures in tests/golden/ that the reference produced.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+import subprocess
+import tempfile
+from pathlib import Path
+
+import numpy as np
+
+HERE = Path(__file__).resolve().parent
+BUILD = HERE / "_build"
+REFOUT = HERE / "_ref"
+REFERENCE_SRC = Path(os.environ.get("SCORE_REFERENCE", "/root/reference"))
+
+STEP_DTYPE = np.dtype([("step", "<u4"), ("n_nuclei", "<u4"), ("t", "<f8"), ("dt", "<f8"), ("dt_used", "<f8"),
+                       ("Xcells", "<f8"), ("X", "<f8"), ("Sv", "<u8"), ("n_full", "<u8"), ("n_new", "<u8"),
+                       ("Pmax", "<f8"), ("rhomax", "<f8"), ("dXstep", "<f8"), ("next_never", "<u4", 2),
+                       ("n_recycled", "<u4", 2)])
+REF_STEP_DTYPE = np.dtype([("step", "<u4"), ("pad", "<u4"), ("t", "<f8"), ("dt", "<f8"), ("Xcells", "<f8"),
+                           ("Sv", "<u8"), ("nfull", "<u8"), ("Pmax", "<f8"), ("rhomax", "<f8"), ("dXstep", "<f8")])
+
+
+class OracleOut(C.Structure):
+    _fields_ = [("n_steps", C.c_uint32), ("status", C.c_int), ("dt0", C.c_double), ("Pmax0", C.c_double),
+                ("n_nuclei", C.c_uint32), ("seconds", C.c_double)]
+
+
+def build_oracle(force: bool = False) -> Path:
+    out = BUILD / "liboracle.so"
+    src = [HERE / "score_oracle.c", HERE / "score_oracle.h", HERE.parent / "include" / "score_gb300.h"]
+    if not force and out.exists() and all(out.stat().st_mtime >= s.stat().st_mtime for s in src):
+        return out
+    BUILD.mkdir(exist_ok=True)
+    tmp = out.with_suffix(".tmp.so")
+    subprocess.run(["gcc", "-O2", "-ffp-contract=off", "-fPIC", "-shared", "-std=gnu11", str(HERE / "score_oracle.c"),
+                    "-o", str(tmp), "-lm"], check=True)
+    os.replace(tmp, out)
+    return out
+
+
+def reference_available() -> bool:
+    return (REFERENCE_SRC / "src" / "SCORE_Kernel.cpp").exists() or (REFOUT / "score_ref_driver").exists()
+
+
+def build_ref() -> Path | None:
+    """Compile the reference harness (only where the reference sources exist)."""
+    exe = REFOUT / "score_ref_driver"
+    if not (REFERENCE_SRC / "src" / "SCORE_Kernel.cpp").exists():
+        return exe if exe.exists() else None
+    subprocess.run(["make", "-s", "-C", str(HERE / "ref"), f"REF={REFERENCE_SRC}", f"-j{os.cpu_count() or 4}"], check=True)
+    return exe
+
+
+_lib = None
+
+
+def _load():
+    global _lib
+    if _lib is None:
+        lib = C.CDLL(str(build_oracle()))
+        lib.oracle_run.restype = C.c_int
+        lib.oracle_mobility_weight.restype = C.c_double
+        lib.oracle_mobility_weight.argtypes = [C.c_void_p, C.c_void_p, C.c_void_p]
+        _lib = lib
+    return _lib
+
+
+def _p(a):
+    return None if a is None else a.ctypes.data_as(C.c_void_p)
+
+
+def run(params, domain, ptable=None, x_target: float = -1.0, max_steps: int = 0, trace_cap: int = 200000) -> dict:
+    """Run nucleation + growth on the CPU restatement; returns trace, labels, counts, summary."""
+    lib = _load()
+    d = domain
+    trace = np.zeros(trace_cap, dtype=STEP_DTYPE)
+    labels = np.empty(d.ncells, dtype=np.uint32)
+    rc = np.empty(max(d.nrxg, 1), dtype=np.uint32)
+    dc = np.empty(d.ndefg, dtype=np.uint32)
+    out = OracleOut()
+    arrs = [np.ascontiguousarray(x) for x in (d.grid, d.defg_quat, d.defg_rho0, d.rxg_quat, d.rxg_site, d.rxg_tincub)]
+    pt = None if ptable is None else np.ascontiguousarray(ptable, dtype=np.float64)
+    s = lib.oracle_run(C.byref(params), _p(arrs[0]), _p(arrs[1]), _p(arrs[2]), C.c_uint32(d.ndefg), _p(arrs[3]), _p(arrs[4]),
+                       _p(arrs[5]), C.c_uint32(d.nrxg), _p(pt), C.c_double(x_target), C.c_uint32(max_steps), _p(trace),
+                       C.c_uint32(trace_cap), _p(labels), _p(rc), _p(dc), C.byref(out))
+    n = min(out.n_steps, trace_cap)
+    return {"status": s, "trace": trace[:n], "labels": labels, "rxg_counts": rc[: d.nrxg], "defg_counts": dc,
+            "dt0": out.dt0, "Pmax0": out.Pmax0, "n_nuclei": out.n_nuclei, "seconds": out.seconds, "n_steps": out.n_steps}
+
+
+def mobility_weight(params, qr, qd) -> float:
+    lib = _load()
+    a = np.ascontiguousarray(qr, dtype=np.float64)
+    b = np.ascontiguousarray(qd, dtype=np.float64)
+    return lib.oracle_mobility_weight(C.byref(params), _p(a), _p(b))
+
+
+def _read_kv(path: Path) -> dict:
+    kv = {"rxg": {}, "defg": {}}
+    for line in path.read_text().splitlines():
+        parts = line.split()
+        if len(parts) == 3 and parts[0] in ("rxg", "defg"):
+            kv[parts[0]][int(parts[1])] = int(parts[2])
+        elif len(parts) == 2:
+            kv[parts[0]] = parts[1]
+    return kv
+
+
+def run_ref(mode: str, uds_path, domain, workdir=None, threads: int = 1, timeout: float = 3600) -> dict:
+    """Run the reference harness in `mode` (loop | asis | ptab) on `domain`."""
+    exe = build_ref()
+    if exe is None or not exe.exists():
+        raise RuntimeError("reference harness unavailable (no reference sources and no prebuilt driver)")
+    wd = Path(workdir or tempfile.mkdtemp(prefix="scoreref_"))
+    wd.mkdir(parents=True, exist_ok=True)
+    scdm = domain.write_scdm(wd / "domain.scdm")
+    prefix = wd / "out"
+    env = dict(os.environ, OMP_NUM_THREADS=str(threads))
+    r = subprocess.run([str(exe), mode, str(uds_path), str(scdm), str(prefix)], cwd=wd, env=env, capture_output=True,
+                       text=True, timeout=timeout)
+    if r.returncode != 0:
+        raise RuntimeError(f"reference harness failed ({r.returncode}): {r.stderr[-2000:]}")
+    res = {"workdir": wd}
+    if mode == "ptab":
+        n = domain.nrxg * domain.ndefg
+        res["ptab"] = np.fromfile(f"{prefix}.ptab", dtype=np.float64, count=n).reshape(domain.nrxg, domain.ndefg)
+        res["ptabnuc"] = np.fromfile(f"{prefix}.ptabnuc", dtype=np.float64, count=n).reshape(domain.nrxg, domain.ndefg)
+    elif mode == "asis":
+        res.update(_read_kv(Path(f"{prefix}.asis")))
+    else:
+        res.update(_read_kv(Path(f"{prefix}.summary")))
+        res["trace"] = np.fromfile(f"{prefix}.trace", dtype=REF_STEP_DTYPE)
+        res["labels"] = np.fromfile(f"{prefix}.labels", dtype=np.uint32)
+    return res

@@ -1,0 +1,863 @@
+// score_gb300 growth context: device memory layout, the per-step launch sequence
+// and the host FP64 master-thread work (dt, physics, P on first use).
+//
+// HBM layout of one domain (N cells, list capacities cap_I = N, cap_B = N or the
+// reference's 2(xy+xz+yz) Border limit):
+//   grid   u32[N]   deformed id < ndefg | CURRENTLY_INFECTED | ndefg + rxg
+//   claim  u32[N]   attempt ordinal of the first infection of this step (0xFFFFFFFF free)
+//   front list L (SoA, slot-indexed): fill f64|f32, [comp f32], P f64|f32, defg u32,
+//          rxg u32, xyz u32, dir u8  -> 29 B (FP64) / 25 B (FP32) per slot
+//   full_L u32[cap_L], recyc_L u32[reccap_L]  (ordered lists rebuilt every step)
+//   ptab   u64[nrxg*ndefg] mobility weights P(rxg,defg), filled on first use
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <atomic>
+#include <chrono>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <string>
+#include <thread>
+#include <vector>
+#include <unordered_set>
+#include <cstddef>
+
+#include "../../include/score_gb300.h"
+#include "device_common.cuh"
+#include "growth_kernels.cuh"
+#include "host_model.h"
+
+using namespace score;
+
+namespace {
+
+// ------------------------------------------------------------------ small kernels
+__global__ void k_count_defg(const uint32_t* grid, uint64_t n, uint32_t ndefg, uint32_t* cnt, uint32_t* err) {
+    for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < n; i += (uint64_t)gridDim.x * blockDim.x) {
+        uint32_t g = grid[i];
+        if (g < ndefg) atomicAdd(&cnt[g], 1u);
+        else atomicOr(err, kErrBounds);
+    }
+}
+
+__global__ void k_gather_u32(const uint32_t* src, const uint32_t* idx, uint32_t n, uint32_t* out) {
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) out[i] = src[idx[i]];
+}
+
+struct NucRec { uint32_t list, slot, site, rxg, defg, pad; double P; };
+
+template <bool FP32>
+__global__ void k_place_nuclei(DomainArgs a, const NucRec* rec, uint32_t n) {
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        const NucRec r = rec[i];
+        const DFront& f = a.f[r.list];
+        if (!FP32) { ((double*)f.fill)[r.slot] = 1.0; ((double*)f.P)[r.slot] = r.P; }
+        else { ((float*)f.fill)[r.slot] = 1.0f; f.comp[r.slot] = 0.0f; ((float*)f.P)[r.slot] = (float)r.P; }
+        f.dir[r.slot] = 26;
+        f.defg[r.slot] = r.defg;
+        f.rxg[r.slot] = r.rxg;
+        f.xyz[r.slot] = r.site;
+        a.grid[r.site] = kCurrentlyInfected;
+    }
+}
+
+__global__ void k_fill_ptab(unsigned long long* ptab, const unsigned long long* idx, const double* val, uint32_t n) {
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
+        ptab[idx[i]] = (unsigned long long)__double_as_longlong(val[i]);
+}
+
+template <bool FP32>
+__global__ void k_fix_pending(DomainArgs a, uint32_t n) {
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        const uint32_t q = a.pending[i];
+        const DFront& f = a.f[q >> 31];
+        const uint32_t s = q & 0x7FFFFFFFu;
+        const double P = __longlong_as_double((long long)a.ptab[(unsigned long long)f.rxg[s] * a.ndefg + f.defg[s]]);
+        if (!FP32) ((double*)f.P)[s] = P;
+        else ((float*)f.P)[s] = (float)P;
+    }
+}
+
+template <bool FP32>
+__global__ void k_labels_front(DomainArgs a, int L, uint32_t n, uint32_t* lab) {
+    const DFront& f = a.f[L];
+    for (uint32_t s = blockIdx.x * blockDim.x + threadIdx.x; s < n; s += gridDim.x * blockDim.x) {
+        if (f.dir[s] == kInactive) continue;
+        bool rx;
+        if (!FP32) rx = !(((const double*)f.fill)[s] < 0.5);
+        else rx = !((((const float*)f.fill)[s] - f.comp[s]) < 0.5f);
+        lab[f.xyz[s]] = rx ? a.ndefg + f.rxg[s] : f.defg[s];
+    }
+}
+
+// stable compaction of ACTIVE slots of list L into scratch arrays (ompshar_defragmentation,
+// SCORE_Kernel.cpp:3877-3937); counter A = actives, B unused
+template <bool FP32>
+__global__ void __launch_bounds__(kBlock) k_defrag_compact(DomainArgs a, int L, uint32_t n, DFront scratch,
+                                                           unsigned long long* status, uint32_t* ticket, uint32_t* out_count) {
+    constexpr int ITEMS = 8;
+    constexpr uint32_t TILE = kBlock * ITEMS;
+    const DFront fr = a.f[L];
+    const uint32_t ntiles = (n + TILE - 1) / TILE;
+    __shared__ uint32_t s_tile, s_ex, s_cntA[ITEMS * kWarps], s_cntB[ITEMS * kWarps];
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    for (;;) {
+        if (threadIdx.x == 0) s_tile = atomicAdd(ticket, 1u);
+        __syncthreads();
+        const uint32_t tile = s_tile;
+        if (tile >= ntiles) break;
+        const uint32_t base = tile * TILE;
+        uint32_t am[ITEMS];
+#pragma unroll
+        for (int k = 0; k < ITEMS; ++k) {
+            const uint32_t s = base + (uint32_t)(k * kBlock) + threadIdx.x;
+            am[k] = __ballot_sync(0xFFFFFFFFu, s < n && fr.dir[s] != kInactive);
+            if (lane == 0) { s_cntA[k * kWarps + warp] = __popc(am[k]); s_cntB[k * kWarps + warp] = 0; }
+        }
+        __syncthreads();
+        if (warp == 0) {
+            uint32_t tA, tB;
+            scan64_pair(s_cntA, s_cntB, tA, tB);
+            if (lane == 0) {
+                uint32_t eA, eB;
+                lookback2(status, tile, tA, 0, eA, eB, &a.st->err);
+                s_ex = eA;
+                if (tile == ntiles - 1) *out_count = eA + tA;
+            }
+        }
+        __syncthreads();
+        const uint32_t lt = lanemask_lt();
+#pragma unroll
+        for (int k = 0; k < ITEMS; ++k) {
+            if (!((am[k] >> lane) & 1u)) continue;
+            const uint32_t s = base + (uint32_t)(k * kBlock) + threadIdx.x;
+            const uint32_t r = s_ex + s_cntA[k * kWarps + warp] + __popc(am[k] & lt);
+            if (!FP32) {
+                ((double*)scratch.fill)[r] = ((const double*)fr.fill)[s];
+                ((double*)scratch.P)[r] = ((const double*)fr.P)[s];
+            } else {
+                ((float*)scratch.fill)[r] = ((const float*)fr.fill)[s];
+                scratch.comp[r] = fr.comp[s];
+                ((float*)scratch.P)[r] = ((const float*)fr.P)[s];
+            }
+            scratch.defg[r] = fr.defg[s]; scratch.rxg[r] = fr.rxg[s]; scratch.xyz[r] = fr.xyz[s]; scratch.dir[r] = fr.dir[s];
+        }
+        __syncthreads();
+    }
+}
+
+__global__ void k_first_inactive(const uint8_t* dir, uint32_t lo, uint32_t hi, uint32_t* out) {
+    for (uint32_t s = lo + blockIdx.x * blockDim.x + threadIdx.x; s < hi; s += gridDim.x * blockDim.x)
+        if (dir[s] == kInactive) atomicMin(out, s);
+}
+
+inline uint32_t blocks_for(uint64_t work, int sms, int per_sm = 8) {
+    uint64_t b = (work + kBlock - 1) / kBlock;
+    uint64_t cap = (uint64_t)sms * per_sm;
+    if (b > cap) b = cap;
+    if (b < 1) b = 1;
+    return (uint32_t)b;
+}
+
+template <typename T>
+cudaError_t dalloc(T** p, size_t count) {
+    return cudaMalloc((void**)p, std::max<size_t>(count, 1) * sizeof(T));
+}
+
+}  // namespace
+
+// ------------------------------------------------------------------ context
+struct score_ctx {
+    score_params prm{};
+    int device = 0;
+    int sms = 1;
+    cudaStream_t stream = nullptr;
+    std::string err;
+    Physics ph;
+
+    uint32_t nx = 0, ny = 0, nz = 0;
+    uint64_t N = 0;
+    uint32_t ndefg = 0, nrxg = 0;
+    bool loaded = false, fp32 = false, failed = false;
+    std::vector<double> defg_q, rxg_q, rho0, rho, tincub;
+    std::vector<uint32_t> site;
+    std::vector<uint8_t> placed;
+    std::vector<uint32_t> nuc_order;   // rxg ids sorted by (tincub, id)
+    size_t nuc_pos = 0;                // nuc_order[0, nuc_pos) already considered
+    std::vector<uint32_t> defg_cnt_host;
+    std::vector<double> user_ptab;
+    std::vector<double> pforce_host;
+
+    DomainArgs a{};
+    DevState* d_state = nullptr;
+    DevState* h_state = nullptr;  // pinned
+    unsigned long long* d_status[3] = {nullptr, nullptr, nullptr};
+    size_t status_words[3] = {0, 0, 0};
+    uint32_t* d_tickets = nullptr;
+    double* d_pforce = nullptr;
+    float* d_pforce32 = nullptr;
+    uint32_t* d_u32tmp = nullptr;
+    size_t u32tmp_cap = 0;
+    void* d_stage = nullptr;
+    size_t stage_cap = 0;
+    DFront scratch{};
+    uint32_t scratch_cap = 0;
+
+    double Xcells = 0.0;
+    uint32_t step = 0, defrag_cnt = 0, n_nuclei = 0;
+    uint32_t next_never[2] = {0, 0}, high_water[2] = {0, 0};
+    score_step_stats last{};
+
+    cudaEvent_t ev[4] = {nullptr, nullptr, nullptr, nullptr};
+    score_timing tm{};
+    uint64_t launches = 0;
+
+    ~score_ctx() { release(); }
+    void release();
+    int fail(int code, const std::string& msg) { err = msg; return code; }
+    int cuda_fail(cudaError_t e, const char* what) {
+        err = std::string(what) + ": " + cudaGetErrorString(e);
+        return SCORE_ERR_CUDA;
+    }
+    bool stage(size_t bytes) {
+        if (bytes <= stage_cap) return true;
+        if (d_stage) cudaFree(d_stage);
+        d_stage = nullptr; stage_cap = 0;
+        if (cudaMalloc(&d_stage, bytes) != cudaSuccess) return false;
+        stage_cap = bytes;
+        return true;
+    }
+};
+
+void score_ctx::release() {
+    if (device >= 0) cudaSetDevice(device);
+    void* ptrs[] = {a.f[0].fill, a.f[0].comp, a.f[0].P, a.f[0].defg, a.f[0].rxg, a.f[0].xyz, a.f[0].dir, a.f[0].full, a.f[0].recyc,
+                    a.f[1].fill, a.f[1].comp, a.f[1].P, a.f[1].defg, a.f[1].rxg, a.f[1].xyz, a.f[1].dir, a.f[1].full, a.f[1].recyc,
+                    a.grid, a.claim, a.ptab, a.defg_cnt, a.rxg_cnt, a.depleted, a.miss, a.pending,
+                    d_state, d_status[0], d_status[1], d_status[2], d_tickets, d_pforce, d_pforce32, d_u32tmp, d_stage,
+                    scratch.fill, scratch.comp, scratch.P, scratch.defg, scratch.rxg, scratch.xyz, scratch.dir};
+    for (void* p : ptrs) if (p) cudaFree(p);
+    a = DomainArgs{};
+    scratch = DFront{};
+    d_state = nullptr; d_tickets = nullptr; d_pforce = nullptr; d_pforce32 = nullptr; d_u32tmp = nullptr; d_stage = nullptr;
+    for (auto& s : d_status) s = nullptr;
+    if (h_state) cudaFreeHost(h_state);
+    h_state = nullptr;
+    for (auto& e : ev) if (e) { cudaEventDestroy(e); e = nullptr; }
+    if (stream) cudaStreamDestroy(stream);
+    stream = nullptr;
+}
+
+// ------------------------------------------------------------------ helpers
+namespace {
+
+constexpr uint32_t kTileGrow = kBlock * 8;
+
+int upload_pforce(score_ctx* c) {
+    // driving force per deformed grain, the grow step's p (SCORE_Kernel.cpp:4082)
+    std::vector<double> pf(c->ndefg);
+    for (uint32_t g = 0; g < c->ndefg; ++g) pf[g] = c->ph.driving_force(c->rho[g]);
+    if (pf == c->pforce_host) return SCORE_OK;
+    c->pforce_host = pf;
+    cudaError_t e = cudaMemcpyAsync(c->d_pforce, pf.data(), pf.size() * 8, cudaMemcpyHostToDevice, c->stream);
+    if (e != cudaSuccess) return c->cuda_fail(e, "upload pforce");
+    if (c->fp32) {
+        std::vector<float> p32(pf.begin(), pf.end());
+        e = cudaMemcpyAsync(c->d_pforce32, p32.data(), p32.size() * 4, cudaMemcpyHostToDevice, c->stream);
+        if (e != cudaSuccess) return c->cuda_fail(e, "upload pforce32");
+        e = cudaStreamSynchronize(c->stream);  // p32 is a temporary
+        if (e != cudaSuccess) return c->cuda_fail(e, "sync");
+    } else {
+        e = cudaStreamSynchronize(c->stream);
+        if (e != cudaSuccess) return c->cuda_fail(e, "sync");
+    }
+    return SCORE_OK;
+}
+
+void set_mobility_args(score_ctx* c) {
+    c->a.mLAGB = c->ph.mLAGB; c->a.mHAGB = c->ph.mHAGB; c->a.mGS = c->ph.mGS; c->a.mRH = c->ph.mRHHAGB;
+    c->a.dt = c->ph.dt; c->a.cinv = (1.0 / c->prm.cellsize);
+    c->a.mLAGB32 = (float)c->ph.mLAGB; c->a.mHAGB32 = (float)c->ph.mHAGB; c->a.mGS32 = (float)c->ph.mGS;
+    c->a.mRH32 = (float)c->ph.mRHHAGB; c->a.dtc32 = (float)(c->ph.dt * (1.0 / c->prm.cellsize));
+}
+
+double weight_of(score_ctx* c, uint32_t r, uint32_t g) {
+    if (!c->user_ptab.empty()) return c->user_ptab[(size_t)r * c->ndefg + g];
+    return mobility_weight(c->prm, &c->rxg_q[4 * (size_t)r], &c->defg_q[4 * (size_t)g]);
+}
+
+// compute P for a list of table indices on the host, in parallel for large batches
+void resolve_weights(score_ctx* c, const std::vector<unsigned long long>& idx, std::vector<double>& val) {
+    val.resize(idx.size());
+    auto work = [&](size_t lo, size_t hi) {
+        for (size_t i = lo; i < hi; ++i) val[i] = weight_of(c, (uint32_t)(idx[i] / c->ndefg), (uint32_t)(idx[i] % c->ndefg));
+    };
+    size_t n = idx.size();
+    unsigned nth = std::max(1u, std::min(32u, std::thread::hardware_concurrency()));
+    if (n < 4096 || nth == 1) { work(0, n); return; }
+    std::vector<std::thread> th;
+    for (unsigned t = 0; t < nth; ++t) th.emplace_back(work, n * t / nth, n * (t + 1) / nth);
+    for (auto& t : th) t.join();
+}
+
+int check_device_errors(score_ctx* c, uint32_t flags) {
+    if (!flags) return SCORE_OK;
+    if (flags & kErrTimeout) return c->fail(SCORE_ERR_TIMEOUT, "a bounded device wait gave up (look-back scan)");
+    if (flags & kErrKeyLimit) return c->fail(SCORE_ERR_KEYLIMIT, "more than 2^32-1 infection attempts in one step");
+    if (flags & kErrBorderRef) return c->fail(SCORE_ERR_BORDER_CAPACITY, "Border list exceeded 2(xy+xz+yz) slots (the reference writes out of bounds here)");
+    if (flags & kErrCapacity) return c->fail(SCORE_ERR_CAPACITY, "front list capacity exceeded");
+    if (flags & kErrMissCap) return c->fail(SCORE_ERR_CAPACITY, "pending mobility-weight list capacity exceeded");
+    return c->fail(SCORE_ERR_STATE, "device bounds check failed (corrupt domain?)");
+}
+
+// site-saturated placement of nuclei with tincub <= t, rxg order
+// (ompshar_sim_myCA_sitesaturatedNucleation / infect_JuvenileNucleation, SCORE_GrowthMachine.cpp:50-189)
+int place_nuclei_upto(score_ctx* c, double tnow, uint32_t* nplaced) {
+    std::vector<uint32_t> cand;
+    while (c->nuc_pos < c->nuc_order.size() && c->tincub[c->nuc_order[c->nuc_pos]] <= tnow) cand.push_back(c->nuc_order[c->nuc_pos++]);
+    std::sort(cand.begin(), cand.end());  // the reference places nuclei in rxg order
+    if (nplaced) *nplaced = 0;
+    if (cand.empty()) return SCORE_OK;
+    const uint32_t n = (uint32_t)cand.size();
+    std::vector<uint32_t> sites(n), gval(n);
+    for (uint32_t i = 0; i < n; ++i) sites[i] = c->site[cand[i]];
+    if (!c->stage((size_t)n * 8)) return c->fail(SCORE_ERR_NOMEM, "staging buffer");
+    uint32_t* d_idx = (uint32_t*)c->d_stage;
+    uint32_t* d_out = d_idx + n;
+    cudaError_t e = cudaMemcpyAsync(d_idx, sites.data(), (size_t)n * 4, cudaMemcpyHostToDevice, c->stream);
+    if (e != cudaSuccess) return c->cuda_fail(e, "upload nucleus sites");
+    k_gather_u32<<<blocks_for(n, c->sms), kBlock, 0, c->stream>>>(c->a.grid, d_idx, n, d_out);
+    c->launches++;
+    e = cudaMemcpyAsync(gval.data(), d_out, (size_t)n * 4, cudaMemcpyDeviceToHost, c->stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(c->stream);
+    if (e != cudaSuccess) return c->cuda_fail(e, "gather nucleus sites");
+
+    std::vector<NucRec> recs;
+    std::unordered_set<uint32_t> taken;
+    std::vector<unsigned long long> pidx;
+    std::vector<double> pval;
+    const uint32_t nx = c->nx, ny = c->ny, nxy = nx * ny;
+    for (uint32_t i = 0; i < n; ++i) {
+        const uint32_t r = cand[i];
+        c->placed[r] = 1;
+        uint32_t g = gval[i];
+        if (taken.count(sites[i])) g = kCurrentlyInfected;
+        if (g >= c->ndefg) continue;  // site already infected or recrystallized: nucleus not placeable
+        const uint32_t s = sites[i];
+        const uint32_t z = s / nxy, y = (s - z * nxy) / nx, x = s - z * nxy - y * nx;
+        const bool inside = x > 0 && x < nx - 1 && y > 0 && y < ny - 1 && z > 0 && z < c->nz - 1;
+        const int L = inside ? 0 : 1;
+        const uint32_t slot = c->next_never[L];
+        if (slot >= c->a.f[L].cap) return c->fail(SCORE_ERR_CAPACITY, "front list capacity exceeded while placing nuclei");
+        if (L == 1 && c->prm.border_policy == SCORE_BORDER_REFERENCE_LIMIT && slot >= c->a.border_ref_cap)
+            return c->fail(SCORE_ERR_BORDER_CAPACITY, "Border list exceeded 2(xy+xz+yz) slots while placing nuclei");
+        c->next_never[L]++;
+        NucRec q{};
+        q.list = (uint32_t)L; q.slot = slot; q.site = s; q.rxg = r; q.defg = g;
+        q.P = weight_of(c, r, g);
+        if (q.P >= c->ph.Pmax) c->ph.Pmax = q.P;  // reg_myMobilityWeightMax, then the master's max
+        recs.push_back(q);
+        taken.insert(s);
+        pidx.push_back((unsigned long long)r * c->ndefg + g);
+        pval.push_back(q.P);
+        c->n_nuclei++;
+        if (nplaced) (*nplaced)++;
+    }
+    if (recs.empty()) return SCORE_OK;
+    const size_t nr = recs.size();
+    const size_t bytes = nr * sizeof(NucRec) + nr * 16;
+    if (!c->stage(bytes)) return c->fail(SCORE_ERR_NOMEM, "staging buffer");
+    NucRec* d_rec = (NucRec*)c->d_stage;
+    unsigned long long* d_pi = (unsigned long long*)(d_rec + nr);
+    double* d_pv = (double*)(d_pi + nr);
+    e = cudaMemcpyAsync(d_rec, recs.data(), nr * sizeof(NucRec), cudaMemcpyHostToDevice, c->stream);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(d_pi, pidx.data(), nr * 8, cudaMemcpyHostToDevice, c->stream);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(d_pv, pval.data(), nr * 8, cudaMemcpyHostToDevice, c->stream);
+    if (e != cudaSuccess) return c->cuda_fail(e, "upload nuclei");
+    if (c->fp32) k_place_nuclei<true><<<blocks_for(nr, c->sms), kBlock, 0, c->stream>>>(c->a, d_rec, (uint32_t)nr);
+    else k_place_nuclei<false><<<blocks_for(nr, c->sms), kBlock, 0, c->stream>>>(c->a, d_rec, (uint32_t)nr);
+    k_fill_ptab<<<blocks_for(nr, c->sms), kBlock, 0, c->stream>>>(c->a.ptab, d_pi, d_pv, (uint32_t)nr);
+    c->launches += 2;
+    e = cudaMemcpyAsync((char*)c->d_state + offsetof(DevState, next_never), c->next_never, 8, cudaMemcpyHostToDevice, c->stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(c->stream);
+    if (e != cudaSuccess) return c->cuda_fail(e, "place nuclei");
+    for (int L = 0; L < 2; ++L) c->high_water[L] = std::max(c->high_water[L], c->next_never[L]);
+    return SCORE_OK;
+}
+
+// ompshar_defragmentation, SCORE_Kernel.cpp:3877-3937, for one list
+int defragment(score_ctx* c, int L) {
+    const uint32_t n = c->next_never[L];
+    if (n == 0) return SCORE_OK;
+    DFront& fr = c->a.f[L];
+    if (c->scratch_cap < n) {
+        void* ptrs[] = {c->scratch.fill, c->scratch.comp, c->scratch.P, c->scratch.defg, c->scratch.rxg, c->scratch.xyz, c->scratch.dir};
+        for (void* p : ptrs) if (p) cudaFree(p);
+        c->scratch = DFront{};
+        const size_t fb = c->fp32 ? 4 : 8;
+        cudaError_t e = cudaMalloc(&c->scratch.fill, (size_t)n * fb);
+        if (e == cudaSuccess && c->fp32) e = cudaMalloc((void**)&c->scratch.comp, (size_t)n * 4);
+        if (e == cudaSuccess) e = cudaMalloc(&c->scratch.P, (size_t)n * fb);
+        if (e == cudaSuccess) e = dalloc(&c->scratch.defg, n);
+        if (e == cudaSuccess) e = dalloc(&c->scratch.rxg, n);
+        if (e == cudaSuccess) e = dalloc(&c->scratch.xyz, n);
+        if (e == cudaSuccess) e = dalloc(&c->scratch.dir, n);
+        if (e != cudaSuccess) return c->fail(SCORE_ERR_NOMEM, "defragmentation scratch");
+        c->scratch_cap = n;
+    }
+    uint32_t* d_cnt = c->d_u32tmp;
+    cudaMemsetAsync(d_cnt, 0, 8, c->stream);
+    cudaMemsetAsync(c->d_tickets, 0, 4 * sizeof(uint32_t), c->stream);
+    cudaMemsetAsync(c->d_status[0], 0, ((n + kTileGrow - 1) / kTileGrow) * 8, c->stream);
+    const uint32_t grid = blocks_for((uint64_t)n, c->sms, 4);
+    if (c->fp32) k_defrag_compact<true><<<grid, kBlock, 0, c->stream>>>(c->a, L, n, c->scratch, c->d_status[0], c->d_tickets, d_cnt);
+    else k_defrag_compact<false><<<grid, kBlock, 0, c->stream>>>(c->a, L, n, c->scratch, c->d_status[0], c->d_tickets, d_cnt);
+    c->launches++;
+    uint32_t active = 0;
+    cudaError_t e = cudaMemcpyAsync(&active, d_cnt, 4, cudaMemcpyDeviceToHost, c->stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(c->stream);
+    if (e != cudaSuccess) return c->cuda_fail(e, "defragment");
+    if (active == n) {
+        // no INACTIVE slot below next_never: the reference's scan for the first INACTIVE
+        // continues into slots left behind by earlier compactions
+        uint32_t first = c->high_water[L];
+        if (c->high_water[L] > n) {
+            e = cudaMemcpyAsync(d_cnt, &first, 4, cudaMemcpyHostToDevice, c->stream);
+            k_first_inactive<<<blocks_for(c->high_water[L] - n, c->sms), kBlock, 0, c->stream>>>(fr.dir, n, c->high_water[L], d_cnt);
+            c->launches++;
+            if (e == cudaSuccess) e = cudaMemcpyAsync(&first, d_cnt, 4, cudaMemcpyDeviceToHost, c->stream);
+            if (e == cudaSuccess) e = cudaStreamSynchronize(c->stream);
+            if (e != cudaSuccess) return c->cuda_fail(e, "defragment");
+        }
+        c->next_never[L] = std::max(n, first);
+    } else {
+        const size_t fb = c->fp32 ? 4 : 8;
+        e = cudaMemcpyAsync(fr.fill, c->scratch.fill, (size_t)active * fb, cudaMemcpyDeviceToDevice, c->stream);
+        if (e == cudaSuccess && c->fp32) e = cudaMemcpyAsync(fr.comp, c->scratch.comp, (size_t)active * 4, cudaMemcpyDeviceToDevice, c->stream);
+        if (e == cudaSuccess) e = cudaMemcpyAsync(fr.P, c->scratch.P, (size_t)active * fb, cudaMemcpyDeviceToDevice, c->stream);
+        if (e == cudaSuccess) e = cudaMemcpyAsync(fr.defg, c->scratch.defg, (size_t)active * 4, cudaMemcpyDeviceToDevice, c->stream);
+        if (e == cudaSuccess) e = cudaMemcpyAsync(fr.rxg, c->scratch.rxg, (size_t)active * 4, cudaMemcpyDeviceToDevice, c->stream);
+        if (e == cudaSuccess) e = cudaMemcpyAsync(fr.xyz, c->scratch.xyz, (size_t)active * 4, cudaMemcpyDeviceToDevice, c->stream);
+        if (e == cudaSuccess) e = cudaMemcpyAsync(fr.dir, c->scratch.dir, (size_t)active, cudaMemcpyDeviceToDevice, c->stream);
+        if (e != cudaSuccess) return c->cuda_fail(e, "defragment copy");
+        c->next_never[L] = active;
+    }
+    e = cudaMemcpyAsync((char*)c->d_state + offsetof(DevState, next_never), c->next_never, 8, cudaMemcpyHostToDevice, c->stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(c->stream);
+    if (e != cudaSuccess) return c->cuda_fail(e, "defragment");
+    return SCORE_OK;
+}
+
+// Size the look-back status buffers for the largest launch of each kind.
+int ensure_status(score_ctx* c, int which, size_t words) {
+    if (words <= c->status_words[which]) return SCORE_OK;
+    if (c->d_status[which]) cudaFree(c->d_status[which]);
+    c->d_status[which] = nullptr;
+    size_t w = std::max<size_t>(words, 1024);
+    if (cudaMalloc((void**)&c->d_status[which], w * 8) != cudaSuccess) return c->fail(SCORE_ERR_NOMEM, "status buffer");
+    c->status_words[which] = w;
+    return SCORE_OK;
+}
+
+}  // namespace
+
+// ------------------------------------------------------------------ C ABI
+extern "C" {
+
+int score_abi_version(void) { return SCORE_ABI_VERSION; }
+
+const char* score_status_string(int s) {
+    switch (s) {
+        case SCORE_OK: return "ok";
+        case SCORE_ERR_ARG: return "bad argument";
+        case SCORE_ERR_CUDA: return "CUDA error";
+        case SCORE_ERR_NOMEM: return "out of memory";
+        case SCORE_ERR_CAPACITY: return "front list capacity exceeded";
+        case SCORE_ERR_BORDER_CAPACITY: return "Border list exceeded the reference's 2(xy+xz+yz) slots";
+        case SCORE_ERR_TIMEOUT: return "bounded device wait gave up";
+        case SCORE_ERR_STATE: return "call out of sequence";
+        case SCORE_ERR_IO: return "input file error";
+        case SCORE_ERR_KEYLIMIT: return "too many infection attempts in one step";
+        case SCORE_ERR_NOT_BUILT: return "CUDA device unavailable";
+        default: return "unknown status";
+    }
+}
+
+int score_params_default(score_params* out) {
+    if (!out) return SCORE_ERR_ARG;
+    params_default(out);
+    return SCORE_OK;
+}
+
+int score_uds_read(const char* path, score_params* out) {
+    if (!path || !out) return SCORE_ERR_ARG;
+    char buf[512];
+    int s = uds_read(path, out, buf, sizeof buf);
+    if (s != SCORE_OK) fprintf(stderr, "score_uds_read: %s\n", buf);
+    return s;
+}
+
+int score_mobility_weight(const score_params* p, const double* rq, const double* dq, double* P) {
+    if (!p || !rq || !dq || !P) return SCORE_ERR_ARG;
+    *P = mobility_weight(*p, rq, dq);
+    return SCORE_OK;
+}
+
+const char* score_last_error(const score_ctx* c) { return c ? c->err.c_str() : "null context"; }
+
+int score_create(score_ctx** out, const score_params* p, int device) {
+    if (!out || !p) return SCORE_ERR_ARG;
+    *out = nullptr;
+    if (p->nx < 3 || p->ny < 3 || p->nz < 3) return SCORE_ERR_ARG;
+    const uint64_t N = (uint64_t)p->nx * p->ny * p->nz;
+    if (N >= 0x7FFFFFFFull) return SCORE_ERR_ARG;  // 31-bit slot counters in the look-back words
+    if (p->n_schedule < 1) return SCORE_ERR_ARG;
+    int ndev = 0;
+    if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) return SCORE_ERR_NOT_BUILT;
+    if (device < 0 || device >= ndev) return SCORE_ERR_ARG;
+    score_ctx* c = new score_ctx();
+    c->prm = *p;
+    c->device = device;
+    c->nx = p->nx; c->ny = p->ny; c->nz = p->nz; c->N = N;
+    c->fp32 = p->precision == SCORE_PRECISION_FP32_KAHAN;
+    cudaError_t e = cudaSetDevice(device);
+    if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking);
+    if (e == cudaSuccess) e = cudaDeviceGetAttribute(&c->sms, cudaDevAttrMultiProcessorCount, device);
+    for (auto& ev : c->ev) if (e == cudaSuccess) e = cudaEventCreate(&ev);
+    if (e == cudaSuccess) e = cudaMallocHost((void**)&c->h_state, sizeof(DevState));
+    if (e != cudaSuccess) { c->device = device; delete c; return SCORE_ERR_CUDA; }
+    *out = c;
+    return SCORE_OK;
+}
+
+void score_destroy(score_ctx* c) { delete c; }
+
+int score_load_domain(score_ctx* c, const uint32_t* grid, const double* defg_quat, const double* defg_rho0, uint32_t ndefg,
+                      const double* rxg_quat, const uint32_t* rxg_site, const double* rxg_tincub, uint32_t nrxg,
+                      const double* ptable) {
+    if (!c || !grid || !defg_quat || !defg_rho0 || !rxg_quat || !rxg_site || ndefg == 0) return SCORE_ERR_ARG;
+    if (c->loaded) return c->fail(SCORE_ERR_STATE, "domain already loaded");
+    if ((uint64_t)ndefg + nrxg >= 4096000000ull) return c->fail(SCORE_ERR_ARG, "too many grains");
+    const uint64_t N = c->N;
+    for (uint32_t r = 0; r < nrxg; ++r) if (rxg_site[r] >= N) return c->fail(SCORE_ERR_ARG, "nucleation site outside the domain");
+    cudaSetDevice(c->device);
+    c->ndefg = ndefg; c->nrxg = nrxg;
+    c->defg_q.assign(defg_quat, defg_quat + 4 * (size_t)ndefg);
+    c->rxg_q.assign(rxg_quat, rxg_quat + 4 * (size_t)nrxg);
+    c->rho0.assign(defg_rho0, defg_rho0 + ndefg);
+    c->rho = c->rho0;
+    c->site.assign(rxg_site, rxg_site + nrxg);
+    c->tincub.assign(nrxg, 0.0);
+    if (rxg_tincub) c->tincub.assign(rxg_tincub, rxg_tincub + nrxg);
+    c->placed.assign(nrxg, 0);
+    c->nuc_order.resize(nrxg);
+    for (uint32_t r = 0; r < nrxg; ++r) c->nuc_order[r] = r;
+    std::stable_sort(c->nuc_order.begin(), c->nuc_order.end(), [&](uint32_t x, uint32_t y) { return c->tincub[x] < c->tincub[y]; });
+    c->nuc_pos = 0;
+    if (ptable) c->user_ptab.assign(ptable, ptable + (size_t)nrxg * ndefg);
+
+    const score_params& p = c->prm;
+    DomainArgs& a = c->a;
+    a.nx = c->nx; a.ny = c->ny; a.nz = c->nz; a.nxy = c->nx * c->ny;
+    a.ndefg = ndefg; a.nrxg = nrxg;
+    a.border_ref_cap = 2 * ((c->nx * c->ny) + (c->nx * c->nz) + (c->ny * c->nz));
+    a.border_policy = p.border_policy; a.boundary = p.boundary; a.mobility_model = p.mobility_model;
+    // capacities: at most N infections ever happen, so N slots per list never overflow
+    const uint32_t capI = (uint32_t)N;
+    const uint32_t capB = (p.border_policy == SCORE_BORDER_REFERENCE_LIMIT) ? std::min<uint32_t>((uint32_t)N, a.border_ref_cap + 1) : (uint32_t)N;
+    // recycle-list caps (ompshar_init_myRXFront{Inside,Border}, SCORE_Kernel.cpp:3615, 3670)
+    const uint32_t recI = (uint32_t)(p.initial_cache * (double)N * p.maxfillperstep * kFullRecyclingFactor);
+    const uint32_t recB = (uint32_t)((double)a.border_ref_cap * p.maxfillperstep * kFullRecyclingFactor);
+    const uint32_t caps[2] = {capI, capB}, recs[2] = {recI, recB};
+    const size_t fb = c->fp32 ? 4 : 8;
+    cudaError_t e = cudaSuccess;
+    for (int L = 0; L < 2; ++L) {
+        DFront& f = a.f[L];
+        f.cap = caps[L]; f.reccap = recs[L];
+        if (e == cudaSuccess) e = cudaMalloc(&f.fill, (size_t)caps[L] * fb);
+        if (e == cudaSuccess && c->fp32) e = cudaMalloc((void**)&f.comp, (size_t)caps[L] * 4);
+        if (e == cudaSuccess) e = cudaMalloc(&f.P, (size_t)caps[L] * fb);
+        if (e == cudaSuccess) e = dalloc(&f.defg, caps[L]);
+        if (e == cudaSuccess) e = dalloc(&f.rxg, caps[L]);
+        if (e == cudaSuccess) e = dalloc(&f.xyz, caps[L]);
+        if (e == cudaSuccess) e = dalloc(&f.dir, caps[L]);
+        if (e == cudaSuccess) e = dalloc(&f.full, caps[L]);
+        if (e == cudaSuccess) e = dalloc(&f.recyc, recs[L]);
+        if (e == cudaSuccess) e = cudaMemsetAsync(f.dir, kInactive, caps[L], c->stream);
+    }
+    const size_t ptab_words = (size_t)nrxg * ndefg;
+    a.misscap = a.pendcap = (uint32_t)std::min<uint64_t>(N, 1ull << 25);
+    if (e == cudaSuccess) e = dalloc(&a.grid, N);
+    if (e == cudaSuccess) e = dalloc(&a.claim, N);
+    if (e == cudaSuccess) e = dalloc(&a.ptab, ptab_words);
+    if (e == cudaSuccess) e = dalloc(&a.defg_cnt, ndefg);
+    if (e == cudaSuccess) e = dalloc(&a.rxg_cnt, nrxg);
+    if (e == cudaSuccess) e = dalloc(&a.depleted, ndefg);
+    if (e == cudaSuccess) e = dalloc(&a.miss, a.misscap);
+    if (e == cudaSuccess) e = dalloc(&a.pending, a.pendcap);
+    if (e == cudaSuccess) e = dalloc(&c->d_state, 1);
+    if (e == cudaSuccess) e = dalloc(&c->d_tickets, 8);
+    if (e == cudaSuccess) e = dalloc(&c->d_pforce, ndefg);
+    if (e == cudaSuccess) e = dalloc(&c->d_pforce32, ndefg);
+    if (e == cudaSuccess) { e = dalloc(&c->d_u32tmp, 64); c->u32tmp_cap = 64; }
+    if (e != cudaSuccess) { c->release(); return c->fail(SCORE_ERR_NOMEM, std::string("device allocation: ") + cudaGetErrorString(e)); }
+    a.pforce = c->d_pforce; a.pforce32 = c->d_pforce32;
+    a.st = c->d_state;
+    // status words: tiles of the grow scans and of the commit scan (26 attempts per full cell)
+    int s = ensure_status(c, 0, (capI + kTileGrow - 1) / kTileGrow + 1);
+    if (s == SCORE_OK) s = ensure_status(c, 1, (capB + kTileGrow - 1) / kTileGrow + 1);
+    if (s == SCORE_OK) s = ensure_status(c, 2, (std::min<uint64_t>(26ull * N, 0xFFFFFFFFull) + kTileGrow - 1) / kTileGrow + 1);
+    if (s != SCORE_OK) { c->release(); return s; }
+
+    e = cudaMemcpyAsync(a.grid, grid, N * 4, cudaMemcpyHostToDevice, c->stream);
+    if (e == cudaSuccess) e = cudaMemsetAsync(a.claim, 0xFF, N * 4, c->stream);
+    if (e == cudaSuccess) {
+        if (ptable) e = cudaMemcpyAsync(a.ptab, ptable, ptab_words * 8, cudaMemcpyHostToDevice, c->stream);
+        else e = cudaMemsetAsync(a.ptab, 0xFF, std::max<size_t>(ptab_words, 1) * 8, c->stream);
+    }
+    if (e == cudaSuccess) e = cudaMemsetAsync(a.defg_cnt, 0, (size_t)ndefg * 4, c->stream);
+    if (e == cudaSuccess) e = cudaMemsetAsync(a.rxg_cnt, 0, std::max<size_t>(nrxg, 1) * 4, c->stream);
+    if (e == cudaSuccess) e = cudaMemsetAsync(c->d_state, 0, sizeof(DevState), c->stream);
+    if (e != cudaSuccess) return c->cuda_fail(e, "load domain");
+    // per-grain cell counts (solve_REPLACE_CA_STRUCTURE, SCORE_Kernel.cpp:6394-6400)
+    k_count_defg<<<blocks_for(N, c->sms, 16), kBlock, 0, c->stream>>>(a.grid, N, ndefg, a.defg_cnt, (uint32_t*)((char*)c->d_state + offsetof(DevState, err)));
+    c->launches++;
+    c->defg_cnt_host.assign(ndefg, 0);
+    e = cudaMemcpyAsync(c->defg_cnt_host.data(), a.defg_cnt, (size_t)ndefg * 4, cudaMemcpyDeviceToHost, c->stream);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(c->h_state, c->d_state, sizeof(DevState), cudaMemcpyDeviceToHost, c->stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(c->stream);
+    if (e != cudaSuccess) return c->cuda_fail(e, "count grains");
+    if (c->h_state->err) return c->fail(SCORE_ERR_ARG, "grid holds ids >= ndefg");
+
+    // start of solve_RXGROWTH (SCORE_Kernel.cpp:6513-6530): rho max, T, G/b, mobilities, dt0
+    Physics& ph = c->ph;
+    ph.init(&c->prm);
+    ph.rhomax = rhomax_of(c->rho, c->defg_cnt_host);
+    ph.update_temperature();
+    ph.update_atomistic();
+    ph.update_mobilities();
+    ph.dt = ph.dt_minimum();
+    s = upload_pforce(c);
+    if (s != SCORE_OK) return s;
+    c->Xcells = 0.0; c->step = 0; c->defrag_cnt = 0; c->n_nuclei = 0;
+    c->next_never[0] = c->next_never[1] = 0;
+    c->high_water[0] = c->high_water[1] = 0;
+    c->tm = score_timing{};
+    c->last = score_step_stats{};
+    c->last.dt = ph.dt;
+    c->last.rhomax = ph.rhomax;
+    c->loaded = true;
+    return SCORE_OK;
+}
+
+int score_place_nuclei(score_ctx* c, uint32_t* n_placed) {
+    if (!c) return SCORE_ERR_ARG;
+    if (!c->loaded) return c->fail(SCORE_ERR_STATE, "no domain loaded");
+    cudaSetDevice(c->device);
+    return place_nuclei_upto(c, c->ph.t, n_placed);
+}
+
+int score_step(score_ctx* c, score_step_stats* out) {
+    if (!c) return SCORE_ERR_ARG;
+    if (!c->loaded) return c->fail(SCORE_ERR_STATE, "no domain loaded");
+    if (c->failed) return SCORE_ERR_STATE;  // a device error left the front lists undefined
+    cudaSetDevice(c->device);
+    Physics& ph = c->ph;
+    const auto host_t0 = std::chrono::steady_clock::now();
+    uint32_t newnuc = 0;
+    int s = place_nuclei_upto(c, ph.t, &newnuc);  // time-dependent nucleation (no-op when site-saturated)
+    if (s != SCORE_OK) return s;
+    // on-the-fly defragmentation at user X logpoints (SCORE_Kernel.cpp:6625-6630, thresholds in cells)
+    if (c->prm.defragmentation && c->defrag_cnt < c->prm.n_defrag && c->Xcells >= c->prm.defrag_x[c->defrag_cnt] * (double)c->N) {
+        for (int L = 0; L < 2; ++L) { s = defragment(c, L); if (s != SCORE_OK) return s; }
+        c->defrag_cnt++;
+    }
+    set_mobility_args(c);
+    DomainArgs& a = c->a;
+    cudaStream_t st = c->stream;
+    cudaMemsetAsync((char*)c->d_state + kStepFieldsOffset, 0, sizeof(DevState) - kStepFieldsOffset, st);
+    cudaMemsetAsync(c->d_tickets, 0, 8 * sizeof(uint32_t), st);
+    for (int L = 0; L < 2; ++L)
+        cudaMemsetAsync(c->d_status[L], 0, ((size_t)(c->next_never[L] + kTileGrow - 1) / kTileGrow + 1) * 8, st);
+    cudaMemsetAsync(c->d_status[2], 0, c->status_words[2] * 8, st);
+    cudaEventRecord(c->ev[0], st);
+    for (int L = 0; L < 2; ++L) {
+        const uint32_t tiles = (c->next_never[L] + kTileGrow - 1) / kTileGrow;
+        const uint32_t grid = std::max<uint32_t>(1, std::min<uint32_t>(tiles, (uint32_t)c->sms * 4));
+        if (c->fp32) k_grow<true><<<grid, kBlock, 0, st>>>(a, L, c->d_status[L], c->d_tickets + L);
+        else k_grow<false><<<grid, kBlock, 0, st>>>(a, L, c->d_status[L], c->d_tickets + L);
+    }
+    cudaEventRecord(c->ev[1], st);
+    const uint32_t pgrid = (uint32_t)c->sms * 8;
+    k_claim<<<pgrid, kBlock, 0, st>>>(a);
+    cudaEventRecord(c->ev[2], st);
+    if (c->fp32) {
+        k_commit<true><<<(uint32_t)c->sms * 4, kBlock, 0, st>>>(a, c->d_status[2], c->d_tickets + 2);
+        k_finalize<true><<<pgrid, kBlock, 0, st>>>(a);
+    } else {
+        k_commit<false><<<(uint32_t)c->sms * 4, kBlock, 0, st>>>(a, c->d_status[2], c->d_tickets + 2);
+        k_finalize<false><<<pgrid, kBlock, 0, st>>>(a);
+    }
+    k_step_end<<<1, 1, 0, st>>>(c->d_state, a.f[0].cap, a.f[1].cap);
+    cudaEventRecord(c->ev[3], st);
+    c->launches += 6;
+    cudaError_t e = cudaMemcpyAsync(c->h_state, c->d_state, sizeof(DevState), cudaMemcpyDeviceToHost, st);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+    if (e != cudaSuccess) { c->failed = true; return c->cuda_fail(e, "growth step"); }
+    const DevState hs = *c->h_state;
+    if (hs.err) { c->failed = true; return check_device_errors(c, hs.err); }
+    float ms_grow = 0, ms_claim = 0, ms_commit = 0;
+    cudaEventElapsedTime(&ms_grow, c->ev[0], c->ev[1]);
+    cudaEventElapsedTime(&ms_claim, c->ev[1], c->ev[2]);
+    cudaEventElapsedTime(&ms_commit, c->ev[2], c->ev[3]);
+    c->tm.grow_ms += ms_grow; c->tm.claim_ms += ms_claim; c->tm.commit_ms += ms_commit;
+    c->tm.total_ms += ms_grow + ms_claim + ms_commit;
+    c->tm.grow_launches += 2;
+    c->tm.kernel_launches += 6;
+    const double bpu = c->fp32 ? 25.0 : 29.0;
+    const uint64_t Sv = hs.sv[0] + hs.sv[1], nfull = (uint64_t)hs.nfull[0] + hs.nfull[1], nnew = (uint64_t)hs.nwin[0] + hs.nwin[1];
+    c->tm.grow_bytes += bpu * (double)Sv;
+    c->tm.step_bytes += bpu * (double)Sv + 120.0 * (double)nfull + 37.0 * (double)nnew;
+
+    // mobility weights requested this step: compute on the host (FP64, libm), patch table + cells
+    double pmax_new = 0.0;
+    if (hs.pmax_bits) memcpy(&pmax_new, &hs.pmax_bits, 8);
+    if (hs.nmiss > 0 || hs.npending > 0) {
+        std::vector<unsigned long long> idx(hs.nmiss);
+        std::vector<double> val;
+        e = cudaMemcpyAsync(idx.data(), a.miss, (size_t)hs.nmiss * 8, cudaMemcpyDeviceToHost, st);
+        if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+        if (e != cudaSuccess) return c->cuda_fail(e, "read misses");
+        resolve_weights(c, idx, val);
+        for (double v : val) if (v > pmax_new) pmax_new = v;
+        if (hs.nmiss > 0) {
+            if (!c->stage((size_t)hs.nmiss * 16)) return c->fail(SCORE_ERR_NOMEM, "staging buffer");
+            unsigned long long* d_i = (unsigned long long*)c->d_stage;
+            double* d_v = (double*)(d_i + hs.nmiss);
+            e = cudaMemcpyAsync(d_i, idx.data(), (size_t)hs.nmiss * 8, cudaMemcpyHostToDevice, st);
+            if (e == cudaSuccess) e = cudaMemcpyAsync(d_v, val.data(), (size_t)hs.nmiss * 8, cudaMemcpyHostToDevice, st);
+            if (e != cudaSuccess) return c->cuda_fail(e, "upload weights");
+            k_fill_ptab<<<blocks_for(hs.nmiss, c->sms), kBlock, 0, st>>>(a.ptab, d_i, d_v, hs.nmiss);
+            c->launches++;
+        }
+        const uint32_t np = std::min(hs.npending, a.pendcap);
+        if (c->fp32) k_fix_pending<true><<<blocks_for(np, c->sms), kBlock, 0, st>>>(a, np);
+        else k_fix_pending<false><<<blocks_for(np, c->sms), kBlock, 0, st>>>(a, np);
+        c->launches++;
+        e = cudaStreamSynchronize(st);
+        if (e != cudaSuccess) return c->cuda_fail(e, "fix pending weights");
+    }
+    // deformed grains that ran out of cells this step (synchronize_mydefpool_counts)
+    if (hs.ndepleted > 0) {
+        std::vector<uint32_t> dep(hs.ndepleted);
+        e = cudaMemcpyAsync(dep.data(), a.depleted, (size_t)hs.ndepleted * 4, cudaMemcpyDeviceToHost, st);
+        if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+        if (e != cudaSuccess) return c->cuda_fail(e, "read depleted grains");
+        for (uint32_t g : dep) c->defg_cnt_host[g] = 0;
+    }
+    for (int L = 0; L < 2; ++L) {
+        c->next_never[L] = hs.next_never[L];
+        c->high_water[L] = std::max(c->high_water[L], c->next_never[L]);
+    }
+
+    // master block, SCORE_Kernel.cpp:6691-6740
+    const double dt_used = ph.dt;
+    if (pmax_new >= ph.Pmax) ph.Pmax = pmax_new;  // running max over every P ever assigned, floored at 0
+    c->Xcells = c->Xcells + (double)nfull;
+    const double X = (c->Xcells / (double)c->N);
+    ph.rhomax = rhomax_of(c->rho, c->defg_cnt_host);
+    const double rhomax_step = ph.rhomax;
+    ph.t += ph.dt;
+    ph.update_temperature();
+    ph.update_atomistic();
+    ph.update_microchemistry();
+    ph.update_mobilities();
+    ph.update_substructure(c->rho, c->rho0);
+    ph.dt = ph.dt_minimum();
+    c->step++;
+    s = upload_pforce(c);
+    if (s != SCORE_OK) return s;
+
+    score_step_stats& o = c->last;
+    o = score_step_stats{};
+    o.step = c->step; o.n_nuclei = newnuc; o.t = ph.t; o.dt = ph.dt; o.dt_used = dt_used;
+    o.Xcells = c->Xcells; o.X = X; o.Sv = Sv; o.n_full = nfull; o.n_new = nnew;
+    o.Pmax = ph.Pmax; o.rhomax = rhomax_step; o.dXstep = hs.dv[0] + hs.dv[1];
+    o.next_never[0] = c->next_never[0]; o.next_never[1] = c->next_never[1];
+    o.n_recycled[0] = hs.nrec[0]; o.n_recycled[1] = hs.nrec[1];
+    o.p_misses = hs.nmiss;
+    c->tm.host_ms += std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - host_t0).count();
+    if (out) *out = o;
+    return SCORE_OK;
+}
+
+int score_run_until(score_ctx* c, double x_target, score_step_stats* trace, uint32_t trace_cap, uint32_t* n_steps) {
+    if (!c) return SCORE_ERR_ARG;
+    if (!c->loaded) return c->fail(SCORE_ERR_STATE, "no domain loaded");
+    const double xt = x_target < 0 ? c->prm.xmax : x_target;
+    uint32_t k = 0;
+    for (;;) {
+        const double X = c->Xcells / (double)c->N;
+        // stop rule at the top of the step loop, SCORE_Kernel.cpp:6619
+        if ((c->Xcells >= (double)c->N) || (X > xt) || (c->step > c->prm.nmax) || (c->ph.t > c->ph.t_end) || (c->ph.t > c->prm.tmax)) break;
+        score_step_stats st;
+        int s = score_step(c, &st);
+        if (s != SCORE_OK) { if (n_steps) *n_steps = k; return s; }
+        if (trace && k < trace_cap) trace[k] = st;
+        ++k;
+    }
+    if (n_steps) *n_steps = k;
+    return SCORE_OK;
+}
+
+int score_get_stats(score_ctx* c, score_step_stats* out) {
+    if (!c || !out) return SCORE_ERR_ARG;
+    *out = c->last;
+    out->step = c->step; out->t = c->ph.t; out->dt = c->ph.dt; out->Xcells = c->Xcells;
+    out->X = c->N ? c->Xcells / (double)c->N : 0.0; out->Pmax = c->ph.Pmax;
+    return SCORE_OK;
+}
+
+int score_export_labels(score_ctx* c, uint32_t* labels) {
+    if (!c || !labels) return SCORE_ERR_ARG;
+    if (!c->loaded) return c->fail(SCORE_ERR_STATE, "no domain loaded");
+    cudaSetDevice(c->device);
+    uint32_t* d_lab = nullptr;
+    cudaError_t e = cudaMalloc(&d_lab, c->N * 4);
+    if (e != cudaSuccess) return c->fail(SCORE_ERR_NOMEM, "label buffer");
+    e = cudaMemcpyAsync(d_lab, c->a.grid, c->N * 4, cudaMemcpyDeviceToDevice, c->stream);
+    for (int L = 0; L < 2 && e == cudaSuccess; ++L) {
+        const uint32_t n = c->next_never[L];
+        if (n == 0) continue;
+        if (c->fp32) k_labels_front<true><<<blocks_for(n, c->sms), kBlock, 0, c->stream>>>(c->a, L, n, d_lab);
+        else k_labels_front<false><<<blocks_for(n, c->sms), kBlock, 0, c->stream>>>(c->a, L, n, d_lab);
+        c->launches++;
+    }
+    if (e == cudaSuccess) e = cudaMemcpyAsync(labels, d_lab, c->N * 4, cudaMemcpyDeviceToHost, c->stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(c->stream);
+    cudaFree(d_lab);
+    if (e != cudaSuccess) return c->cuda_fail(e, "export labels");
+    return SCORE_OK;
+}
+
+int score_grain_counts(score_ctx* c, uint32_t* rxg_counts, uint32_t* defg_counts) {
+    if (!c) return SCORE_ERR_ARG;
+    if (!c->loaded) return c->fail(SCORE_ERR_STATE, "no domain loaded");
+    cudaSetDevice(c->device);
+    cudaError_t e = cudaSuccess;
+    if (rxg_counts && c->nrxg) e = cudaMemcpyAsync(rxg_counts, c->a.rxg_cnt, (size_t)c->nrxg * 4, cudaMemcpyDeviceToHost, c->stream);
+    if (e == cudaSuccess && defg_counts) e = cudaMemcpyAsync(defg_counts, c->a.defg_cnt, (size_t)c->ndefg * 4, cudaMemcpyDeviceToHost, c->stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(c->stream);
+    if (e != cudaSuccess) return c->cuda_fail(e, "grain counts");
+    return SCORE_OK;
+}
+
+int score_get_timing(score_ctx* c, score_timing* out) {
+    if (!c || !out) return SCORE_ERR_ARG;
+    *out = c->tm;
+    out->kernel_launches = c->launches;
+    return SCORE_OK;
+}
+
+}  // extern "C"

@@ -1,0 +1,44 @@
+import os
+import sys
+from pathlib import Path
+
+import pytest
+
+ROOT = Path(__file__).resolve().parent.parent
+if str(ROOT) not in sys.path:
+    sys.path.insert(0, str(ROOT))
+
+
+def pytest_configure(config):
+    config.addinivalue_line("markers", "gpu: needs a CUDA device (GB300); runs the sm_103a kernels")
+    config.addinivalue_line("markers", "slow: longer CPU cases (reference runs at 128^3)")
+
+
+@pytest.fixture(scope="session")
+def built():
+    """Compile the native library and the oracle once per session."""
+    import __graft_entry__
+    __graft_entry__.build()
+    return True
+
+
+def has_gpu() -> bool:
+    try:
+        import torch
+        return torch.cuda.is_available()
+    except Exception:
+        return False
+
+
+@pytest.fixture(scope="session")
+def gpu(built):
+    if not has_gpu():
+        pytest.fail("GPU test selected but no CUDA device is visible")
+    return True
+
+
+@pytest.fixture
+def tmp_uds(tmp_path):
+    def make(spec):
+        return spec.write(tmp_path / "params.uds")
+    return make
