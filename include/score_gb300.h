@@ -154,6 +154,11 @@ const char* score_last_error(const score_ctx* ctx);
 int  score_load_domain(score_ctx* ctx, const uint32_t* grid, const double* defg_quat, const double* defg_rho0,
                        uint32_t ndefg, const double* rxg_quat, const uint32_t* rxg_site, const double* rxg_tincub,
                        uint32_t nrxg, const double* ptable);
+/* A context may load again: with the same ndefg/nrxg it reuses its device buffers. */
+
+/* Return the loaded domain to its just-loaded state without any host copy
+ * (the device keeps the loaded grid): the start of a fresh solve_RXGROWTH. */
+int  score_restart(score_ctx* ctx);
 
 /* site-saturated placement of every nucleus with tincub <= t, in rxg order
  * (caHdl::ompshar_sim_myCA_sitesaturatedNucleation, src/SCORE_GrowthMachine.cpp:50-189) */
@@ -179,14 +184,17 @@ int  score_export_labels(score_ctx* ctx, uint32_t* labels);
 /* per-grain cell counts (caHdl::synchronize_*_counts, SCORE_Kernel.cpp:5983-6028) */
 int  score_grain_counts(score_ctx* ctx, uint32_t* rxg_counts, uint32_t* defg_counts);
 
-/* device-side timing of the last run_until: kernel-only ms, ms of the dominant
- * (grow) kernel, its launches, and the algorithmic bytes those launches moved */
+/* device-side timing since the last load/restart (CUDA events on the context's
+ * stream): kernel-only ms per phase, ms of the dominant (grow) kernel, its
+ * launches, the algorithmic bytes those launches moved, and run_ms = event time
+ * from the start of the restart/reset to the end of the last score_run_until */
 typedef struct score_timing {
     double total_ms, grow_ms, claim_ms, commit_ms, host_ms;
     uint64_t grow_launches;
     double grow_bytes;      /* algorithmic bytes of all grow launches */
     double step_bytes;      /* algorithmic bytes of all kernels */
-    uint64_t kernel_launches;
+    uint64_t kernel_launches;  /* kernels launched by this context since creation */
+    double run_ms;
 } score_timing;
 int  score_get_timing(score_ctx* ctx, score_timing* out);
 

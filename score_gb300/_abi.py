@@ -71,6 +71,7 @@ class Timing(C.Structure):
     _fields_ = [
         ("total_ms", _d), ("grow_ms", _d), ("claim_ms", _d), ("commit_ms", _d), ("host_ms", _d),
         ("grow_launches", C.c_uint64), ("grow_bytes", _d), ("step_bytes", _d), ("kernel_launches", C.c_uint64),
+        ("run_ms", _d),
     ]
 
 
@@ -96,6 +97,7 @@ SIGNATURES = {
     "score_destroy": (None, [_vp]),
     "score_last_error": (C.c_char_p, [_vp]),
     "score_load_domain": (C.c_int, [_vp, _vp, _vp, _vp, _u32, _vp, _vp, _vp, _u32, _vp]),
+    "score_restart": (C.c_int, [_vp]),
     "score_place_nuclei": (C.c_int, [_vp, _P(_u32)]),
     "score_step": (C.c_int, [_vp, _P(StepStats)]),
     "score_run_until": (C.c_int, [_vp, _d, _P(StepStats), _u32, _P(_u32)]),

@@ -10,6 +10,8 @@ namespace score {
 constexpr int kBlock = 256;                 // threads per block of the tiled kernels
 constexpr int kWarps = kBlock / 32;
 constexpr uint8_t kInactive = 0xFF;         // dir byte of an INACTIVE slot
+constexpr uint8_t kStale = 0x40;            // dir bit: cached fill increment not computed yet
+constexpr uint8_t kCodeMask = 0x3F;         // dir bits holding the infector code 0..26
 constexpr uint32_t kClaimFree = 0xFFFFFFFFu;
 constexpr unsigned long long kPtabEmpty = 0xFFFFFFFFFFFFFFFFull;    // NaN bit pattern, never a weight
 constexpr unsigned long long kPtabPending = 0xFFFFFFFFFFFFFFFEull;  // requested from the host this step

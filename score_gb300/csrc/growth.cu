@@ -1,27 +1,27 @@
 // score_gb300 growth context: device memory layout, the per-step launch sequence
 // and the host FP64 master-thread work (dt, physics, P on first use).
 //
-// HBM layout of one domain (N cells, list capacities cap_I = N, cap_B = N or the
+// HBM layout of one domain (N cells; list capacities cap_I = N, cap_B = N or the
 // reference's 2(xy+xz+yz) Border limit):
 //   grid   u32[N]   deformed id < ndefg | CURRENTLY_INFECTED | ndefg + rxg
 //   claim  u32[N]   attempt ordinal of the first infection of this step (0xFFFFFFFF free)
-//   front list L (SoA, slot-indexed): fill f64|f32, [comp f32], P f64|f32, defg u32,
-//          rxg u32, xyz u32, dir u8  -> 29 B (FP64) / 25 B (FP32) per slot
-//   full_L u32[cap_L], recyc_L u32[reccap_L]  (ordered lists rebuilt every step)
+//   front list L (SoA, slot-indexed): fill f64|f32, [comp f32], vel f64|f32, defg u32,
+//          rxg u32, xyz u32, dir u8
+//   full_L u32[cap_L], recyc_L u32[reccap_L], amask u32[N]  (rebuilt every step)
 //   ptab   u64[nrxg*ndefg] mobility weights P(rxg,defg), filled on first use
+//   status u64 look-back words of the three scans, cleared by k_step_end
 #include <cuda_runtime.h>
 
 #include <algorithm>
-#include <atomic>
 #include <chrono>
 #include <cmath>
+#include <cstddef>
 #include <cstdio>
 #include <cstring>
 #include <string>
 #include <thread>
-#include <vector>
 #include <unordered_set>
-#include <cstddef>
+#include <vector>
 
 #include "../../include/score_gb300.h"
 #include "device_common.cuh"
@@ -31,6 +31,8 @@
 using namespace score;
 
 namespace {
+
+constexpr uint32_t kTile = kBlock * 8;  // slots (grow) / full cells (commit) per look-back tile
 
 // ------------------------------------------------------------------ small kernels
 __global__ void k_count_defg(const uint32_t* grid, uint64_t n, uint32_t ndefg, uint32_t* cnt, uint32_t* err) {
@@ -45,16 +47,22 @@ __global__ void k_gather_u32(const uint32_t* src, const uint32_t* idx, uint32_t 
     for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) out[i] = src[idx[i]];
 }
 
+__global__ void k_zero_u64(unsigned long long* p, size_t n) {
+    for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x) p[i] = 0ull;
+}
+
 struct NucRec { uint32_t list, slot, site, rxg, defg, pad; double P; };
 
+// nucleus: fill 1.0 (ALMOST_FULLY_INFECTED), infector 26 (f_geo 1.0)
 template <bool FP32>
 __global__ void k_place_nuclei(DomainArgs a, const NucRec* rec, uint32_t n) {
     for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
         const NucRec r = rec[i];
         const DFront& f = a.f[r.list];
-        if (!FP32) { ((double*)f.fill)[r.slot] = 1.0; ((double*)f.P)[r.slot] = r.P; }
-        else { ((float*)f.fill)[r.slot] = 1.0f; f.comp[r.slot] = 0.0f; ((float*)f.P)[r.slot] = (float)r.P; }
-        f.dir[r.slot] = 26;
+        const double v = velocity_factor(a, r.P, r.defg, 26);
+        if (!FP32) { ((double*)f.fill)[r.slot] = 1.0; ((double*)f.vel)[r.slot] = v; }
+        else { ((float*)f.fill)[r.slot] = 1.0f; f.comp[r.slot] = 0.0f; ((float*)f.vel)[r.slot] = (float)v; }
+        f.dir[r.slot] = 26 | kStale;
         f.defg[r.slot] = r.defg;
         f.rxg[r.slot] = r.rxg;
         f.xyz[r.slot] = r.site;
@@ -67,15 +75,18 @@ __global__ void k_fill_ptab(unsigned long long* ptab, const unsigned long long* 
         ptab[idx[i]] = (unsigned long long)__double_as_longlong(val[i]);
 }
 
+// new cells whose P arrived from the host: their velocity factor
 template <bool FP32>
 __global__ void k_fix_pending(DomainArgs a, uint32_t n) {
     for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
         const uint32_t q = a.pending[i];
         const DFront& f = a.f[q >> 31];
         const uint32_t s = q & 0x7FFFFFFFu;
-        const double P = __longlong_as_double((long long)a.ptab[(unsigned long long)f.rxg[s] * a.ndefg + f.defg[s]]);
-        if (!FP32) ((double*)f.P)[s] = P;
-        else ((float*)f.P)[s] = (float)P;
+        const uint32_t g = f.defg[s];
+        const double P = __longlong_as_double((long long)a.ptab[(unsigned long long)f.rxg[s] * a.ndefg + g]);
+        const double v = velocity_factor(a, P, g, f.dir[s] & kCodeMask);
+        if (!FP32) ((double*)f.vel)[s] = v;
+        else ((float*)f.vel)[s] = (float)v;
     }
 }
 
@@ -92,18 +103,18 @@ __global__ void k_labels_front(DomainArgs a, int L, uint32_t n, uint32_t* lab) {
 }
 
 // stable compaction of ACTIVE slots of list L into scratch arrays (ompshar_defragmentation,
-// SCORE_Kernel.cpp:3877-3937); counter A = actives, B unused
+// SCORE_Kernel.cpp:3877-3937); uses the list's grow look-back words and ticket
 template <bool FP32>
-__global__ void __launch_bounds__(kBlock) k_defrag_compact(DomainArgs a, int L, uint32_t n, DFront scratch,
-                                                           unsigned long long* status, uint32_t* ticket, uint32_t* out_count) {
+__global__ void __launch_bounds__(kBlock) k_defrag_compact(DomainArgs a, int L, uint32_t n, DFront scratch, uint32_t* out_count) {
     constexpr int ITEMS = 8;
     constexpr uint32_t TILE = kBlock * ITEMS;
     const DFront fr = a.f[L];
+    unsigned long long* status = a.status + (L == 0 ? 0u : a.status_off1);
     const uint32_t ntiles = (n + TILE - 1) / TILE;
     __shared__ uint32_t s_tile, s_ex, s_cntA[ITEMS * kWarps], s_cntB[ITEMS * kWarps];
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     for (;;) {
-        if (threadIdx.x == 0) s_tile = atomicAdd(ticket, 1u);
+        if (threadIdx.x == 0) s_tile = atomicAdd(a.tickets + L, 1u);
         __syncthreads();
         const uint32_t tile = s_tile;
         if (tile >= ntiles) break;
@@ -135,11 +146,12 @@ __global__ void __launch_bounds__(kBlock) k_defrag_compact(DomainArgs a, int L, 
             const uint32_t r = s_ex + s_cntA[k * kWarps + warp] + __popc(am[k] & lt);
             if (!FP32) {
                 ((double*)scratch.fill)[r] = ((const double*)fr.fill)[s];
-                ((double*)scratch.P)[r] = ((const double*)fr.P)[s];
+                ((double*)scratch.vel)[r] = ((const double*)fr.vel)[s];
+                scratch.inc[r] = fr.inc[s];
             } else {
                 ((float*)scratch.fill)[r] = ((const float*)fr.fill)[s];
                 scratch.comp[r] = fr.comp[s];
-                ((float*)scratch.P)[r] = ((const float*)fr.P)[s];
+                ((float*)scratch.vel)[r] = ((const float*)fr.vel)[s];
             }
             scratch.defg[r] = fr.defg[s]; scratch.rxg[r] = fr.rxg[s]; scratch.xyz[r] = fr.xyz[s]; scratch.dir[r] = fr.dir[s];
         }
@@ -179,26 +191,28 @@ struct score_ctx {
     uint32_t nx = 0, ny = 0, nz = 0;
     uint64_t N = 0;
     uint32_t ndefg = 0, nrxg = 0;
-    bool loaded = false, fp32 = false, failed = false;
+    bool loaded = false, fp32 = false, failed = false, refresh = false;
     std::vector<double> defg_q, rxg_q, rho0, rho, tincub;
     std::vector<uint32_t> site;
     std::vector<uint8_t> placed;
     std::vector<uint32_t> nuc_order;   // rxg ids sorted by (tincub, id)
     size_t nuc_pos = 0;                // nuc_order[0, nuc_pos) already considered
-    std::vector<uint32_t> defg_cnt_host;
+    std::vector<uint32_t> defg_cnt_host, defg_cnt_init_host;
     std::vector<double> user_ptab;
     std::vector<double> pforce_host;
+    double mob_host[4] = {0, 0, 0, 0};  // mobilities the front's vel factors were computed with
+    double dt_cached = -1.0;             // dt the front's cached fill increments were computed with
+    double pf_sig[2] = {0, 0};           // Gb^2/2 and drag the driving-force table was computed with
+    uint64_t rho_version = 0, pf_rho_version = ~0ull, rhomax_version = ~0ull;
 
     DomainArgs a{};
     DevState* d_state = nullptr;
-    DevState* h_state = nullptr;  // pinned
-    unsigned long long* d_status[3] = {nullptr, nullptr, nullptr};
-    size_t status_words[3] = {0, 0, 0};
-    uint32_t* d_tickets = nullptr;
+    DevState* d_snap = nullptr;        // per-step snapshot written by k_step_end
+    DevState* h_state = nullptr;       // pinned host copy of the snapshot
     double* d_pforce = nullptr;
-    float* d_pforce32 = nullptr;
+    uint32_t* d_grid_init = nullptr;       // the loaded deformed grid (restart source)
+    uint32_t* d_defg_cnt_init = nullptr;   // its per-grain cell counts
     uint32_t* d_u32tmp = nullptr;
-    size_t u32tmp_cap = 0;
     void* d_stage = nullptr;
     size_t stage_cap = 0;
     DFront scratch{};
@@ -209,12 +223,13 @@ struct score_ctx {
     uint32_t next_never[2] = {0, 0}, high_water[2] = {0, 0};
     score_step_stats last{};
 
-    cudaEvent_t ev[4] = {nullptr, nullptr, nullptr, nullptr};
+    cudaEvent_t ev[6] = {nullptr, nullptr, nullptr, nullptr, nullptr, nullptr};  // 0-3 step phases, 4-5 run span
     score_timing tm{};
     uint64_t launches = 0;
 
-    ~score_ctx() { release(); }
-    void release();
+    ~score_ctx() { release_domain(); release_stream(); }
+    void release_domain();
+    void release_stream();
     int fail(int code, const std::string& msg) { err = msg; return code; }
     int cuda_fail(cudaError_t e, const char* what) {
         err = std::string(what) + ": " + cudaGetErrorString(e);
@@ -230,18 +245,24 @@ struct score_ctx {
     }
 };
 
-void score_ctx::release() {
+void score_ctx::release_domain() {
     if (device >= 0) cudaSetDevice(device);
-    void* ptrs[] = {a.f[0].fill, a.f[0].comp, a.f[0].P, a.f[0].defg, a.f[0].rxg, a.f[0].xyz, a.f[0].dir, a.f[0].full, a.f[0].recyc,
-                    a.f[1].fill, a.f[1].comp, a.f[1].P, a.f[1].defg, a.f[1].rxg, a.f[1].xyz, a.f[1].dir, a.f[1].full, a.f[1].recyc,
-                    a.grid, a.claim, a.ptab, a.defg_cnt, a.rxg_cnt, a.depleted, a.miss, a.pending,
-                    d_state, d_status[0], d_status[1], d_status[2], d_tickets, d_pforce, d_pforce32, d_u32tmp, d_stage,
-                    scratch.fill, scratch.comp, scratch.P, scratch.defg, scratch.rxg, scratch.xyz, scratch.dir};
+    void* ptrs[] = {a.f[0].inc, a.f[1].inc, scratch.inc, a.f[0].fill, a.f[0].comp, a.f[0].vel, a.f[0].defg, a.f[0].rxg, a.f[0].xyz, a.f[0].dir, a.f[0].full, a.f[0].recyc,
+                    a.f[1].fill, a.f[1].comp, a.f[1].vel, a.f[1].defg, a.f[1].rxg, a.f[1].xyz, a.f[1].dir, a.f[1].full, a.f[1].recyc,
+                    a.grid, a.claim, a.amask, a.ptab, a.defg_cnt, a.rxg_cnt, a.depleted, a.miss, a.pending, a.status, a.tickets,
+                    d_state, d_snap, d_pforce, d_u32tmp, d_stage, d_grid_init, d_defg_cnt_init,
+                    scratch.fill, scratch.comp, scratch.vel, scratch.defg, scratch.rxg, scratch.xyz, scratch.dir};
     for (void* p : ptrs) if (p) cudaFree(p);
     a = DomainArgs{};
     scratch = DFront{};
-    d_state = nullptr; d_tickets = nullptr; d_pforce = nullptr; d_pforce32 = nullptr; d_u32tmp = nullptr; d_stage = nullptr;
-    for (auto& s : d_status) s = nullptr;
+    d_state = nullptr; d_snap = nullptr; d_pforce = nullptr; d_u32tmp = nullptr; d_stage = nullptr;
+    d_grid_init = nullptr; d_defg_cnt_init = nullptr;
+    stage_cap = 0; scratch_cap = 0;
+    loaded = false;
+}
+
+void score_ctx::release_stream() {
+    if (device >= 0) cudaSetDevice(device);
     if (h_state) cudaFreeHost(h_state);
     h_state = nullptr;
     for (auto& e : ev) if (e) { cudaEventDestroy(e); e = nullptr; }
@@ -252,34 +273,34 @@ void score_ctx::release() {
 // ------------------------------------------------------------------ helpers
 namespace {
 
-constexpr uint32_t kTileGrow = kBlock * 8;
-
-int upload_pforce(score_ctx* c) {
-    // driving force per deformed grain, the grow step's p (SCORE_Kernel.cpp:4082)
+// Driving force per deformed grain, the grow step's p (SCORE_Kernel.cpp:4082).  When it or
+// the mobilities change, the front's velocity factors are recomputed in the next grow.
+int upload_physics(score_ctx* c) {
+    const double mob[4] = {c->ph.mLAGB, c->ph.mHAGB, c->ph.mGS, c->ph.mRHHAGB};
+    const bool mob_same = memcmp(mob, c->mob_host, sizeof mob) == 0;
+    // p depends on Gb^2/2, the drag and rho only: skip the per-grain pass when none changed
+    const double sig[2] = {c->ph.Gbhalfsq, c->ph.zener()};
+    if (mob_same && !c->pforce_host.empty() && memcmp(sig, c->pf_sig, sizeof sig) == 0 && c->pf_rho_version == c->rho_version)
+        return SCORE_OK;
+    memcpy(c->pf_sig, sig, sizeof sig);
+    c->pf_rho_version = c->rho_version;
     std::vector<double> pf(c->ndefg);
     for (uint32_t g = 0; g < c->ndefg; ++g) pf[g] = c->ph.driving_force(c->rho[g]);
+    if (pf == c->pforce_host && mob_same) return SCORE_OK;
+    c->refresh = true;
+    memcpy(c->mob_host, mob, sizeof mob);
     if (pf == c->pforce_host) return SCORE_OK;
     c->pforce_host = pf;
-    cudaError_t e = cudaMemcpyAsync(c->d_pforce, pf.data(), pf.size() * 8, cudaMemcpyHostToDevice, c->stream);
-    if (e != cudaSuccess) return c->cuda_fail(e, "upload pforce");
-    if (c->fp32) {
-        std::vector<float> p32(pf.begin(), pf.end());
-        e = cudaMemcpyAsync(c->d_pforce32, p32.data(), p32.size() * 4, cudaMemcpyHostToDevice, c->stream);
-        if (e != cudaSuccess) return c->cuda_fail(e, "upload pforce32");
-        e = cudaStreamSynchronize(c->stream);  // p32 is a temporary
-        if (e != cudaSuccess) return c->cuda_fail(e, "sync");
-    } else {
-        e = cudaStreamSynchronize(c->stream);
-        if (e != cudaSuccess) return c->cuda_fail(e, "sync");
-    }
+    cudaError_t e = cudaMemcpyAsync(c->d_pforce, c->pforce_host.data(), pf.size() * 8, cudaMemcpyHostToDevice, c->stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(c->stream);
+    if (e != cudaSuccess) return c->cuda_fail(e, "upload driving force");
     return SCORE_OK;
 }
 
-void set_mobility_args(score_ctx* c) {
+void set_step_args(score_ctx* c) {
     c->a.mLAGB = c->ph.mLAGB; c->a.mHAGB = c->ph.mHAGB; c->a.mGS = c->ph.mGS; c->a.mRH = c->ph.mRHHAGB;
     c->a.dt = c->ph.dt; c->a.cinv = (1.0 / c->prm.cellsize);
-    c->a.mLAGB32 = (float)c->ph.mLAGB; c->a.mHAGB32 = (float)c->ph.mHAGB; c->a.mGS32 = (float)c->ph.mGS;
-    c->a.mRH32 = (float)c->ph.mRHHAGB; c->a.dtc32 = (float)(c->ph.dt * (1.0 / c->prm.cellsize));
+    c->a.dtc32 = (float)(c->ph.dt * (1.0 / c->prm.cellsize));
 }
 
 double weight_of(score_ctx* c, uint32_t r, uint32_t g) {
@@ -375,6 +396,7 @@ int place_nuclei_upto(score_ctx* c, double tnow, uint32_t* nplaced) {
     if (e == cudaSuccess) e = cudaMemcpyAsync(d_pi, pidx.data(), nr * 8, cudaMemcpyHostToDevice, c->stream);
     if (e == cudaSuccess) e = cudaMemcpyAsync(d_pv, pval.data(), nr * 8, cudaMemcpyHostToDevice, c->stream);
     if (e != cudaSuccess) return c->cuda_fail(e, "upload nuclei");
+    set_step_args(c);
     if (c->fp32) k_place_nuclei<true><<<blocks_for(nr, c->sms), kBlock, 0, c->stream>>>(c->a, d_rec, (uint32_t)nr);
     else k_place_nuclei<false><<<blocks_for(nr, c->sms), kBlock, 0, c->stream>>>(c->a, d_rec, (uint32_t)nr);
     k_fill_ptab<<<blocks_for(nr, c->sms), kBlock, 0, c->stream>>>(c->a.ptab, d_pi, d_pv, (uint32_t)nr);
@@ -392,13 +414,14 @@ int defragment(score_ctx* c, int L) {
     if (n == 0) return SCORE_OK;
     DFront& fr = c->a.f[L];
     if (c->scratch_cap < n) {
-        void* ptrs[] = {c->scratch.fill, c->scratch.comp, c->scratch.P, c->scratch.defg, c->scratch.rxg, c->scratch.xyz, c->scratch.dir};
+        void* ptrs[] = {c->scratch.inc, c->scratch.fill, c->scratch.comp, c->scratch.vel, c->scratch.defg, c->scratch.rxg, c->scratch.xyz, c->scratch.dir};
         for (void* p : ptrs) if (p) cudaFree(p);
         c->scratch = DFront{};
         const size_t fb = c->fp32 ? 4 : 8;
         cudaError_t e = cudaMalloc(&c->scratch.fill, (size_t)n * fb);
         if (e == cudaSuccess && c->fp32) e = cudaMalloc((void**)&c->scratch.comp, (size_t)n * 4);
-        if (e == cudaSuccess) e = cudaMalloc(&c->scratch.P, (size_t)n * fb);
+        if (e == cudaSuccess) e = cudaMalloc(&c->scratch.vel, (size_t)n * fb);
+        if (e == cudaSuccess && !c->fp32) e = dalloc(&c->scratch.inc, n);
         if (e == cudaSuccess) e = dalloc(&c->scratch.defg, n);
         if (e == cudaSuccess) e = dalloc(&c->scratch.rxg, n);
         if (e == cudaSuccess) e = dalloc(&c->scratch.xyz, n);
@@ -408,14 +431,18 @@ int defragment(score_ctx* c, int L) {
     }
     uint32_t* d_cnt = c->d_u32tmp;
     cudaMemsetAsync(d_cnt, 0, 8, c->stream);
-    cudaMemsetAsync(c->d_tickets, 0, 4 * sizeof(uint32_t), c->stream);
-    cudaMemsetAsync(c->d_status[0], 0, ((n + kTileGrow - 1) / kTileGrow) * 8, c->stream);
     const uint32_t grid = blocks_for((uint64_t)n, c->sms, 4);
-    if (c->fp32) k_defrag_compact<true><<<grid, kBlock, 0, c->stream>>>(c->a, L, n, c->scratch, c->d_status[0], c->d_tickets, d_cnt);
-    else k_defrag_compact<false><<<grid, kBlock, 0, c->stream>>>(c->a, L, n, c->scratch, c->d_status[0], c->d_tickets, d_cnt);
+    if (c->fp32) k_defrag_compact<true><<<grid, kBlock, 0, c->stream>>>(c->a, L, n, c->scratch, d_cnt);
+    else k_defrag_compact<false><<<grid, kBlock, 0, c->stream>>>(c->a, L, n, c->scratch, d_cnt);
     c->launches++;
     uint32_t active = 0;
     cudaError_t e = cudaMemcpyAsync(&active, d_cnt, 4, cudaMemcpyDeviceToHost, c->stream);
+    // the grow scan of this step needs its look-back words and ticket cleared again
+    if (e == cudaSuccess) {
+        k_zero_u64<<<blocks_for(c->a.status_words, c->sms), kBlock, 0, c->stream>>>(c->a.status, c->a.status_words);
+        c->launches++;
+        e = cudaMemsetAsync(c->a.tickets, 0, 8 * sizeof(uint32_t), c->stream);
+    }
     if (e == cudaSuccess) e = cudaStreamSynchronize(c->stream);
     if (e != cudaSuccess) return c->cuda_fail(e, "defragment");
     if (active == n) {
@@ -435,7 +462,8 @@ int defragment(score_ctx* c, int L) {
         const size_t fb = c->fp32 ? 4 : 8;
         e = cudaMemcpyAsync(fr.fill, c->scratch.fill, (size_t)active * fb, cudaMemcpyDeviceToDevice, c->stream);
         if (e == cudaSuccess && c->fp32) e = cudaMemcpyAsync(fr.comp, c->scratch.comp, (size_t)active * 4, cudaMemcpyDeviceToDevice, c->stream);
-        if (e == cudaSuccess) e = cudaMemcpyAsync(fr.P, c->scratch.P, (size_t)active * fb, cudaMemcpyDeviceToDevice, c->stream);
+        if (e == cudaSuccess) e = cudaMemcpyAsync(fr.vel, c->scratch.vel, (size_t)active * fb, cudaMemcpyDeviceToDevice, c->stream);
+        if (e == cudaSuccess && !c->fp32) e = cudaMemcpyAsync(fr.inc, c->scratch.inc, (size_t)active * 8, cudaMemcpyDeviceToDevice, c->stream);
         if (e == cudaSuccess) e = cudaMemcpyAsync(fr.defg, c->scratch.defg, (size_t)active * 4, cudaMemcpyDeviceToDevice, c->stream);
         if (e == cudaSuccess) e = cudaMemcpyAsync(fr.rxg, c->scratch.rxg, (size_t)active * 4, cudaMemcpyDeviceToDevice, c->stream);
         if (e == cudaSuccess) e = cudaMemcpyAsync(fr.xyz, c->scratch.xyz, (size_t)active * 4, cudaMemcpyDeviceToDevice, c->stream);
@@ -449,14 +477,53 @@ int defragment(score_ctx* c, int L) {
     return SCORE_OK;
 }
 
-// Size the look-back status buffers for the largest launch of each kind.
-int ensure_status(score_ctx* c, int which, size_t words) {
-    if (words <= c->status_words[which]) return SCORE_OK;
-    if (c->d_status[which]) cudaFree(c->d_status[which]);
-    c->d_status[which] = nullptr;
-    size_t w = std::max<size_t>(words, 1024);
-    if (cudaMalloc((void**)&c->d_status[which], w * 8) != cudaSuccess) return c->fail(SCORE_ERR_NOMEM, "status buffer");
-    c->status_words[which] = w;
+// Return the domain to its loaded state on the device (grid from the pristine copy,
+// empty fronts, empty P cache) and redo the start of solve_RXGROWTH
+// (SCORE_Kernel.cpp:6513-6530): rho max, T, G/b, mobilities, dt0.
+int reset_state(score_ctx* c) {
+    DomainArgs& a = c->a;
+    const uint64_t N = c->N;
+    cudaStream_t st = c->stream;
+    cudaEventRecord(c->ev[4], st);  // start of the run span reported as score_timing.run_ms
+    cudaError_t e = cudaMemcpyAsync(a.grid, c->d_grid_init, N * 4, cudaMemcpyDeviceToDevice, st);
+    if (e == cudaSuccess) e = cudaMemsetAsync(a.claim, 0xFF, N * 4, st);
+    for (int L = 0; L < 2 && e == cudaSuccess; ++L)
+        e = cudaMemsetAsync(a.f[L].dir, kInactive, std::max<size_t>(c->high_water[L], 1), st);
+    if (e == cudaSuccess && c->user_ptab.empty())
+        e = cudaMemsetAsync(a.ptab, 0xFF, std::max<size_t>((size_t)c->nrxg * c->ndefg, 1) * 8, st);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(a.defg_cnt, c->d_defg_cnt_init, (size_t)c->ndefg * 4, cudaMemcpyDeviceToDevice, st);
+    if (e == cudaSuccess) e = cudaMemsetAsync(a.rxg_cnt, 0, std::max<size_t>(c->nrxg, 1) * 4, st);
+    if (e == cudaSuccess) e = cudaMemsetAsync(c->d_state, 0, sizeof(DevState), st);
+    if (e == cudaSuccess) e = cudaMemsetAsync(a.status, 0, (size_t)a.status_words * 8, st);
+    if (e == cudaSuccess) e = cudaMemsetAsync(a.tickets, 0, 8 * sizeof(uint32_t), st);
+    if (e != cudaSuccess) return c->cuda_fail(e, "reset domain");
+    c->rho = c->rho0;
+    c->defg_cnt_host = c->defg_cnt_init_host;
+    c->placed.assign(c->nrxg, 0);
+    c->nuc_pos = 0;
+    Physics& ph = c->ph;
+    ph.init(&c->prm);
+    ph.rhomax = rhomax_of(c->rho, c->defg_cnt_host);
+    c->rho_version = 0; c->rhomax_version = 0; c->pf_rho_version = ~0ull;
+    ph.update_temperature();
+    ph.update_atomistic();
+    ph.update_mobilities();
+    ph.dt = ph.dt_minimum();
+    c->pforce_host.clear();
+    memset(c->mob_host, 0, sizeof c->mob_host);
+    int s = upload_physics(c);
+    if (s != SCORE_OK) return s;
+    c->refresh = false;  // the front is empty; new cells get their factors when they are created
+    c->dt_cached = -1.0;
+    c->Xcells = 0.0; c->step = 0; c->defrag_cnt = 0; c->n_nuclei = 0;
+    c->next_never[0] = c->next_never[1] = 0;
+    c->high_water[0] = c->high_water[1] = 0;
+    c->tm = score_timing{};
+    c->last = score_step_stats{};
+    c->last.dt = ph.dt;
+    c->last.rhomax = ph.rhomax;
+    c->failed = false;
+    c->loaded = true;
     return SCORE_OK;
 }
 
@@ -526,7 +593,7 @@ int score_create(score_ctx** out, const score_params* p, int device) {
     if (e == cudaSuccess) e = cudaDeviceGetAttribute(&c->sms, cudaDevAttrMultiProcessorCount, device);
     for (auto& ev : c->ev) if (e == cudaSuccess) e = cudaEventCreate(&ev);
     if (e == cudaSuccess) e = cudaMallocHost((void**)&c->h_state, sizeof(DevState));
-    if (e != cudaSuccess) { c->device = device; delete c; return SCORE_ERR_CUDA; }
+    if (e != cudaSuccess) { delete c; return SCORE_ERR_CUDA; }
     *out = c;
     return SCORE_OK;
 }
@@ -537,123 +604,120 @@ int score_load_domain(score_ctx* c, const uint32_t* grid, const double* defg_qua
                       const double* rxg_quat, const uint32_t* rxg_site, const double* rxg_tincub, uint32_t nrxg,
                       const double* ptable) {
     if (!c || !grid || !defg_quat || !defg_rho0 || !rxg_quat || !rxg_site || ndefg == 0) return SCORE_ERR_ARG;
-    if (c->loaded) return c->fail(SCORE_ERR_STATE, "domain already loaded");
     if ((uint64_t)ndefg + nrxg >= 4096000000ull) return c->fail(SCORE_ERR_ARG, "too many grains");
     const uint64_t N = c->N;
     for (uint32_t r = 0; r < nrxg; ++r) if (rxg_site[r] >= N) return c->fail(SCORE_ERR_ARG, "nucleation site outside the domain");
     cudaSetDevice(c->device);
+    // a context reloads in place when the pool sizes match; otherwise it reallocates
+    const bool reuse = c->a.grid && c->ndefg == ndefg && c->nrxg == nrxg;
+    if (!reuse && c->a.grid) c->release_domain();
+    c->loaded = false;
     c->ndefg = ndefg; c->nrxg = nrxg;
     c->defg_q.assign(defg_quat, defg_quat + 4 * (size_t)ndefg);
     c->rxg_q.assign(rxg_quat, rxg_quat + 4 * (size_t)nrxg);
     c->rho0.assign(defg_rho0, defg_rho0 + ndefg);
-    c->rho = c->rho0;
     c->site.assign(rxg_site, rxg_site + nrxg);
     c->tincub.assign(nrxg, 0.0);
     if (rxg_tincub) c->tincub.assign(rxg_tincub, rxg_tincub + nrxg);
-    c->placed.assign(nrxg, 0);
     c->nuc_order.resize(nrxg);
     for (uint32_t r = 0; r < nrxg; ++r) c->nuc_order[r] = r;
     std::stable_sort(c->nuc_order.begin(), c->nuc_order.end(), [&](uint32_t x, uint32_t y) { return c->tincub[x] < c->tincub[y]; });
-    c->nuc_pos = 0;
+    c->user_ptab.clear();
     if (ptable) c->user_ptab.assign(ptable, ptable + (size_t)nrxg * ndefg);
 
     const score_params& p = c->prm;
     DomainArgs& a = c->a;
-    a.nx = c->nx; a.ny = c->ny; a.nz = c->nz; a.nxy = c->nx * c->ny;
-    a.ndefg = ndefg; a.nrxg = nrxg;
-    a.border_ref_cap = 2 * ((c->nx * c->ny) + (c->nx * c->nz) + (c->ny * c->nz));
-    a.border_policy = p.border_policy; a.boundary = p.boundary; a.mobility_model = p.mobility_model;
-    // capacities: at most N infections ever happen, so N slots per list never overflow
-    const uint32_t capI = (uint32_t)N;
-    const uint32_t capB = (p.border_policy == SCORE_BORDER_REFERENCE_LIMIT) ? std::min<uint32_t>((uint32_t)N, a.border_ref_cap + 1) : (uint32_t)N;
-    // recycle-list caps (ompshar_init_myRXFront{Inside,Border}, SCORE_Kernel.cpp:3615, 3670)
-    const uint32_t recI = (uint32_t)(p.initial_cache * (double)N * p.maxfillperstep * kFullRecyclingFactor);
-    const uint32_t recB = (uint32_t)((double)a.border_ref_cap * p.maxfillperstep * kFullRecyclingFactor);
-    const uint32_t caps[2] = {capI, capB}, recs[2] = {recI, recB};
-    const size_t fb = c->fp32 ? 4 : 8;
-    cudaError_t e = cudaSuccess;
-    for (int L = 0; L < 2; ++L) {
-        DFront& f = a.f[L];
-        f.cap = caps[L]; f.reccap = recs[L];
-        if (e == cudaSuccess) e = cudaMalloc(&f.fill, (size_t)caps[L] * fb);
-        if (e == cudaSuccess && c->fp32) e = cudaMalloc((void**)&f.comp, (size_t)caps[L] * 4);
-        if (e == cudaSuccess) e = cudaMalloc(&f.P, (size_t)caps[L] * fb);
-        if (e == cudaSuccess) e = dalloc(&f.defg, caps[L]);
-        if (e == cudaSuccess) e = dalloc(&f.rxg, caps[L]);
-        if (e == cudaSuccess) e = dalloc(&f.xyz, caps[L]);
-        if (e == cudaSuccess) e = dalloc(&f.dir, caps[L]);
-        if (e == cudaSuccess) e = dalloc(&f.full, caps[L]);
-        if (e == cudaSuccess) e = dalloc(&f.recyc, recs[L]);
-        if (e == cudaSuccess) e = cudaMemsetAsync(f.dir, kInactive, caps[L], c->stream);
-    }
     const size_t ptab_words = (size_t)nrxg * ndefg;
-    a.misscap = a.pendcap = (uint32_t)std::min<uint64_t>(N, 1ull << 25);
-    if (e == cudaSuccess) e = dalloc(&a.grid, N);
-    if (e == cudaSuccess) e = dalloc(&a.claim, N);
-    if (e == cudaSuccess) e = dalloc(&a.ptab, ptab_words);
-    if (e == cudaSuccess) e = dalloc(&a.defg_cnt, ndefg);
-    if (e == cudaSuccess) e = dalloc(&a.rxg_cnt, nrxg);
-    if (e == cudaSuccess) e = dalloc(&a.depleted, ndefg);
-    if (e == cudaSuccess) e = dalloc(&a.miss, a.misscap);
-    if (e == cudaSuccess) e = dalloc(&a.pending, a.pendcap);
-    if (e == cudaSuccess) e = dalloc(&c->d_state, 1);
-    if (e == cudaSuccess) e = dalloc(&c->d_tickets, 8);
-    if (e == cudaSuccess) e = dalloc(&c->d_pforce, ndefg);
-    if (e == cudaSuccess) e = dalloc(&c->d_pforce32, ndefg);
-    if (e == cudaSuccess) { e = dalloc(&c->d_u32tmp, 64); c->u32tmp_cap = 64; }
-    if (e != cudaSuccess) { c->release(); return c->fail(SCORE_ERR_NOMEM, std::string("device allocation: ") + cudaGetErrorString(e)); }
-    a.pforce = c->d_pforce; a.pforce32 = c->d_pforce32;
-    a.st = c->d_state;
-    // status words: tiles of the grow scans and of the commit scan (26 attempts per full cell)
-    int s = ensure_status(c, 0, (capI + kTileGrow - 1) / kTileGrow + 1);
-    if (s == SCORE_OK) s = ensure_status(c, 1, (capB + kTileGrow - 1) / kTileGrow + 1);
-    if (s == SCORE_OK) s = ensure_status(c, 2, (std::min<uint64_t>(26ull * N, 0xFFFFFFFFull) + kTileGrow - 1) / kTileGrow + 1);
-    if (s != SCORE_OK) { c->release(); return s; }
-
-    e = cudaMemcpyAsync(a.grid, grid, N * 4, cudaMemcpyHostToDevice, c->stream);
-    if (e == cudaSuccess) e = cudaMemsetAsync(a.claim, 0xFF, N * 4, c->stream);
-    if (e == cudaSuccess) {
-        if (ptable) e = cudaMemcpyAsync(a.ptab, ptable, ptab_words * 8, cudaMemcpyHostToDevice, c->stream);
-        else e = cudaMemsetAsync(a.ptab, 0xFF, std::max<size_t>(ptab_words, 1) * 8, c->stream);
+    cudaError_t e = cudaSuccess;
+    if (!reuse) {
+        a.nx = c->nx; a.ny = c->ny; a.nz = c->nz; a.nxy = c->nx * c->ny;
+        a.dnx = make_fastdiv(c->nx); a.dnxy = make_fastdiv(c->nx * c->ny);
+        a.ndefg = ndefg; a.nrxg = nrxg;
+        a.border_ref_cap = 2 * ((c->nx * c->ny) + (c->nx * c->nz) + (c->ny * c->nz));
+        a.border_policy = p.border_policy; a.boundary = p.boundary; a.mobility_model = p.mobility_model;
+        // capacities: at most N infections ever happen, so N slots per list never overflow
+        const uint32_t capI = (uint32_t)N;
+        const uint32_t capB = (p.border_policy == SCORE_BORDER_REFERENCE_LIMIT) ? std::min<uint32_t>((uint32_t)N, a.border_ref_cap + 1) : (uint32_t)N;
+        // recycle-list caps (ompshar_init_myRXFront{Inside,Border}, SCORE_Kernel.cpp:3615, 3670)
+        const uint32_t recI = (uint32_t)(p.initial_cache * (double)N * p.maxfillperstep * kFullRecyclingFactor);
+        const uint32_t recB = (uint32_t)((double)a.border_ref_cap * p.maxfillperstep * kFullRecyclingFactor);
+        const uint32_t caps[2] = {capI, capB}, recs[2] = {recI, recB};
+        const size_t fb = c->fp32 ? 4 : 8;
+        for (int L = 0; L < 2; ++L) {
+            DFront& f = a.f[L];
+            f.cap = caps[L]; f.reccap = recs[L];
+            if (e == cudaSuccess) e = cudaMalloc(&f.fill, (size_t)caps[L] * fb);
+            if (e == cudaSuccess && c->fp32) e = cudaMalloc((void**)&f.comp, (size_t)caps[L] * 4);
+            if (e == cudaSuccess) e = cudaMalloc(&f.vel, (size_t)caps[L] * fb);
+            if (e == cudaSuccess && !c->fp32) e = dalloc(&f.inc, caps[L]);
+            if (e == cudaSuccess) e = dalloc(&f.defg, caps[L]);
+            if (e == cudaSuccess) e = dalloc(&f.rxg, caps[L]);
+            if (e == cudaSuccess) e = dalloc(&f.xyz, caps[L]);
+            if (e == cudaSuccess) e = dalloc(&f.dir, caps[L]);
+            if (e == cudaSuccess) e = dalloc(&f.full, caps[L]);
+            if (e == cudaSuccess) e = dalloc(&f.recyc, recs[L]);
+        }
+        // look-back words: grow tiles of both lists, commit tiles over at most N full cells
+        a.status_off1 = capI / kTile + 2;
+        a.status_off2 = a.status_off1 + capB / kTile + 2;
+        a.status_words = a.status_off2 + (uint32_t)(N / kBlock) + 2;  // commit tiles hold kBlock full cells
+        a.misscap = a.pendcap = (uint32_t)std::min<uint64_t>(N, 1ull << 25);
+        if (e == cudaSuccess) e = dalloc(&a.grid, N);
+        if (e == cudaSuccess) e = dalloc(&c->d_grid_init, N);
+        if (e == cudaSuccess) e = dalloc(&a.claim, N);
+        if (e == cudaSuccess) e = dalloc(&a.amask, N);
+        if (e == cudaSuccess) e = dalloc(&a.ptab, ptab_words);
+        if (e == cudaSuccess) e = dalloc(&a.defg_cnt, ndefg);
+        if (e == cudaSuccess) e = dalloc(&c->d_defg_cnt_init, ndefg);
+        if (e == cudaSuccess) e = dalloc(&a.rxg_cnt, nrxg);
+        if (e == cudaSuccess) e = dalloc(&a.depleted, ndefg);
+        if (e == cudaSuccess) e = dalloc(&a.miss, a.misscap);
+        if (e == cudaSuccess) e = dalloc(&a.pending, a.pendcap);
+        if (e == cudaSuccess) e = dalloc(&a.status, a.status_words);
+        if (e == cudaSuccess) e = dalloc(&a.tickets, 8);
+        if (e == cudaSuccess) e = dalloc(&c->d_state, 1);
+        if (e == cudaSuccess) e = dalloc(&c->d_snap, 1);
+        if (e == cudaSuccess) e = dalloc(&c->d_pforce, ndefg);
+        if (e == cudaSuccess) e = dalloc(&c->d_u32tmp, 64);
+        if (e != cudaSuccess) { c->release_domain(); return c->fail(SCORE_ERR_NOMEM, std::string("device allocation: ") + cudaGetErrorString(e)); }
+        a.pforce = c->d_pforce;
+        a.st = c->d_state;
+        c->high_water[0] = a.f[0].cap; c->high_water[1] = a.f[1].cap;  // the reset clears every slot once
+    } else {
+        c->high_water[0] = std::max(c->high_water[0], c->next_never[0]);
+        c->high_water[1] = std::max(c->high_water[1], c->next_never[1]);
     }
-    if (e == cudaSuccess) e = cudaMemsetAsync(a.defg_cnt, 0, (size_t)ndefg * 4, c->stream);
-    if (e == cudaSuccess) e = cudaMemsetAsync(a.rxg_cnt, 0, std::max<size_t>(nrxg, 1) * 4, c->stream);
+    e = cudaMemcpyAsync(c->d_grid_init, grid, N * 4, cudaMemcpyHostToDevice, c->stream);
+    if (e == cudaSuccess && ptable) e = cudaMemcpyAsync(a.ptab, ptable, ptab_words * 8, cudaMemcpyHostToDevice, c->stream);
+    if (e == cudaSuccess) e = cudaMemsetAsync(c->d_defg_cnt_init, 0, (size_t)ndefg * 4, c->stream);
     if (e == cudaSuccess) e = cudaMemsetAsync(c->d_state, 0, sizeof(DevState), c->stream);
     if (e != cudaSuccess) return c->cuda_fail(e, "load domain");
     // per-grain cell counts (solve_REPLACE_CA_STRUCTURE, SCORE_Kernel.cpp:6394-6400)
-    k_count_defg<<<blocks_for(N, c->sms, 16), kBlock, 0, c->stream>>>(a.grid, N, ndefg, a.defg_cnt, (uint32_t*)((char*)c->d_state + offsetof(DevState, err)));
+    k_count_defg<<<blocks_for(N, c->sms, 16), kBlock, 0, c->stream>>>(c->d_grid_init, N, ndefg, c->d_defg_cnt_init,
+                                                                      (uint32_t*)((char*)c->d_state + offsetof(DevState, err)));
     c->launches++;
-    c->defg_cnt_host.assign(ndefg, 0);
-    e = cudaMemcpyAsync(c->defg_cnt_host.data(), a.defg_cnt, (size_t)ndefg * 4, cudaMemcpyDeviceToHost, c->stream);
+    c->defg_cnt_init_host.assign(ndefg, 0);
+    e = cudaMemcpyAsync(c->defg_cnt_init_host.data(), c->d_defg_cnt_init, (size_t)ndefg * 4, cudaMemcpyDeviceToHost, c->stream);
     if (e == cudaSuccess) e = cudaMemcpyAsync(c->h_state, c->d_state, sizeof(DevState), cudaMemcpyDeviceToHost, c->stream);
     if (e == cudaSuccess) e = cudaStreamSynchronize(c->stream);
     if (e != cudaSuccess) return c->cuda_fail(e, "count grains");
     if (c->h_state->err) return c->fail(SCORE_ERR_ARG, "grid holds ids >= ndefg");
+    return reset_state(c);
+}
 
-    // start of solve_RXGROWTH (SCORE_Kernel.cpp:6513-6530): rho max, T, G/b, mobilities, dt0
-    Physics& ph = c->ph;
-    ph.init(&c->prm);
-    ph.rhomax = rhomax_of(c->rho, c->defg_cnt_host);
-    ph.update_temperature();
-    ph.update_atomistic();
-    ph.update_mobilities();
-    ph.dt = ph.dt_minimum();
-    s = upload_pforce(c);
-    if (s != SCORE_OK) return s;
-    c->Xcells = 0.0; c->step = 0; c->defrag_cnt = 0; c->n_nuclei = 0;
-    c->next_never[0] = c->next_never[1] = 0;
-    c->high_water[0] = c->high_water[1] = 0;
-    c->tm = score_timing{};
-    c->last = score_step_stats{};
-    c->last.dt = ph.dt;
-    c->last.rhomax = ph.rhomax;
-    c->loaded = true;
-    return SCORE_OK;
+int score_restart(score_ctx* c) {
+    if (!c) return SCORE_ERR_ARG;
+    if (!c->a.grid || c->ndefg == 0) return c->fail(SCORE_ERR_STATE, "no domain loaded");
+    cudaSetDevice(c->device);
+    c->high_water[0] = std::max(c->high_water[0], c->next_never[0]);
+    c->high_water[1] = std::max(c->high_water[1], c->next_never[1]);
+    return reset_state(c);
 }
 
 int score_place_nuclei(score_ctx* c, uint32_t* n_placed) {
     if (!c) return SCORE_ERR_ARG;
     if (!c->loaded) return c->fail(SCORE_ERR_STATE, "no domain loaded");
+    if (c->failed) return SCORE_ERR_STATE;
     cudaSetDevice(c->device);
     return place_nuclei_upto(c, c->ph.t, n_placed);
 }
@@ -673,36 +737,33 @@ int score_step(score_ctx* c, score_step_stats* out) {
         for (int L = 0; L < 2; ++L) { s = defragment(c, L); if (s != SCORE_OK) return s; }
         c->defrag_cnt++;
     }
-    set_mobility_args(c);
+    set_step_args(c);
     DomainArgs& a = c->a;
+    a.dt_changed = (c->ph.dt != c->dt_cached) ? 1 : 0;
+    c->dt_cached = c->ph.dt;
     cudaStream_t st = c->stream;
-    cudaMemsetAsync((char*)c->d_state + kStepFieldsOffset, 0, sizeof(DevState) - kStepFieldsOffset, st);
-    cudaMemsetAsync(c->d_tickets, 0, 8 * sizeof(uint32_t), st);
-    for (int L = 0; L < 2; ++L)
-        cudaMemsetAsync(c->d_status[L], 0, ((size_t)(c->next_never[L] + kTileGrow - 1) / kTileGrow + 1) * 8, st);
-    cudaMemsetAsync(c->d_status[2], 0, c->status_words[2] * 8, st);
     cudaEventRecord(c->ev[0], st);
     for (int L = 0; L < 2; ++L) {
-        const uint32_t tiles = (c->next_never[L] + kTileGrow - 1) / kTileGrow;
-        const uint32_t grid = std::max<uint32_t>(1, std::min<uint32_t>(tiles, (uint32_t)c->sms * 4));
-        if (c->fp32) k_grow<true><<<grid, kBlock, 0, st>>>(a, L, c->d_status[L], c->d_tickets + L);
-        else k_grow<false><<<grid, kBlock, 0, st>>>(a, L, c->d_status[L], c->d_tickets + L);
+        const uint32_t tiles = (c->next_never[L] + kTile - 1) / kTile;
+        const uint32_t grid = std::max<uint32_t>(1, std::min<uint32_t>(tiles, (uint32_t)c->sms * 5));
+        if (c->fp32) {
+            if (c->refresh) k_grow<true, true><<<grid, kBlock, 0, st>>>(a, L);
+            else k_grow<true, false><<<grid, kBlock, 0, st>>>(a, L);
+        } else {
+            if (c->refresh) k_grow<false, true><<<grid, kBlock, 0, st>>>(a, L);
+            else k_grow<false, false><<<grid, kBlock, 0, st>>>(a, L);
+        }
     }
+    c->refresh = false;
     cudaEventRecord(c->ev[1], st);
-    const uint32_t pgrid = (uint32_t)c->sms * 8;
-    k_claim<<<pgrid, kBlock, 0, st>>>(a);
+    k_claim<<<(uint32_t)c->sms * 4, kBlock, 0, st>>>(a);
     cudaEventRecord(c->ev[2], st);
-    if (c->fp32) {
-        k_commit<true><<<(uint32_t)c->sms * 4, kBlock, 0, st>>>(a, c->d_status[2], c->d_tickets + 2);
-        k_finalize<true><<<pgrid, kBlock, 0, st>>>(a);
-    } else {
-        k_commit<false><<<(uint32_t)c->sms * 4, kBlock, 0, st>>>(a, c->d_status[2], c->d_tickets + 2);
-        k_finalize<false><<<pgrid, kBlock, 0, st>>>(a);
-    }
-    k_step_end<<<1, 1, 0, st>>>(c->d_state, a.f[0].cap, a.f[1].cap);
+    if (c->fp32) k_commit<true><<<(uint32_t)c->sms * 4, kBlock, 0, st>>>(a);
+    else k_commit<false><<<(uint32_t)c->sms * 4, kBlock, 0, st>>>(a);
+    k_step_end<<<(uint32_t)c->sms, kBlock, 0, st>>>(a, c->d_snap);
     cudaEventRecord(c->ev[3], st);
-    c->launches += 6;
-    cudaError_t e = cudaMemcpyAsync(c->h_state, c->d_state, sizeof(DevState), cudaMemcpyDeviceToHost, st);
+    c->launches += 5;
+    cudaError_t e = cudaMemcpyAsync(c->h_state, c->d_snap, sizeof(DevState), cudaMemcpyDeviceToHost, st);
     if (e == cudaSuccess) e = cudaStreamSynchronize(st);
     if (e != cudaSuccess) { c->failed = true; return c->cuda_fail(e, "growth step"); }
     const DevState hs = *c->h_state;
@@ -714,8 +775,9 @@ int score_step(score_ctx* c, score_step_stats* out) {
     c->tm.grow_ms += ms_grow; c->tm.claim_ms += ms_claim; c->tm.commit_ms += ms_commit;
     c->tm.total_ms += ms_grow + ms_claim + ms_commit;
     c->tm.grow_launches += 2;
-    c->tm.kernel_launches += 6;
-    const double bpu = c->fp32 ? 25.0 : 29.0;
+    c->tm.kernel_launches += 5;
+    // algorithmic bytes: grow 25 B (FP64: dir 1, vel 8, fill 8 r + 8 w) or 17 B (FP32: dir, vel 4, fill 4 + comp 4 r/w)
+    const double bpu = c->fp32 ? 17.0 : 25.0;
     const uint64_t Sv = hs.sv[0] + hs.sv[1], nfull = (uint64_t)hs.nfull[0] + hs.nfull[1], nnew = (uint64_t)hs.nwin[0] + hs.nwin[1];
     c->tm.grow_bytes += bpu * (double)Sv;
     c->tm.step_bytes += bpu * (double)Sv + 120.0 * (double)nfull + 37.0 * (double)nnew;
@@ -755,6 +817,7 @@ int score_step(score_ctx* c, score_step_stats* out) {
         if (e == cudaSuccess) e = cudaStreamSynchronize(st);
         if (e != cudaSuccess) return c->cuda_fail(e, "read depleted grains");
         for (uint32_t g : dep) c->defg_cnt_host[g] = 0;
+        c->rhomax_version = ~0ull;  // the set of grains with cells left changed
     }
     for (int L = 0; L < 2; ++L) {
         c->next_never[L] = hs.next_never[L];
@@ -766,24 +829,30 @@ int score_step(score_ctx* c, score_step_stats* out) {
     if (pmax_new >= ph.Pmax) ph.Pmax = pmax_new;  // running max over every P ever assigned, floored at 0
     c->Xcells = c->Xcells + (double)nfull;
     const double X = (c->Xcells / (double)c->N);
-    ph.rhomax = rhomax_of(c->rho, c->defg_cnt_host);
+    if (c->rhomax_version != c->rho_version) {  // rho max only moves when rho or the grain set changes
+        ph.rhomax = rhomax_of(c->rho, c->defg_cnt_host);
+        c->rhomax_version = c->rho_version;
+    }
     const double rhomax_step = ph.rhomax;
     ph.t += ph.dt;
     ph.update_temperature();
     ph.update_atomistic();
     ph.update_microchemistry();
     ph.update_mobilities();
-    ph.update_substructure(c->rho, c->rho0);
+    if (c->prm.recovery_model != SCORE_RECOVERY_NONE && c->prm.recovery_model != SCORE_RECOVERY_NES_SOLUTEDRAG) {
+        ph.update_substructure(c->rho, c->rho0);
+        c->rho_version++;
+    }
     ph.dt = ph.dt_minimum();
     c->step++;
-    s = upload_pforce(c);
+    s = upload_physics(c);
     if (s != SCORE_OK) return s;
 
     score_step_stats& o = c->last;
     o = score_step_stats{};
     o.step = c->step; o.n_nuclei = newnuc; o.t = ph.t; o.dt = ph.dt; o.dt_used = dt_used;
     o.Xcells = c->Xcells; o.X = X; o.Sv = Sv; o.n_full = nfull; o.n_new = nnew;
-    o.Pmax = ph.Pmax; o.rhomax = rhomax_step; o.dXstep = hs.dv[0] + hs.dv[1];
+    o.Pmax = ph.Pmax; o.rhomax = rhomax_step; o.dXstep = 0.0;
     o.next_never[0] = c->next_never[0]; o.next_never[1] = c->next_never[1];
     o.n_recycled[0] = hs.nrec[0]; o.n_recycled[1] = hs.nrec[1];
     o.p_misses = hs.nmiss;
@@ -808,6 +877,12 @@ int score_run_until(score_ctx* c, double x_target, score_step_stats* trace, uint
         ++k;
     }
     if (n_steps) *n_steps = k;
+    cudaEventRecord(c->ev[5], c->stream);
+    cudaError_t e = cudaEventSynchronize(c->ev[5]);
+    float ms = 0.0f;
+    if (e == cudaSuccess) e = cudaEventElapsedTime(&ms, c->ev[4], c->ev[5]);
+    if (e != cudaSuccess) return c->cuda_fail(e, "run timing");
+    c->tm.run_ms = ms;
     return SCORE_OK;
 }
 
@@ -823,10 +898,8 @@ int score_export_labels(score_ctx* c, uint32_t* labels) {
     if (!c || !labels) return SCORE_ERR_ARG;
     if (!c->loaded) return c->fail(SCORE_ERR_STATE, "no domain loaded");
     cudaSetDevice(c->device);
-    uint32_t* d_lab = nullptr;
-    cudaError_t e = cudaMalloc(&d_lab, c->N * 4);
-    if (e != cudaSuccess) return c->fail(SCORE_ERR_NOMEM, "label buffer");
-    e = cudaMemcpyAsync(d_lab, c->a.grid, c->N * 4, cudaMemcpyDeviceToDevice, c->stream);
+    uint32_t* d_lab = c->a.amask;  // N words, free between steps
+    cudaError_t e = cudaMemcpyAsync(d_lab, c->a.grid, c->N * 4, cudaMemcpyDeviceToDevice, c->stream);
     for (int L = 0; L < 2 && e == cudaSuccess; ++L) {
         const uint32_t n = c->next_never[L];
         if (n == 0) continue;
@@ -836,7 +909,6 @@ int score_export_labels(score_ctx* c, uint32_t* labels) {
     }
     if (e == cudaSuccess) e = cudaMemcpyAsync(labels, d_lab, c->N * 4, cudaMemcpyDeviceToHost, c->stream);
     if (e == cudaSuccess) e = cudaStreamSynchronize(c->stream);
-    cudaFree(d_lab);
     if (e != cudaSuccess) return c->cuda_fail(e, "export labels");
     return SCORE_OK;
 }

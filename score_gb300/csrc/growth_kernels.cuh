@@ -1,21 +1,32 @@
 // sm_103a kernels of one recrystallization growth step.
 //
-//   k_grow      per list: FP64 (or FP32+Kahan) fill update of every ACTIVE slot in
-//               [0, next_never), ordered compaction of full slots (FullRX list) and of
-//               INACTIVE slots (recycle list, capped), fused Sv / dV reductions.
-//               caregionMemHdl::ompshar_sim_myCA_calcGrowthStep{Inside,Border},
-//               SCORE_Kernel.cpp:4046-4130, 4183-4249.
-//   k_claim     one thread per infection attempt (full cell x 26 directions, in the
-//               reference's sequential order = the attempt ordinal): atomicMin of the
-//               ordinal into the target's claim word if the target is still deformed.
-//   k_commit    winners (claim == own ordinal) are ranked per destination list in
-//               ordinal order (look-back scan) and take recycled slots first, then
-//               appended ones, exactly like omp_getNextFreeSlotInRXFront*(CELLRECYCLE);
-//               the new front cell gets the overshoot carry, P, grain ids.
-//               ompshar_sim_myCA_updateFullRX{Inside,Border} + omp_infect_OutOfRXFront*,
-//               SCORE_Kernel.cpp:4252-4774.
-//   k_finalize  full cells become recrystallized: grid label ndefg+rxg, grain counts,
-//               slot INACTIVE (the tail of the same functions, :4640-4653, :4752-4764).
+// GB300 executes FP64 at 1/64 of the FP32 rate, so the bit-exact FP64 path keeps
+// FP64 instructions off the per-update critical path.  Every front cell stores
+//   vel = (m(P) * p(defg)) * f_geo(infector)      (the reference's first three roundings)
+//   inc = (vel * dt) * (1/cellsize)               (its fill increment for the current dt)
+// vel is computed once when the cell is infected (again only when T, rho or the drag
+// change); inc is recomputed only when dt changed or for cells infected in the last
+// step (kStale bit of the infector byte).  A typical update is then one DADD,
+//   fill = fill + inc,
+// with the "fill >= 1" test on the integer bit pattern (fill is never negative).
+// A cell whose driving force is <= 5e-16 stores vel = inc = -1 and is skipped, as the
+// reference skips it (calcGrowthStepInside, SCORE_Kernel.cpp:4046-4130).
+//
+//   k_grow    per list: fill update of every ACTIVE slot in [0, next_never), ordered
+//             compaction of full slots (FullRX list) and INACTIVE slots (recycle list,
+//             capped) with a decoupled look-back scan; Sv count.
+//   k_claim   one thread per full cell: the 26 infection attempts in the reference's
+//             order; a still-deformed target gets atomicMin(claim, attempt ordinal),
+//             where ordinal = 26 * (full-cell rank, Inside list first) + direction rank.
+//             The thread records which attempts it made (26-bit mask).
+//   k_commit  one thread per full cell, tiles in full-cell order: attempts whose claim
+//             holds the own ordinal won; winners are ranked per destination list by a
+//             look-back scan and take recycled slots first, then appended slots, like
+//             omp_getNextFreeSlotInRXFront*(CELLRECYCLE).  The full cell then becomes
+//             recrystallized (grid = ndefg + rxg, counts, slot INACTIVE) — the tail of
+//             updateFullRX{Inside,Border}, SCORE_Kernel.cpp:4559-4774.
+//   k_step_end  slot high-water marks, stats snapshot, reset of the per-step fields and
+//             of the look-back status words for the next step.
 #pragma once
 #include <cstdint>
 #include "device_common.cuh"
@@ -25,52 +36,75 @@ namespace score {
 struct DFront {
     void* fill;          // double (FP64) or float (FP32)
     float* comp;         // Kahan compensation (FP32 only)
-    void* P;             // double (FP64) or float (FP32)
+    void* vel;           // double (FP64) or float (FP32): (m p) f_geo, or -1 = no driving force
+    double* inc;         // FP64 only: cached (vel dt) / cellsize for the current dt
     uint32_t* defg;
     uint32_t* rxg;
     uint32_t* xyz;       // linear cell index x + y nx + z nx ny
-    uint8_t* dir;        // infector code 0..26, kInactive = INACTIVE
+    uint8_t* dir;        // infector code 0..26 (| kStale), kInactive = INACTIVE
     uint32_t* full;      // FullRX list (slot indices, slot order)
     uint32_t* recyc;     // recycle list (slot indices, slot order, capped)
     uint32_t cap;        // device capacity of the slot arrays
     uint32_t reccap;     // ntotalRecyclingList of the reference
 };
 
+// n / d for n < 2^31 by multiply-high (Granlund-Montgomery), d >= 1
+struct FastDiv {
+    uint32_t d, mul, shr;
+};
+inline FastDiv make_fastdiv(uint32_t d) {
+    FastDiv f{d, 0u, 0u};
+    if (d > 1) {
+        uint32_t l = 0;
+        while ((1ull << l) < d) ++l;  // ceil(log2 d)
+        const uint32_t p = 31 + l;
+        f.mul = (uint32_t)(((1ull << p) + d - 1) / d);
+        f.shr = p - 32;
+    }
+    return f;
+}
+__device__ __forceinline__ uint32_t fdiv(uint32_t n, const FastDiv& f) {
+    return f.d == 1 ? n : (__umulhi(n, f.mul) >> f.shr);
+}
+
 struct DomainArgs {
     DFront f[2];
     DevState* st;
     uint32_t* grid;
     uint32_t* claim;
+    uint32_t* amask;            // per full cell: attempts made (bit d)
     unsigned long long* ptab;   // nrxg x ndefg mobility weights as bits (kPtabEmpty = unknown)
     const double* pforce;       // per deformed grain driving force (FP64)
-    const float* pforce32;
     uint32_t* defg_cnt;
     uint32_t* rxg_cnt;
     uint32_t* depleted;
     unsigned long long* miss;   // table indices the host must fill
     uint32_t* pending;          // (list << 31) | slot of new cells waiting for P
+    unsigned long long* status; // look-back words: [0, s1) list 0, [s1, s2) list 1, [s2, s3) commit
+    uint32_t* tickets;          // tile tickets: 0,1 grow lists, 2 commit
+    uint32_t status_off1, status_off2, status_words;
     uint32_t misscap, pendcap;
     uint32_t nx, ny, nz, nxy;
+    FastDiv dnx, dnxy;
     uint32_t ndefg, nrxg;
     uint32_t border_ref_cap;
     int32_t border_policy, boundary, mobility_model;
+    int32_t dt_changed;         // dt differs from the dt the cached increments were made with
     double mLAGB, mHAGB, mGS, mRH, dt, cinv;
-    float mLAGB32, mHAGB32, mGS32, mRH32, dtc32;
+    float dtc32;
 };
 
 __device__ __forceinline__ void decode(const DomainArgs& a, uint32_t cell, int& x, int& y, int& z) {
-    z = (int)(cell / a.nxy);
-    uint32_t r = cell - (uint32_t)z * a.nxy;
-    y = (int)(r / a.nx);
-    x = (int)(r - (uint32_t)y * a.nx);
+    const uint32_t zz = fdiv(cell, a.dnxy);
+    const uint32_t r = cell - zz * a.nxy;
+    const uint32_t yy = fdiv(r, a.dnx);
+    x = (int)(r - yy * a.nx); y = (int)yy; z = (int)zz;
 }
 
-// Target cell of attempt d from a cell of list L.  Inside cells are strictly interior
-// so their neighbours need no wrap; Border cells wrap x,y periodically and drop z
-// (reference) or wrap z (periodic build option).  Returns false if the attempt is dropped.
-__device__ __forceinline__ bool target_of(const DomainArgs& a, int L, uint32_t cell, int d, uint32_t& t) {
-    int x, y, z;
-    decode(a, cell, x, y, z);
+// Target of attempt d from (x,y,z) of a cell of list L.  Inside cells are strictly
+// interior so their neighbours need no wrap; Border cells wrap x,y periodically and
+// drop z (reference) or wrap z (periodic build option).  false = attempt dropped.
+__device__ __forceinline__ bool target_of(const DomainArgs& a, int L, int x, int y, int z, int d, uint32_t& t, bool& interior) {
     int tx = x + c_dx[d], ty = y + c_dy[d], tz = z + c_dz[d];
     if (L == 1) {
         if (tx < 0) tx += (int)a.nx;
@@ -87,26 +121,25 @@ __device__ __forceinline__ bool target_of(const DomainArgs& a, int L, uint32_t c
         atomicOr(&a.st->err, kErrBounds);
         return false;
     }
+    interior = tx > 0 && tx < (int)a.nx - 1 && ty > 0 && ty < (int)a.ny - 1 && tz > 0 && tz < (int)a.nz - 1;
     t = (uint32_t)tx + a.nx * ((uint32_t)ty + a.ny * (uint32_t)tz);
     return true;
 }
 
-// Inside full cells closer than 2 cells to a face send every infection to the Border
-// list (InfectIntoBorder, SCORE_Kernel.cpp:4606-4609).
-__device__ __forceinline__ bool into_border(const DomainArgs& a, uint32_t cell) {
-    int x, y, z;
-    decode(a, cell, x, y, z);
-    return !(x > 1 && x < (int)a.nx - 2 && y > 1 && y < (int)a.ny - 2 && z > 1 && z < (int)a.nz - 2);
+// mobility m(P) of the reference (get_currentintrinsicmobility, SCORE_Kernel.cpp:5459-5470)
+__device__ __forceinline__ double mobility(const DomainArgs& a, double P) {
+    if (a.mobility_model == 2) return __dmul_rn(P, a.mRH);
+    if (P < 0.0) return a.mLAGB;
+    return __dadd_rn(__dmul_rn(P, a.mGS), __dmul_rn(__dsub_rn(1.0, P), a.mHAGB));
 }
-// Border full cells route strictly interior targets to the Inside list (:4387).
-__device__ __forceinline__ bool strictly_interior(const DomainArgs& a, uint32_t cell) {
-    int x, y, z;
-    decode(a, cell, x, y, z);
-    return x > 0 && x < (int)a.nx - 1 && y > 0 && y < (int)a.ny - 1 && z > 0 && z < (int)a.nz - 1;
+// velocity factor (m p) f_geo, or -1 when the driving force is not above 5e-16
+__device__ __forceinline__ double velocity_factor(const DomainArgs& a, double P, uint32_t defg, int code) {
+    const double p = a.pforce[defg];
+    if (!(p > 5.0e-16)) return -1.0;
+    return __dmul_rn(__dmul_rn(mobility(a, P), p), c_sf[code]);
 }
 
-// warp-0 exclusive scan of 2*32 tile counters laid out [item][warp]; returns the two
-// tile totals in lane 0.  cntA/cntB are rewritten with exclusive offsets.
+// warp-0 exclusive scan of 2x64 tile counters laid out [item][warp]; tile totals in lane 0
 __device__ __forceinline__ void scan64_pair(uint32_t* cntA, uint32_t* cntB, uint32_t& totA, uint32_t& totB) {
     const int lane = threadIdx.x & 31;
     uint32_t a0 = cntA[2 * lane], a1 = cntA[2 * lane + 1], b0 = cntB[2 * lane], b1 = cntB[2 * lane + 1];
@@ -124,74 +157,116 @@ __device__ __forceinline__ void scan64_pair(uint32_t* cntA, uint32_t* cntB, uint
 }
 
 // ------------------------------------------------------------------ K1 grow
-template <bool FP32>
-__global__ void __launch_bounds__(kBlock) k_grow(DomainArgs a, int L, unsigned long long* status, uint32_t* ticket) {
-    constexpr int ITEMS = 8;  // ITEMS * kWarps must be 64 for scan64_pair
+// REFRESH: recompute vel of every active slot from the P table and the current
+// physics (after T, rho or the drag changed) before growing it.
+template <bool FP32, bool REFRESH>
+__global__ void __launch_bounds__(kBlock, 5) k_grow(DomainArgs a, int L) {
+    constexpr int ITEMS = 8;  // ITEMS * kWarps == 64 for scan64_pair
     constexpr uint32_t TILE = kBlock * ITEMS;
     const DFront fr = a.f[L];
+    unsigned long long* status = a.status + (L == 0 ? 0u : a.status_off1);
+    uint32_t* ticket = a.tickets + L;
     const uint32_t n = a.st->next_never[L];
     const uint32_t ntiles = (n + TILE - 1) / TILE;
     __shared__ uint32_t s_tile, s_exF, s_exI;
     __shared__ uint32_t s_cntF[ITEMS * kWarps], s_cntI[ITEMS * kWarps];
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     unsigned long long sv = 0;
-    double dv = 0.0;
     for (;;) {
         if (threadIdx.x == 0) s_tile = atomicAdd(ticket, 1u);
         __syncthreads();
         const uint32_t tile = s_tile;
         if (tile >= ntiles) break;
         const uint32_t base = tile * TILE;
-        uint32_t fm[ITEMS], im[ITEMS];
+        uint8_t d[ITEMS];
 #pragma unroll
         for (int k = 0; k < ITEMS; ++k) {
             const uint32_t slot = base + (uint32_t)(k * kBlock) + threadIdx.x;
-            const bool valid = slot < n;
-            const uint8_t d = valid ? fr.dir[slot] : kInactive;
-            const bool inact = valid && d == kInactive;
-            bool full = false;
-            if (valid && d != kInactive) {
-                ++sv;
-                const uint32_t g = fr.defg[slot];
-                if (!FP32) {
-                    const double P = ((const double*)fr.P)[slot];
-                    double m;
-                    if (a.mobility_model == 2) m = __dmul_rn(P, a.mRH);
-                    else if (P < 0.0) m = a.mLAGB;
-                    else m = __dadd_rn(__dmul_rn(P, a.mGS), __dmul_rn(__dsub_rn(1.0, P), a.mHAGB));
-                    const double p = a.pforce[g];
-                    if (p > 5.0e-16) {
-                        double v = __dmul_rn(m, p);
-                        v = __dmul_rn(v, c_sf[d]);
-                        const double inc = __dmul_rn(__dmul_rn(v, a.dt), a.cinv);
-                        const double f = __dadd_rn(((double*)fr.fill)[slot], inc);
-                        ((double*)fr.fill)[slot] = f;
-                        dv += inc;
-                        full = f >= 1.0;
+            d[k] = slot < n ? fr.dir[slot] : kInactive;
+        }
+        bool full[ITEMS];
+        if (!FP32) {
+            double w[ITEMS], fill[ITEMS];  // w: cached inc, or vel when the increment is stale
+#pragma unroll
+            for (int k = 0; k < ITEMS; ++k) {
+                const uint32_t slot = base + (uint32_t)(k * kBlock) + threadIdx.x;
+                w[k] = -1.0; fill[k] = 0.0;
+                if (d[k] != kInactive) {
+                    if (REFRESH) {
+                        const uint32_t g = fr.defg[slot];
+                        const double P = __longlong_as_double((long long)a.ptab[(unsigned long long)fr.rxg[slot] * a.ndefg + g]);
+                        w[k] = velocity_factor(a, P, g, d[k] & kCodeMask);
+                        ((double*)fr.vel)[slot] = w[k];
+                    } else if (a.dt_changed || (d[k] & kStale)) {
+                        w[k] = ((const double*)fr.vel)[slot];
+                    } else {
+                        w[k] = fr.inc[slot];
                     }
-                } else {
-                    const float P = ((const float*)fr.P)[slot];
-                    float m;
-                    if (a.mobility_model == 2) m = P * a.mRH32;
-                    else if (P < 0.0f) m = a.mLAGB32;
-                    else m = P * a.mGS32 + (1.0f - P) * a.mHAGB32;
-                    const float p = a.pforce32[g];
-                    if (p > 5.0e-16f) {
-                        const float inc = m * p * c_sf32[d] * a.dtc32;
-                        // Kahan-compensated accumulation of the fill
-                        const float f0 = ((float*)fr.fill)[slot];
-                        const float y = inc - fr.comp[slot];
-                        const float t = f0 + y;
-                        const float cnew = (t - f0) - y;
-                        fr.comp[slot] = cnew;
-                        ((float*)fr.fill)[slot] = t;
-                        dv += (double)inc;
-                        full = (t - cnew) >= 1.0f;
+                    fill[k] = ((const double*)fr.fill)[slot];
+                }
+            }
+#pragma unroll
+            for (int k = 0; k < ITEMS; ++k) {
+                full[k] = false;
+                if (d[k] != kInactive) {
+                    ++sv;
+                    const uint32_t slot = base + (uint32_t)(k * kBlock) + threadIdx.x;
+                    double inc = w[k];
+                    if (REFRESH || a.dt_changed || (d[k] & kStale)) {
+                        if (__double_as_longlong(w[k]) >= 0) inc = __dmul_rn(__dmul_rn(w[k], a.dt), a.cinv);
+                        fr.inc[slot] = inc;
+                        if (d[k] & kStale) fr.dir[slot] = d[k] & kCodeMask;
+                    }
+                    if (__double_as_longlong(inc) >= 0) {  // sign bit clear: driving force present
+                        const double f = __dadd_rn(fill[k], inc);
+                        ((double*)fr.fill)[slot] = f;
+                        full[k] = __double_as_longlong(f) >= 0x3FF0000000000000ll;  // f >= 1.0, f never negative
                     }
                 }
             }
-            fm[k] = __ballot_sync(0xFFFFFFFFu, full);
-            im[k] = __ballot_sync(0xFFFFFFFFu, inact);
+        } else {
+            float vel[ITEMS], fill[ITEMS], comp[ITEMS];
+#pragma unroll
+            for (int k = 0; k < ITEMS; ++k) {
+                const uint32_t slot = base + (uint32_t)(k * kBlock) + threadIdx.x;
+                vel[k] = -1.0f; fill[k] = 0.0f; comp[k] = 0.0f;
+                if (d[k] != kInactive) {
+                    if (REFRESH) {
+                        const uint32_t g = fr.defg[slot];
+                        const double P = __longlong_as_double((long long)a.ptab[(unsigned long long)fr.rxg[slot] * a.ndefg + g]);
+                        vel[k] = (float)velocity_factor(a, P, g, d[k] & kCodeMask);
+                        ((float*)fr.vel)[slot] = vel[k];
+                    } else {
+                        vel[k] = ((const float*)fr.vel)[slot];
+                    }
+                    fill[k] = ((const float*)fr.fill)[slot];
+                    comp[k] = fr.comp[slot];
+                }
+            }
+#pragma unroll
+            for (int k = 0; k < ITEMS; ++k) {
+                full[k] = false;
+                if (d[k] != kInactive) {
+                    ++sv;
+                    if (vel[k] >= 0.0f) {
+                        // Kahan-compensated accumulation of the fill
+                        const float inc = vel[k] * a.dtc32;
+                        const float y = inc - comp[k];
+                        const float t = fill[k] + y;
+                        const float c = (t - fill[k]) - y;
+                        const uint32_t slot = base + (uint32_t)(k * kBlock) + threadIdx.x;
+                        ((float*)fr.fill)[slot] = t;
+                        fr.comp[slot] = c;
+                        full[k] = (t - c) >= 1.0f;
+                    }
+                }
+            }
+        }
+        uint32_t fm[ITEMS], im[ITEMS];
+#pragma unroll
+        for (int k = 0; k < ITEMS; ++k) {
+            fm[k] = __ballot_sync(0xFFFFFFFFu, full[k]);
+            im[k] = __ballot_sync(0xFFFFFFFFu, d[k] == kInactive && base + (uint32_t)(k * kBlock) + threadIdx.x < n);
             if (lane == 0) {
                 s_cntF[k * kWarps + warp] = __popc(fm[k]);
                 s_cntI[k * kWarps + warp] = __popc(im[k]);
@@ -225,46 +300,44 @@ __global__ void __launch_bounds__(kBlock) k_grow(DomainArgs a, int L, unsigned l
         }
         __syncthreads();
     }
-    // block-level reductions of the observation counters
 #pragma unroll
-    for (int o = 16; o > 0; o >>= 1) {
-        sv += __shfl_down_sync(0xFFFFFFFFu, sv, o);
-        dv += __shfl_down_sync(0xFFFFFFFFu, dv, o);
-    }
-    if (lane == 0 && sv) {
-        atomicAdd(&a.st->sv[L], sv);
-        atomicAdd(&a.st->dv[L], dv);
-    }
+    for (int o = 16; o > 0; o >>= 1) sv += __shfl_down_sync(0xFFFFFFFFu, sv, o);
+    if (lane == 0 && sv) atomicAdd(&a.st->sv[L], sv);
 }
 
 // ------------------------------------------------------------------ K2 claim
-__device__ __forceinline__ bool attempt_total(const DomainArgs& a, uint32_t& F0, uint32_t& total) {
-    F0 = a.st->nfull[0];
-    const unsigned long long t = 26ull * ((unsigned long long)F0 + a.st->nfull[1]);
-    if (t >= 0xFFFFFFFFull) return false;
-    total = (uint32_t)t;
-    return true;
-}
-
 __global__ void __launch_bounds__(kBlock) k_claim(DomainArgs a) {
-    uint32_t F0, total;
-    if (!attempt_total(a, F0, total)) {
+    const uint32_t F0 = a.st->nfull[0], F = F0 + a.st->nfull[1];
+    if (26ull * F >= 0xFFFFFFFFull) {
         if (blockIdx.x == 0 && threadIdx.x == 0) atomicOr(&a.st->err, kErrKeyLimit);
         return;
     }
-    for (uint32_t o = blockIdx.x * blockDim.x + threadIdx.x; o < total; o += gridDim.x * blockDim.x) {
-        const uint32_t f = o / 26u;
-        const int d = (int)(o - f * 26u);
+    for (uint32_t f = blockIdx.x * blockDim.x + threadIdx.x; f < F; f += gridDim.x * blockDim.x) {
         const int L = f >= F0 ? 1 : 0;
         const uint32_t slot = a.f[L].full[L ? f - F0 : f];
-        uint32_t t;
-        if (!target_of(a, L, a.f[L].xyz[slot], d, t)) continue;
-        if (a.grid[t] < a.ndefg) atomicMin(&a.claim[t], o);
+        int x, y, z;
+        decode(a, a.f[L].xyz[slot], x, y, z);
+        uint32_t tg[26], gv[26];
+        // every neighbour load is issued before the first atomic
+#pragma unroll
+        for (int d = 0; d < 26; ++d) {
+            bool inter;
+            gv[d] = 0xFFFFFFFFu;
+            if (target_of(a, L, x, y, z, d, tg[d], inter)) gv[d] = __ldg(&a.grid[tg[d]]);
+        }
+        uint32_t mask = 0;
+#pragma unroll
+        for (int d = 0; d < 26; ++d) {
+            if (gv[d] < a.ndefg) {
+                atomicMin(&a.claim[tg[d]], f * 26u + (uint32_t)d);
+                mask |= 1u << d;
+            }
+        }
+        a.amask[f] = mask;
     }
 }
 
-// P of a new cell: the infector's P when the deformed grain is the same, else the
-// table entry; unknown entries are requested from the host (returned as pending).
+// P of a new cell from the table; unknown entries are requested from the host
 __device__ __forceinline__ bool lookup_p(const DomainArgs& a, uint32_t rxg, uint32_t defg, double& P) {
     unsigned long long* e = &a.ptab[(unsigned long long)rxg * a.ndefg + defg];
     unsigned long long bits = *(volatile unsigned long long*)e;
@@ -283,150 +356,175 @@ __device__ __forceinline__ bool lookup_p(const DomainArgs& a, uint32_t rxg, uint
     return true;
 }
 
-// ------------------------------------------------------------------ K3 commit
-template <bool FP32>
-__global__ void __launch_bounds__(kBlock) k_commit(DomainArgs a, unsigned long long* status, uint32_t* ticket) {
-    constexpr int ITEMS = 8;
-    constexpr uint32_t TILE = kBlock * ITEMS;
-    uint32_t F0, total;
-    if (!attempt_total(a, F0, total)) return;
-    const uint32_t ntiles = (total + TILE - 1) / TILE;
-    __shared__ uint32_t s_tile, s_exA, s_exB;
-    __shared__ uint32_t s_cntA[ITEMS * kWarps], s_cntB[ITEMS * kWarps];
+// ------------------------------------------------------------------ K3 commit (+ finalize)
+// scan of the per-thread win counts (A: to Inside, B: to Border) over one tile of
+// kBlock full cells: per-warp inclusive scans, then the warp totals
+__device__ __forceinline__ void block_scan_pair(uint32_t cA, uint32_t cB, uint32_t* sA, uint32_t* sB, uint32_t& exA, uint32_t& exB,
+                                                uint32_t& totA, uint32_t& totB) {
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    uint32_t ia = cA, ib = cB;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        const uint32_t xa = __shfl_up_sync(0xFFFFFFFFu, ia, o), xb = __shfl_up_sync(0xFFFFFFFFu, ib, o);
+        if (lane >= o) { ia += xa; ib += xb; }
+    }
+    if (lane == 31) { sA[warp] = ia; sB[warp] = ib; }
+    __syncthreads();
+    uint32_t wa = 0, wb = 0, ta = 0, tb = 0;
+#pragma unroll
+    for (int w = 0; w < kWarps; ++w) {
+        const uint32_t va = sA[w], vb = sB[w];
+        if (w < warp) { wa += va; wb += vb; }
+        ta += va; tb += vb;
+    }
+    exA = wa + ia - cA; exB = wb + ib - cB;
+    totA = ta; totB = tb;
+}
+
+template <bool FP32>
+__global__ void __launch_bounds__(kBlock) k_commit(DomainArgs a) {
+    const uint32_t F0 = a.st->nfull[0], F = F0 + a.st->nfull[1];
+    if (26ull * F >= 0xFFFFFFFFull) return;
+    unsigned long long* status = a.status + a.status_off2;
+    const uint32_t ntiles = (F + kBlock - 1) / kBlock;
+    __shared__ uint32_t s_tile, s_exA, s_exB;
+    __shared__ uint32_t s_wA[kWarps], s_wB[kWarps];
     for (;;) {
-        if (threadIdx.x == 0) s_tile = atomicAdd(ticket, 1u);
+        if (threadIdx.x == 0) s_tile = atomicAdd(a.tickets + 2, 1u);
         __syncthreads();
         const uint32_t tile = s_tile;
         if (tile >= ntiles) break;
-        const uint32_t base = tile * TILE;
-        uint32_t am[ITEMS], bm[ITEMS], tgt[ITEMS];
+        const uint32_t f = tile * kBlock + threadIdx.x;
+        uint32_t win = 0, tob = 0, slot = 0, cell = 0;
+        int L = 0, x = 0, y = 0, z = 0;
+        if (f < F) {
+            const uint32_t mask = a.amask[f];
+            L = f >= F0 ? 1 : 0;
+            slot = a.f[L].full[L ? f - F0 : f];
+            cell = a.f[L].xyz[slot];
+            decode(a, cell, x, y, z);
+            if (mask) {
+                const bool allB = (L == 0) && !(x > 1 && x < (int)a.nx - 2 && y > 1 && y < (int)a.ny - 2 && z > 1 && z < (int)a.nz - 2);
+                uint32_t cl[26];
+                uint32_t inter_m = 0;
 #pragma unroll
-        for (int k = 0; k < ITEMS; ++k) {
-            const uint32_t o = base + (uint32_t)(k * kBlock) + threadIdx.x;
-            bool winA = false, winB = false;
-            tgt[k] = 0;
-            if (o < total) {
-                const uint32_t f = o / 26u;
-                const int d = (int)(o - f * 26u);
-                const int L = f >= F0 ? 1 : 0;
-                const uint32_t slot = a.f[L].full[L ? f - F0 : f];
-                const uint32_t cell = a.f[L].xyz[slot];
-                uint32_t t;
-                if (target_of(a, L, cell, d, t) && a.claim[t] == o) {
-                    const bool toBorder = (L == 0) ? into_border(a, cell) : !strictly_interior(a, t);
-                    winA = !toBorder; winB = toBorder;
-                    tgt[k] = t;
+                for (int d = 0; d < 26; ++d) {
+                    cl[d] = kClaimFree;
+                    if ((mask >> d) & 1u) {
+                        uint32_t t;
+                        bool inter;
+                        target_of(a, L, x, y, z, d, t, inter);
+                        cl[d] = a.claim[t];
+                        if (inter) inter_m |= 1u << d;
+                    }
+                }
+#pragma unroll
+                for (int d = 0; d < 26; ++d) {
+                    if (cl[d] == f * 26u + (uint32_t)d) {
+                        win |= 1u << d;
+                        // Inside full cells near a face infect into the Border list (:4606-4609);
+                        // Border full cells send strictly interior targets to the Inside list (:4387)
+                        if (L == 0 ? allB : !((inter_m >> d) & 1u)) tob |= 1u << d;
+                    }
                 }
             }
-            am[k] = __ballot_sync(0xFFFFFFFFu, winA);
-            bm[k] = __ballot_sync(0xFFFFFFFFu, winB);
-            if (lane == 0) {
-                s_cntA[k * kWarps + warp] = __popc(am[k]);
-                s_cntB[k * kWarps + warp] = __popc(bm[k]);
-            }
+        }
+        const uint32_t cB = __popc(tob), cA = __popc(win) - cB;
+        uint32_t exA, exB, totA, totB;
+        block_scan_pair(cA, cB, s_wA, s_wB, exA, exB, totA, totB);
+        if (threadIdx.x == 0) {
+            uint32_t pA, pB;
+            lookback2(status, tile, totA, totB, pA, pB, &a.st->err);
+            s_exA = pA; s_exB = pB;
+            if (tile == ntiles - 1) { a.st->nwin[0] = pA + totA; a.st->nwin[1] = pB + totB; }
         }
         __syncthreads();
-        if (warp == 0) {
-            uint32_t totA, totB;
-            scan64_pair(s_cntA, s_cntB, totA, totB);
-            if (lane == 0) {
-                uint32_t exA, exB;
-                lookback2(status, tile, totA, totB, exA, exB, &a.st->err);
-                s_exA = exA; s_exB = exB;
-                if (tile == ntiles - 1) { a.st->nwin[0] = exA + totA; a.st->nwin[1] = exB + totB; }
+        if (f < F) {
+            const DFront& src = a.f[L];
+            const uint32_t rsrc = src.rxg[slot], gsrc = src.defg[slot];
+            if (win) {
+                uint32_t rA = s_exA + exA, rB = s_exB + exB;
+                double over = 0.0;
+                float over32 = 0.0f;
+                if (!FP32) over = __dsub_rn(((const double*)src.fill)[slot], 1.0);
+                else over32 = (((const float*)src.fill)[slot] - 1.0f) - src.comp[slot];
+                uint32_t m = win;
+                while (m) {
+                    const int d = __ffs(m) - 1;
+                    m &= m - 1;
+                    uint32_t t;
+                    bool inter;
+                    target_of(a, L, x, y, z, d, t, inter);
+                    const int D = (tob >> d) & 1u;
+                    const uint32_t r = D ? rB++ : rA++;
+                    const DFront& dst = a.f[D];
+                    const uint32_t nrec = a.st->nrec[D];
+                    const uint32_t ns = r < nrec ? dst.recyc[r] : a.st->next_never[D] + (r - nrec);
+                    if (ns >= dst.cap) { atomicOr(&a.st->err, kErrCapacity); continue; }
+                    if (D == 1 && a.border_policy == 0 && r >= nrec && ns >= a.border_ref_cap) atomicOr(&a.st->err, kErrBorderRef);
+                    const uint32_t gt = a.grid[t];
+                    const int cls = c_cls[d];
+                    double P = 0.0;
+                    const bool known = lookup_p(a, rsrc, gt, P);
+                    if (!FP32) {
+                        const double fac = cls == 1 ? 0.0682 : (cls == 2 ? 0.0542 : 0.0484);
+                        ((double*)dst.fill)[ns] = __dmul_rn(over, fac);
+                        ((double*)dst.vel)[ns] = known ? velocity_factor(a, P, gt, c_code[d]) : -1.0;
+                    } else {
+                        const float fac = cls == 1 ? 0.0682f : (cls == 2 ? 0.0542f : 0.0484f);
+                        ((float*)dst.fill)[ns] = over32 * fac;
+                        dst.comp[ns] = 0.0f;
+                        ((float*)dst.vel)[ns] = known ? (float)velocity_factor(a, P, gt, c_code[d]) : -1.0f;
+                    }
+                    dst.dir[ns] = c_code[d] | kStale;
+                    dst.defg[ns] = gt;
+                    dst.rxg[ns] = rsrc;
+                    dst.xyz[ns] = t;
+                    a.grid[t] = 4096002000u;  // CURRENTLY_INFECTED
+                    a.claim[t] = kClaimFree;
+                    if (!known) {
+                        const uint32_t q = atomicAdd(&a.st->npending, 1u);
+                        if (q < a.pendcap) a.pending[q] = ((uint32_t)D << 31) | ns;
+                        else atomicOr(&a.st->err, kErrMissCap);
+                    } else if (P > 0.0) {
+                        atomicMax(&a.st->pmax_bits, (unsigned long long)__double_as_longlong(P));
+                    }
+                }
             }
-        }
-        __syncthreads();
-        const uint32_t lt = lanemask_lt();
-#pragma unroll
-        for (int k = 0; k < ITEMS; ++k) {
-            const bool wA = (am[k] >> lane) & 1u, wB = (bm[k] >> lane) & 1u;
-            if (!(wA || wB)) continue;
-            const int D = wB ? 1 : 0;
-            const uint32_t r = wB ? s_exB + s_cntB[k * kWarps + warp] + __popc(bm[k] & lt)
-                                  : s_exA + s_cntA[k * kWarps + warp] + __popc(am[k] & lt);
-            const uint32_t o = base + (uint32_t)(k * kBlock) + threadIdx.x;
-            const uint32_t f = o / 26u;
-            const int d = (int)(o - f * 26u);
-            const int L = f >= F0 ? 1 : 0;
-            const uint32_t src = a.f[L].full[L ? f - F0 : f];
-            const uint32_t t = tgt[k];
-            const DFront& dst = a.f[D];
-            const uint32_t nrec = a.st->nrec[D];
-            const uint32_t ns = r < nrec ? dst.recyc[r] : a.st->next_never[D] + (r - nrec);
-            if (ns >= dst.cap) { atomicOr(&a.st->err, kErrCapacity); continue; }
-            if (D == 1 && a.border_policy == 0 && r >= nrec && ns >= a.border_ref_cap) atomicOr(&a.st->err, kErrBorderRef);
-            const uint32_t gt = a.grid[t];
-            const uint32_t gsrc = a.f[L].defg[src];
-            const uint32_t rsrc = a.f[L].rxg[src];
-            const int cls = c_cls[d];
-            double P = 0.0;
-            bool known = true;
-            if (!FP32) {
-                const double over = __dsub_rn(((const double*)a.f[L].fill)[src], 1.0);
-                const double fac = cls == 1 ? 0.0682 : (cls == 2 ? 0.0542 : 0.0484);
-                ((double*)dst.fill)[ns] = __dmul_rn(over, fac);
-                if (gsrc == gt) P = ((const double*)a.f[L].P)[src];
-                else known = lookup_p(a, rsrc, gt, P);
-                ((double*)dst.P)[ns] = known ? P : __longlong_as_double((long long)kPtabEmpty);
-            } else {
-                const float over = (((const float*)a.f[L].fill)[src] - 1.0f) - a.f[L].comp[src];
-                const float fac = cls == 1 ? 0.0682f : (cls == 2 ? 0.0542f : 0.0484f);
-                ((float*)dst.fill)[ns] = over * fac;
-                dst.comp[ns] = 0.0f;
-                float P32 = 0.0f;
-                if (gsrc == gt) { P32 = ((const float*)a.f[L].P)[src]; P = (double)P32; }
-                else { known = lookup_p(a, rsrc, gt, P); P32 = (float)P; }
-                ((float*)dst.P)[ns] = known ? P32 : __int_as_float(0x7FFFFFFF);
+            // the full cell is now recrystallized
+            a.grid[cell] = a.ndefg + rsrc;
+            atomicAdd(&a.rxg_cnt[rsrc], 1u);
+            const uint32_t old = atomicSub(&a.defg_cnt[gsrc], 1u);
+            if (old == 1u) {
+                const uint32_t q = atomicAdd(&a.st->ndepleted, 1u);
+                if (q < a.ndefg) a.depleted[q] = gsrc;
             }
-            dst.dir[ns] = c_code[d];
-            dst.defg[ns] = gt;
-            dst.rxg[ns] = rsrc;
-            dst.xyz[ns] = t;
-            a.grid[t] = 4096002000u;  // CURRENTLY_INFECTED
-            a.claim[t] = kClaimFree;
-            if (!known) {
-                const uint32_t q = atomicAdd(&a.st->npending, 1u);
-                if (q < a.pendcap) a.pending[q] = ((uint32_t)D << 31) | ns;
-                else atomicOr(&a.st->err, kErrMissCap);
-            } else if (P > 0.0) {
-                atomicMax(&a.st->pmax_bits, (unsigned long long)__double_as_longlong(P));
-            }
+            src.dir[slot] = kInactive;
+            if (!FP32) ((double*)src.fill)[slot] = 0.0;
+            else { ((float*)src.fill)[slot] = 0.0f; src.comp[slot] = 0.0f; }
         }
         __syncthreads();
     }
 }
 
-// ------------------------------------------------------------------ K4 finalize
-template <bool FP32>
-__global__ void __launch_bounds__(kBlock) k_finalize(DomainArgs a) {
-    const uint32_t F0 = a.st->nfull[0], F = F0 + a.st->nfull[1];
-    for (uint32_t f = blockIdx.x * blockDim.x + threadIdx.x; f < F; f += gridDim.x * blockDim.x) {
-        const int L = f >= F0 ? 1 : 0;
-        const DFront& fr = a.f[L];
-        const uint32_t slot = fr.full[L ? f - F0 : f];
-        const uint32_t r = fr.rxg[slot], g = fr.defg[slot];
-        a.grid[fr.xyz[slot]] = a.ndefg + r;
-        atomicAdd(&a.rxg_cnt[r], 1u);
-        const uint32_t old = atomicSub(&a.defg_cnt[g], 1u);
-        if (old == 1u) {
-            const uint32_t q = atomicAdd(&a.st->ndepleted, 1u);
-            if (q < a.ndefg) a.depleted[q] = g;
+// ------------------------------------------------------------------ K4 step end
+// Thread 0 of block 0 advances the high-water marks, snapshots the per-step fields
+// for the host and clears them and the tickets; all blocks clear the look-back words
+// (no kernel of this step reads them any more).
+__global__ void __launch_bounds__(kBlock) k_step_end(DomainArgs a, DevState* snapshot) {
+    if (blockIdx.x == 0 && threadIdx.x == 0) {
+        DevState* st = a.st;
+        const uint32_t cap[2] = {a.f[0].cap, a.f[1].cap};
+        for (int D = 0; D < 2; ++D) {
+            if (st->nwin[D] > st->nrec[D]) st->next_never[D] += st->nwin[D] - st->nrec[D];
+            if (st->next_never[D] > cap[D]) { st->next_never[D] = cap[D]; st->err |= kErrCapacity; }
         }
-        fr.dir[slot] = kInactive;
-        if (!FP32) ((double*)fr.fill)[slot] = 0.0;
-        else { ((float*)fr.fill)[slot] = 0.0f; fr.comp[slot] = 0.0f; }
+        *snapshot = *st;
+        char* p = (char*)st + kStepFieldsOffset;
+        for (size_t i = 0; i < sizeof(DevState) - kStepFieldsOffset; ++i) p[i] = 0;
+        a.tickets[0] = a.tickets[1] = a.tickets[2] = 0;
     }
-}
-
-// ------------------------------------------------------------------ K5 step end
-__global__ void k_step_end(DevState* st, uint32_t cap0, uint32_t cap1) {
-    const uint32_t cap[2] = {cap0, cap1};
-    for (int D = 0; D < 2; ++D) {
-        if (st->nwin[D] > st->nrec[D]) st->next_never[D] += st->nwin[D] - st->nrec[D];
-        if (st->next_never[D] > cap[D]) { st->next_never[D] = cap[D]; st->err |= kErrCapacity; }
-    }
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < a.status_words; i += gridDim.x * blockDim.x) a.status[i] = 0ull;
 }
 
 }  // namespace score

@@ -295,6 +295,10 @@ class GrowthMachine:
         self._check(self._lib.score_load_domain(self._ctx, _ptr(g), _ptr(dq), _ptr(rho), d.ndefg, _ptr(rq), _ptr(site),
                                                 _ptr(tinc), d.nrxg, _ptr(ptable)))
 
+    def restart(self) -> None:
+        """Back to the just-loaded state from device-resident inputs (no host copy)."""
+        self._check(self._lib.score_restart(self._ctx))
+
     def place_nuclei(self) -> int:
         n = C.c_uint32()
         self._check(self._lib.score_place_nuclei(self._ctx, C.byref(n)))

@@ -13,7 +13,7 @@ import score_gb300 as sg
 
 pytestmark = pytest.mark.gpu
 
-FIELDS_EXACT = ["Xcells", "Sv", "n_full", "t", "dt", "dt_used", "Pmax", "rhomax"]
+FIELDS_EXACT = ["Xcells", "Sv", "n_full", "n_new", "t", "dt", "dt_used", "Pmax", "rhomax"]
 
 
 def run_gpu(p, d, ptable=None, x_target=-1.0):
@@ -23,43 +23,128 @@ def run_gpu(p, d, ptable=None, x_target=-1.0):
         tr = gm.run_until(x_target)
         lab = gm.labels()
         rc, dc = gm.grain_counts()
-        tm = gm.timing()
-    return tr, lab, rc, dc, tm
+    return tr, lab, rc, dc
 
 
-def compare(p, d, ptable=None):
-    ref = oracle.run(p, d, ptable)
-    assert ref["status"] == 0
-    tr, lab, rc, dc, _ = run_gpu(p, d, ptable)
+def assert_same(tr, lab, rc, dc, ref):
     ot = ref["trace"]
     assert len(tr) == len(ot), f"step count {len(tr)} vs oracle {len(ot)}"
     for f in FIELDS_EXACT:
         g = np.array([getattr(s, f) for s in tr])
-        assert np.array_equal(g, ot[f]), f"{f} differs at step {int(np.argmax(g != ot[f]))}"
+        assert np.array_equal(g, ot[f]), f"{f} differs first at step {int(np.argmax(g != ot[f]))}"
     nn = np.array([list(s.next_never) for s in tr])
     assert np.array_equal(nn, ot["next_never"]), "slot high-water marks differ (slot order diverged)"
     nr = np.array([list(s.n_recycled) for s in tr])
     assert np.array_equal(nr, ot["n_recycled"]), "recycle-list lengths differ"
     assert np.array_equal(lab.ravel(), ref["labels"]), "final labels differ"
-    assert np.array_equal(rc, ref["rxg_counts"]) and np.array_equal(dc, ref["defg_counts"])
-    return tr, ref
+    assert np.array_equal(rc, ref["rxg_counts"]) and np.array_equal(dc, ref["defg_counts"]), "grain counts differ"
+
+
+def compare(p, d, ptable=None):
+    ref = oracle.run(p, d, ptable)
+    assert ref["status"] == 0
+    out = run_gpu(p, d, ptable)
+    assert_same(*out, ref)
+    return out, ref
 
 
 @pytest.mark.parametrize("shape,ngr,nnuc,seed", [((64, 64, 64), 40, 24, 7), ((50, 72, 56), 90, 60, 3)])
 def test_fp64_matches_oracle(gpu, tmp_uds, shape, ngr, nnuc, seed):
     nx, ny, nz = shape
     d = sg.generate_domain(nx, ny, nz, ngr, nnuc, seed=seed)
-    p = sg.read_uds(tmp_uds(sg.UdsSpec(nx=nx, ny=ny, nz=nz)))
-    compare(p, d)
+    compare(sg.read_uds(tmp_uds(sg.UdsSpec(nx=nx, ny=ny, nz=nz))), d)
 
 
-def test_fp64_distinct_mobilities_matches_oracle(gpu, tmp_uds):
+def test_fp64_distinct_mobilities(gpu, tmp_uds):
     d = sg.generate_domain(64, 64, 64, 60, 40, seed=11)
-    spec = sg.UdsSpec(nx=64, ny=64, nz=64, LAGBm0="30.0", GSm0="600.0")
-    compare(sg.read_uds(tmp_uds(spec)), d)
+    compare(sg.read_uds(tmp_uds(sg.UdsSpec(nx=64, ny=64, nz=64, LAGBm0="30.0", GSm0="600.0"))), d)
 
 
-def test_fp64_rollett_holm_matches_oracle(gpu, tmp_uds):
+def test_fp64_rollett_holm(gpu, tmp_uds):
     d = sg.generate_domain(64, 64, 64, 60, 40, seed=12)
-    spec = sg.UdsSpec(nx=64, ny=64, nz=64, mobility_model=2, RH_HAGBHact="2.45")
+    compare(sg.read_uds(tmp_uds(sg.UdsSpec(nx=64, ny=64, nz=64, mobility_model=2))), d)
+
+
+def test_fp64_defragmentation(gpu, tmp_uds):
+    d = sg.generate_domain(64, 64, 64, 50, 30, seed=13)
+    spec = sg.UdsSpec(nx=64, ny=64, nz=64, defragmentation=1, defrag_x=["0.2", "0.5", "0.8"])
     compare(sg.read_uds(tmp_uds(spec)), d)
+
+
+def test_fp64_periodic_boundary(gpu, tmp_uds):
+    d = sg.generate_domain(56, 64, 60, 50, 30, seed=14)
+    compare(sg.read_uds(tmp_uds(sg.UdsSpec(nx=56, ny=64, nz=60, boundary=1))), d)
+
+
+def test_fp64_border_grow_policy(gpu, tmp_uds):
+    d = sg.generate_domain(64, 64, 64, 50, 200, seed=15)
+    compare(sg.read_uds(tmp_uds(sg.UdsSpec(nx=64, ny=64, nz=64, border_policy=1, initial_cache="0.05"))), d)
+
+
+def test_fp64_incubation_times(gpu, tmp_uds):
+    d = sg.generate_domain(64, 64, 64, 50, 60, seed=16, nucleation_rate=3000.0)
+    assert d.rxg_tincub.max() > 0
+    compare(sg.read_uds(tmp_uds(sg.UdsSpec(nx=64, ny=64, nz=64))), d)
+
+
+def test_fp64_recovery_refreshes_velocities(gpu, tmp_uds):
+    d = sg.generate_domain(64, 64, 64, 50, 30, seed=17)
+    compare(sg.read_uds(tmp_uds(sg.UdsSpec(nx=64, ny=64, nz=64, recovery=10, recovery_k="20.0"))), d)
+    compare(sg.read_uds(tmp_uds(sg.UdsSpec(nx=64, ny=64, nz=64, recovery=3))), d)
+
+
+def test_fp64_heating_schedule(gpu, tmp_uds):
+    d = sg.generate_domain(64, 64, 64, 50, 30, seed=18)
+    spec = sg.UdsSpec(nx=64, ny=64, nz=64, schedule=[("0.0", "700.0"), ("0.05", "760.0"), ("360000.0", "760.0")])
+    compare(sg.read_uds(tmp_uds(spec)), d)
+
+
+def test_fp64_zener_drag(gpu, tmp_uds):
+    d = sg.generate_domain(64, 64, 64, 50, 30, seed=19)
+    compare(sg.read_uds(tmp_uds(sg.UdsSpec(nx=64, ny=64, nz=64, zener=1, zener_table=[("0.0", "2.0e5"), ("360000.0", "2.0e5")]))), d)
+
+
+def test_fp64_user_ptable(gpu, tmp_uds):
+    d = sg.generate_domain(60, 60, 60, 40, 25, seed=20)
+    p = sg.read_uds(tmp_uds(sg.UdsSpec(nx=60, ny=60, nz=60, LAGBm0="30.0", GSm0="600.0")))
+    pt = np.array([[sg.mobility_weight(p, d.rxg_quat[r], d.defg_quat[g]) for g in range(d.ndefg)] for r in range(d.nrxg)])
+    compare(p, d, pt)
+
+
+def test_restart_and_reload_reproduce(gpu, tmp_uds):
+    d = sg.generate_domain(64, 64, 64, 40, 24, seed=21)
+    p = sg.read_uds(tmp_uds(sg.UdsSpec(nx=64, ny=64, nz=64)))
+    ref = oracle.run(p, d)
+    with sg.GrowthMachine(p, device=0) as gm:
+        gm.load_domain(d)
+        for _ in range(2):
+            gm.place_nuclei()
+            tr = gm.run_until()
+            lab = gm.labels()
+            rc, dc = gm.grain_counts()
+            assert_same(tr, lab, rc, dc, ref)
+            gm.restart()
+        d2 = sg.generate_domain(64, 64, 64, 40, 24, seed=22)
+        ref2 = oracle.run(p, d2)
+        gm.load_domain(d2)
+        gm.place_nuclei()
+        tr = gm.run_until()
+        assert_same(tr, gm.labels(), *gm.grain_counts(), ref2)
+
+
+def test_fp32_kahan_error_is_small(gpu, tmp_uds):
+    """FP32+Kahan fill vs the FP64 oracle: label mismatch, max |dX(t)|, mean grain size error."""
+    d = sg.generate_domain(96, 96, 96, 120, 80, seed=23)
+    p64 = sg.read_uds(tmp_uds(sg.UdsSpec(nx=96, ny=96, nz=96)))
+    p32 = sg.read_uds(tmp_uds(sg.UdsSpec(nx=96, ny=96, nz=96, precision=1)))
+    ref = oracle.run(p64, d)
+    tr, lab, rc, dc = run_gpu(p32, d)
+    mismatch = np.mean(lab.ravel() != ref["labels"])
+    x32 = np.array([s.X for s in tr])
+    x64 = ref["trace"]["X"]
+    n = min(len(x32), len(x64))
+    dx = np.max(np.abs(x32[:n] - x64[:n]))
+    gs_err = abs(rc.mean() - ref["rxg_counts"].mean()) / ref["rxg_counts"].mean()
+    assert mismatch < 1e-3, mismatch
+    assert dx < 5e-3, dx
+    assert gs_err < 1e-3, gs_err
