@@ -254,6 +254,7 @@ def main():
         gm.place_nuclei()
         tr = gm.run_until(X_TARGET)
         tm = gm.timing()
+        one_run.misses = sum(s.p_misses for s in tr)
         return sum(s.Sv for s in tr), len(tr), tm
 
     for _ in range(args.warmup):
@@ -326,7 +327,8 @@ def main():
                        "cells": n ** 3, "grains": ngr, "nuclei": nnuc, "growth_steps_per_run": tot_steps // args.steps,
                        "updates_per_run": tot_sv // args.steps, "time_to_X099_ms": run_ms / args.steps,
                        "l2": "inputs larger than L2 (grid alone 512 MiB)", "parallelism": f"{world} independent domains",
-                       "phase_ms_per_run": {k: v / args.steps for k, v in phase.items()}},
+                       "phase_ms_per_run": {k: v / args.steps for k, v in phase.items()},
+                       "host_weight_misses_per_run": getattr(one_run, "misses", None)},
             "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                          "frac": achieved / peak if peak else None, "traffic": traffic,
                          "kernel": "k_grow", "bytes_per_update": bpu, "peak_source": f"{peak_kind} (MEASURED_PEAKS.json hbm_gbs)"},

@@ -31,6 +31,8 @@ struct DevState {
     uint32_t next_never[2];     // slots ever used per list (Inside, Border)
     uint32_t err;               // sticky error flags
     uint32_t err_info;
+    uint32_t tiles_used[3];     // look-back tiles the last grow (x2) and commit launches used
+    uint32_t pad0;
     // ---- per step ----
     uint32_t nfull[2];          // FullRX list lengths
     uint32_t ninactive[2];      // INACTIVE slots seen by the scan (uncapped)
@@ -44,7 +46,7 @@ struct DevState {
     unsigned long long pmax_bits;  // max over new non-negative P (ordered bits)
     double dv[2];               // sum of fill increments
 };
-constexpr size_t kStepFieldsOffset = 16;  // offsetof(DevState, nfull)
+constexpr size_t kStepFieldsOffset = 32;  // offsetof(DevState, nfull)
 
 // ---- memory order helpers (device scope) ----
 __device__ __forceinline__ unsigned long long ld_acquire_u64(const unsigned long long* p) {
@@ -71,34 +73,51 @@ __device__ __forceinline__ unsigned long long pack2(uint32_t a, uint32_t b) {
     return ((unsigned long long)(a & kMask31) << 31) | (unsigned long long)(b & kMask31);
 }
 
-// Called by ONE thread of the block owning `tile`.  Returns the exclusive prefix of
-// both counters over all earlier tiles and publishes this tile's inclusive prefix.
-// Waits are bounded: after kSpinLimit polls the error flag is set and the partial
-// sum is used (results are then invalid and the host reports SCORE_ERR_TIMEOUT).
+// Called by ALL 32 lanes of one warp of the block owning `tile` (warp-parallel
+// look-back: each round inspects 32 predecessors at once).  Returns, in every lane,
+// the exclusive prefix of both counters over all earlier tiles and publishes this
+// tile's inclusive prefix.  Waits are bounded: after kSpinLimit polls the error flag
+// is set and the partial sum is used (results are then invalid and the host reports
+// SCORE_ERR_TIMEOUT).
 __device__ __forceinline__ void lookback2(unsigned long long* status, uint32_t tile, uint32_t aggA, uint32_t aggB,
                                           uint32_t& exA, uint32_t& exB, uint32_t* err) {
+    const int lane = threadIdx.x & 31;
     if (tile == 0) {
-        st_release_u64(&status[0], kFlagIncl | pack2(aggA, aggB));
+        if (lane == 0) st_release_u64(&status[0], kFlagIncl | pack2(aggA, aggB));
         exA = 0; exB = 0;
         return;
     }
-    st_release_u64(&status[tile], kFlagAgg | pack2(aggA, aggB));
+    if (lane == 0) st_release_u64(&status[tile], kFlagAgg | pack2(aggA, aggB));
     uint32_t accA = 0, accB = 0;
     int64_t j = (int64_t)tile - 1;
-    uint32_t polls = 0;
+    bool timed_out = false;
     while (j >= 0) {
-        unsigned long long s = ld_acquire_u64(&status[j]);
-        if ((s & (kFlagIncl | kFlagAgg)) == 0) {
-            if (++polls > kSpinLimit) { atomicOr(err, kErrTimeout); break; }
-            if (polls > 64) __nanosleep(64);
-            continue;
+        const int64_t idx = j - lane;  // lane 0 looks at the nearest predecessor
+        unsigned long long s = kFlagIncl;  // before tile 0: an inclusive zero
+        if (idx >= 0) {
+            uint32_t polls = 0;
+            for (;;) {
+                s = ld_acquire_u64(&status[idx]);
+                if (s & (kFlagIncl | kFlagAgg)) break;
+                if (++polls > kSpinLimit) { timed_out = true; s = kFlagIncl; break; }
+                if (polls > 32) __nanosleep(32);
+            }
         }
-        accA += (uint32_t)((s >> 31) & kMask31);
-        accB += (uint32_t)(s & kMask31);
-        if (s & kFlagIncl) break;
-        --j;
+        const uint32_t incl = __ballot_sync(0xFFFFFFFFu, (s & kFlagIncl) != 0);
+        const int stop = incl ? __ffs(incl) - 1 : 31;  // nearest inclusive predecessor in this window
+        uint32_t a = lane <= stop ? (uint32_t)((s >> 31) & kMask31) : 0u;
+        uint32_t b = lane <= stop ? (uint32_t)(s & kMask31) : 0u;
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) {
+            a += __shfl_xor_sync(0xFFFFFFFFu, a, o);
+            b += __shfl_xor_sync(0xFFFFFFFFu, b, o);
+        }
+        accA += a; accB += b;
+        if (incl) break;
+        j -= 32;
     }
-    st_release_u64(&status[tile], kFlagIncl | pack2(accA + aggA, accB + aggB));
+    if (__any_sync(0xFFFFFFFFu, timed_out) && lane == 0) atomicOr(err, kErrTimeout);
+    if (lane == 0) st_release_u64(&status[tile], kFlagIncl | pack2(accA + aggA, accB + aggB));
     exA = accA; exB = accB;
 }
 

@@ -32,7 +32,7 @@ using namespace score;
 
 namespace {
 
-constexpr uint32_t kTile = kBlock * 8;  // slots (grow) / full cells (commit) per look-back tile
+static_assert(offsetof(DevState, nfull) == kStepFieldsOffset, "per-step fields must start at kStepFieldsOffset");
 
 // ------------------------------------------------------------------ small kernels
 __global__ void k_count_defg(const uint32_t* grid, uint64_t n, uint32_t ndefg, uint32_t* cnt, uint32_t* err) {
@@ -128,11 +128,10 @@ __global__ void __launch_bounds__(kBlock) k_defrag_compact(DomainArgs a, int L, 
         }
         __syncthreads();
         if (warp == 0) {
-            uint32_t tA, tB;
+            uint32_t tA, tB, eA, eB;
             scan64_pair(s_cntA, s_cntB, tA, tB);
+            lookback2(status, tile, tA, 0, eA, eB, &a.st->err);
             if (lane == 0) {
-                uint32_t eA, eB;
-                lookback2(status, tile, tA, 0, eA, eB, &a.st->err);
                 s_ex = eA;
                 if (tile == ntiles - 1) *out_count = eA + tA;
             }
@@ -211,6 +210,8 @@ struct score_ctx {
     DevState* h_state = nullptr;       // pinned host copy of the snapshot
     double* d_pforce = nullptr;
     uint32_t* d_grid_init = nullptr;       // the loaded deformed grid (restart source)
+    double* d_rxq = nullptr;               // orientation quaternions on the device
+    double* d_dfq = nullptr;
     uint32_t* d_defg_cnt_init = nullptr;   // its per-grain cell counts
     uint32_t* d_u32tmp = nullptr;
     void* d_stage = nullptr;
@@ -250,13 +251,13 @@ void score_ctx::release_domain() {
     void* ptrs[] = {a.f[0].inc, a.f[1].inc, scratch.inc, a.f[0].fill, a.f[0].comp, a.f[0].vel, a.f[0].defg, a.f[0].rxg, a.f[0].xyz, a.f[0].dir, a.f[0].full, a.f[0].recyc,
                     a.f[1].fill, a.f[1].comp, a.f[1].vel, a.f[1].defg, a.f[1].rxg, a.f[1].xyz, a.f[1].dir, a.f[1].full, a.f[1].recyc,
                     a.grid, a.claim, a.amask, a.ptab, a.defg_cnt, a.rxg_cnt, a.depleted, a.miss, a.pending, a.status, a.tickets,
-                    d_state, d_snap, d_pforce, d_u32tmp, d_stage, d_grid_init, d_defg_cnt_init,
+                    d_state, d_snap, d_pforce, d_u32tmp, d_stage, d_grid_init, d_defg_cnt_init, d_rxq, d_dfq,
                     scratch.fill, scratch.comp, scratch.vel, scratch.defg, scratch.rxg, scratch.xyz, scratch.dir};
     for (void* p : ptrs) if (p) cudaFree(p);
     a = DomainArgs{};
     scratch = DFront{};
     d_state = nullptr; d_snap = nullptr; d_pforce = nullptr; d_u32tmp = nullptr; d_stage = nullptr;
-    d_grid_init = nullptr; d_defg_cnt_init = nullptr;
+    d_grid_init = nullptr; d_defg_cnt_init = nullptr; d_rxq = nullptr; d_dfq = nullptr;
     stage_cap = 0; scratch_cap = 0;
     loaded = false;
 }
@@ -658,9 +659,10 @@ int score_load_domain(score_ctx* c, const uint32_t* grid, const double* defg_qua
             if (e == cudaSuccess) e = dalloc(&f.recyc, recs[L]);
         }
         // look-back words: grow tiles of both lists, commit tiles over at most N full cells
-        a.status_off1 = capI / kTile + 2;
-        a.status_off2 = a.status_off1 + capB / kTile + 2;
-        a.status_words = a.status_off2 + (uint32_t)(N / kBlock) + 2;  // commit tiles hold kBlock full cells
+        // one word per warp tile: grow tiles of 256 slots per list, commit tiles of 32 full cells
+        a.status_off1 = capI / kGrowTile + 2;
+        a.status_off2 = a.status_off1 + capB / kGrowTile + 2;
+        a.status_words = a.status_off2 + (uint32_t)(N / 32) + 2;
         a.misscap = a.pendcap = (uint32_t)std::min<uint64_t>(N, 1ull << 25);
         if (e == cudaSuccess) e = dalloc(&a.grid, N);
         if (e == cudaSuccess) e = dalloc(&c->d_grid_init, N);
@@ -679,15 +681,22 @@ int score_load_domain(score_ctx* c, const uint32_t* grid, const double* defg_qua
         if (e == cudaSuccess) e = dalloc(&c->d_snap, 1);
         if (e == cudaSuccess) e = dalloc(&c->d_pforce, ndefg);
         if (e == cudaSuccess) e = dalloc(&c->d_u32tmp, 64);
+        if (e == cudaSuccess) e = dalloc(&c->d_rxq, 4 * (size_t)nrxg);
+        if (e == cudaSuccess) e = dalloc(&c->d_dfq, 4 * (size_t)ndefg);
         if (e != cudaSuccess) { c->release_domain(); return c->fail(SCORE_ERR_NOMEM, std::string("device allocation: ") + cudaGetErrorString(e)); }
         a.pforce = c->d_pforce;
         a.st = c->d_state;
+        a.rxq = c->d_rxq; a.dfq = c->d_dfq;
+        weight_constants(p, &a.pc_fac, &a.pc_lagb, &a.pc_maxdev, a.pc_m40, &a.pc_theta_sat);
+        a.pc_margin = 1e-9;
         c->high_water[0] = a.f[0].cap; c->high_water[1] = a.f[1].cap;  // the reset clears every slot once
     } else {
         c->high_water[0] = std::max(c->high_water[0], c->next_never[0]);
         c->high_water[1] = std::max(c->high_water[1], c->next_never[1]);
     }
     e = cudaMemcpyAsync(c->d_grid_init, grid, N * 4, cudaMemcpyHostToDevice, c->stream);
+    if (e == cudaSuccess && nrxg) e = cudaMemcpyAsync(c->d_rxq, rxg_quat, 4 * (size_t)nrxg * 8, cudaMemcpyHostToDevice, c->stream);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(c->d_dfq, defg_quat, 4 * (size_t)ndefg * 8, cudaMemcpyHostToDevice, c->stream);
     if (e == cudaSuccess && ptable) e = cudaMemcpyAsync(a.ptab, ptable, ptab_words * 8, cudaMemcpyHostToDevice, c->stream);
     if (e == cudaSuccess) e = cudaMemsetAsync(c->d_defg_cnt_init, 0, (size_t)ndefg * 4, c->stream);
     if (e == cudaSuccess) e = cudaMemsetAsync(c->d_state, 0, sizeof(DevState), c->stream);
@@ -744,8 +753,8 @@ int score_step(score_ctx* c, score_step_stats* out) {
     cudaStream_t st = c->stream;
     cudaEventRecord(c->ev[0], st);
     for (int L = 0; L < 2; ++L) {
-        const uint32_t tiles = (c->next_never[L] + kTile - 1) / kTile;
-        const uint32_t grid = std::max<uint32_t>(1, std::min<uint32_t>(tiles, (uint32_t)c->sms * 5));
+        const uint32_t tiles = (c->next_never[L] + kGrowTile - 1) / kGrowTile;  // warp tiles
+        const uint32_t grid = std::max<uint32_t>(1, std::min<uint32_t>((tiles + kWarps - 1) / kWarps, (uint32_t)c->sms * 4));
         if (c->fp32) {
             if (c->refresh) k_grow<true, true><<<grid, kBlock, 0, st>>>(a, L);
             else k_grow<true, false><<<grid, kBlock, 0, st>>>(a, L);
@@ -758,8 +767,8 @@ int score_step(score_ctx* c, score_step_stats* out) {
     cudaEventRecord(c->ev[1], st);
     k_claim<<<(uint32_t)c->sms * 4, kBlock, 0, st>>>(a);
     cudaEventRecord(c->ev[2], st);
-    if (c->fp32) k_commit<true><<<(uint32_t)c->sms * 4, kBlock, 0, st>>>(a);
-    else k_commit<false><<<(uint32_t)c->sms * 4, kBlock, 0, st>>>(a);
+    if (c->fp32) k_commit<true><<<(uint32_t)c->sms * 3, kBlock, 0, st>>>(a);
+    else k_commit<false><<<(uint32_t)c->sms * 3, kBlock, 0, st>>>(a);
     k_step_end<<<(uint32_t)c->sms, kBlock, 0, st>>>(a, c->d_snap);
     cudaEventRecord(c->ev[3], st);
     c->launches += 5;

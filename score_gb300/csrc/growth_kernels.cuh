@@ -92,6 +92,15 @@ struct DomainArgs {
     int32_t dt_changed;         // dt differs from the dt the cached increments were made with
     double mLAGB, mHAGB, mGS, mRH, dt, cinv;
     float dtc32;
+    // device classification of mobility weights whose value is an exact constant
+    const double* rxq;          // nrxg x 4 orientation quaternions
+    const double* dfq;          // ndefg x 4
+    double pc_fac;              // 1/sqrt(2) as the host computes it
+    double pc_lagb;             // 15 deg in rad (LAGB/HAGB threshold)
+    double pc_maxdev;           // 10 deg in rad (proximity to 40 deg <111>)
+    double pc_m40[4];           // the 40 deg <111> quaternion as the host computes it
+    double pc_theta_sat;        // Rollett-Holm: P is exactly 1.0 for theta above this (inf = never)
+    double pc_margin;           // safety margin around every threshold [rad]
 };
 
 __device__ __forceinline__ void decode(const DomainArgs& a, uint32_t cell, int& x, int& y, int& z) {
@@ -157,31 +166,35 @@ __device__ __forceinline__ void scan64_pair(uint32_t* cntA, uint32_t* cntB, uint
 }
 
 // ------------------------------------------------------------------ K1 grow
+// One WARP per look-back tile of 32 x kGrowItems slots (slot = base + 32 k + lane):
+// warps never wait for each other except through the look-back words.
 // REFRESH: recompute vel of every active slot from the P table and the current
 // physics (after T, rho or the drag changed) before growing it.
+constexpr int kGrowItems = 8;
+constexpr uint32_t kGrowTile = 32 * kGrowItems;
+
 template <bool FP32, bool REFRESH>
-__global__ void __launch_bounds__(kBlock, 5) k_grow(DomainArgs a, int L) {
-    constexpr int ITEMS = 8;  // ITEMS * kWarps == 64 for scan64_pair
-    constexpr uint32_t TILE = kBlock * ITEMS;
+__global__ void __launch_bounds__(kBlock, 4) k_grow(DomainArgs a, int L) {
+    constexpr int ITEMS = kGrowItems;
     const DFront fr = a.f[L];
     unsigned long long* status = a.status + (L == 0 ? 0u : a.status_off1);
     uint32_t* ticket = a.tickets + L;
     const uint32_t n = a.st->next_never[L];
-    const uint32_t ntiles = (n + TILE - 1) / TILE;
-    __shared__ uint32_t s_tile, s_exF, s_exI;
-    __shared__ uint32_t s_cntF[ITEMS * kWarps], s_cntI[ITEMS * kWarps];
-    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const uint32_t ntiles = (n + kGrowTile - 1) / kGrowTile;
+    if (blockIdx.x == 0 && threadIdx.x == 0) a.st->tiles_used[L] = ntiles;
+    const int lane = threadIdx.x & 31;
+    const uint32_t lt = lanemask_lt();
     unsigned long long sv = 0;
     for (;;) {
-        if (threadIdx.x == 0) s_tile = atomicAdd(ticket, 1u);
-        __syncthreads();
-        const uint32_t tile = s_tile;
+        uint32_t tile = 0;
+        if (lane == 0) tile = atomicAdd(ticket, 1u);
+        tile = __shfl_sync(0xFFFFFFFFu, tile, 0);
         if (tile >= ntiles) break;
-        const uint32_t base = tile * TILE;
+        const uint32_t base = tile * kGrowTile;
         uint8_t d[ITEMS];
 #pragma unroll
         for (int k = 0; k < ITEMS; ++k) {
-            const uint32_t slot = base + (uint32_t)(k * kBlock) + threadIdx.x;
+            const uint32_t slot = base + (uint32_t)(k * 32) + lane;
             d[k] = slot < n ? fr.dir[slot] : kInactive;
         }
         bool full[ITEMS];
@@ -189,7 +202,7 @@ __global__ void __launch_bounds__(kBlock, 5) k_grow(DomainArgs a, int L) {
             double w[ITEMS], fill[ITEMS];  // w: cached inc, or vel when the increment is stale
 #pragma unroll
             for (int k = 0; k < ITEMS; ++k) {
-                const uint32_t slot = base + (uint32_t)(k * kBlock) + threadIdx.x;
+                const uint32_t slot = base + (uint32_t)(k * 32) + lane;
                 w[k] = -1.0; fill[k] = 0.0;
                 if (d[k] != kInactive) {
                     if (REFRESH) {
@@ -210,7 +223,7 @@ __global__ void __launch_bounds__(kBlock, 5) k_grow(DomainArgs a, int L) {
                 full[k] = false;
                 if (d[k] != kInactive) {
                     ++sv;
-                    const uint32_t slot = base + (uint32_t)(k * kBlock) + threadIdx.x;
+                    const uint32_t slot = base + (uint32_t)(k * 32) + lane;
                     double inc = w[k];
                     if (REFRESH || a.dt_changed || (d[k] & kStale)) {
                         if (__double_as_longlong(w[k]) >= 0) inc = __dmul_rn(__dmul_rn(w[k], a.dt), a.cinv);
@@ -228,7 +241,7 @@ __global__ void __launch_bounds__(kBlock, 5) k_grow(DomainArgs a, int L) {
             float vel[ITEMS], fill[ITEMS], comp[ITEMS];
 #pragma unroll
             for (int k = 0; k < ITEMS; ++k) {
-                const uint32_t slot = base + (uint32_t)(k * kBlock) + threadIdx.x;
+                const uint32_t slot = base + (uint32_t)(k * 32) + lane;
                 vel[k] = -1.0f; fill[k] = 0.0f; comp[k] = 0.0f;
                 if (d[k] != kInactive) {
                     if (REFRESH) {
@@ -254,7 +267,7 @@ __global__ void __launch_bounds__(kBlock, 5) k_grow(DomainArgs a, int L) {
                         const float y = inc - comp[k];
                         const float t = fill[k] + y;
                         const float c = (t - fill[k]) - y;
-                        const uint32_t slot = base + (uint32_t)(k * kBlock) + threadIdx.x;
+                        const uint32_t slot = base + (uint32_t)(k * 32) + lane;
                         ((float*)fr.fill)[slot] = t;
                         fr.comp[slot] = c;
                         full[k] = (t - c) >= 1.0f;
@@ -262,43 +275,32 @@ __global__ void __launch_bounds__(kBlock, 5) k_grow(DomainArgs a, int L) {
                 }
             }
         }
-        uint32_t fm[ITEMS], im[ITEMS];
+        uint32_t fm[ITEMS], im[ITEMS], totF = 0, totI = 0;
 #pragma unroll
         for (int k = 0; k < ITEMS; ++k) {
             fm[k] = __ballot_sync(0xFFFFFFFFu, full[k]);
-            im[k] = __ballot_sync(0xFFFFFFFFu, d[k] == kInactive && base + (uint32_t)(k * kBlock) + threadIdx.x < n);
-            if (lane == 0) {
-                s_cntF[k * kWarps + warp] = __popc(fm[k]);
-                s_cntI[k * kWarps + warp] = __popc(im[k]);
-            }
+            im[k] = __ballot_sync(0xFFFFFFFFu, d[k] == kInactive && base + (uint32_t)(k * 32) + lane < n);
+            totF += __popc(fm[k]);
+            totI += __popc(im[k]);
         }
-        __syncthreads();
-        if (warp == 0) {
-            uint32_t totF, totI;
-            scan64_pair(s_cntF, s_cntI, totF, totI);
-            if (lane == 0) {
-                uint32_t exF, exI;
-                lookback2(status, tile, totF, totI, exF, exI, &a.st->err);
-                s_exF = exF; s_exI = exI;
-                if (tile == ntiles - 1) {
-                    a.st->nfull[L] = exF + totF;
-                    a.st->ninactive[L] = exI + totI;
-                    a.st->nrec[L] = min(exI + totI, fr.reccap);
-                }
-            }
+        uint32_t exF, exI;
+        lookback2(status, tile, totF, totI, exF, exI, &a.st->err);
+        if (tile == ntiles - 1 && lane == 0) {
+            a.st->nfull[L] = exF + totF;
+            a.st->ninactive[L] = exI + totI;
+            a.st->nrec[L] = min(exI + totI, fr.reccap);
         }
-        __syncthreads();
-        const uint32_t lt = lanemask_lt();
 #pragma unroll
         for (int k = 0; k < ITEMS; ++k) {
-            const uint32_t slot = base + (uint32_t)(k * kBlock) + threadIdx.x;
-            if ((fm[k] >> lane) & 1u) fr.full[s_exF + s_cntF[k * kWarps + warp] + __popc(fm[k] & lt)] = slot;
+            const uint32_t slot = base + (uint32_t)(k * 32) + lane;
+            if ((fm[k] >> lane) & 1u) fr.full[exF + __popc(fm[k] & lt)] = slot;
             if ((im[k] >> lane) & 1u) {
-                const uint32_t r = s_exI + s_cntI[k * kWarps + warp] + __popc(im[k] & lt);
+                const uint32_t r = exI + __popc(im[k] & lt);
                 if (r < fr.reccap) fr.recyc[r] = slot;
             }
+            exF += __popc(fm[k]);
+            exI += __popc(im[k]);
         }
-        __syncthreads();
     }
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) sv += __shfl_down_sync(0xFFFFFFFFu, sv, o);
@@ -337,11 +339,100 @@ __global__ void __launch_bounds__(kBlock) k_claim(DomainArgs a) {
     }
 }
 
-// P of a new cell from the table; unknown entries are requested from the host
+// ---- device classification of mobility weights ----
+// The weight P(rxg,defg) is -1 (LAGB), 0 (HAGB away from 40deg<111>) or, for the
+// Rollett-Holm sigmoid at large disorientation, exactly 1.0.  The disorientation's
+// scalar part omega is computed with the host's exact operation sequence (no FMA),
+// so only acos differs between device and host libm (a few ulp); a case whose angle
+// lies within pc_margin of a threshold, and every case whose weight is a genuine
+// libm expression, is left to the host.
+__device__ __forceinline__ void d_quat_mul(const double a[4], const double b[4], double r[4]) {
+    r[0] = __dsub_rn(__dsub_rn(__dsub_rn(__dmul_rn(a[0], b[0]), __dmul_rn(a[1], b[1])), __dmul_rn(a[2], b[2])), __dmul_rn(a[3], b[3]));
+    r[1] = __dadd_rn(__dadd_rn(__dmul_rn(b[0], a[1]), __dmul_rn(a[0], b[1])), __dsub_rn(__dmul_rn(a[2], b[3]), __dmul_rn(a[3], b[2])));
+    r[2] = __dadd_rn(__dadd_rn(__dmul_rn(b[0], a[2]), __dmul_rn(a[0], b[2])), __dadd_rn(-__dmul_rn(a[1], b[3]), __dmul_rn(a[3], b[1])));
+    r[3] = __dadd_rn(__dadd_rn(__dmul_rn(b[0], a[3]), __dmul_rn(a[0], b[3])), __dsub_rn(__dmul_rn(a[1], b[2]), __dmul_rn(a[2], b[1])));
+}
+// the 24 Grimmer candidates (6 quaternions), same order and roundings as the host
+__device__ __forceinline__ void d_grimmer(const DomainArgs& A, const double p[4], const double q[4], double c[6][4]) {
+    const double qi[4] = {q[0], -q[1], -q[2], -q[3]};
+    double r[4];
+    d_quat_mul(qi, p, r);
+    const double a = r[0], b = r[1], cc = r[2], d = r[3], f = A.pc_fac;
+    c[0][0] = __dmul_rn(__dadd_rn(a, b), f);  c[0][1] = __dmul_rn(__dsub_rn(a, b), f);  c[0][2] = __dmul_rn(__dadd_rn(cc, d), f); c[0][3] = __dmul_rn(__dsub_rn(cc, d), f);
+    c[1][0] = __dmul_rn(__dadd_rn(a, cc), f); c[1][1] = __dmul_rn(__dsub_rn(a, cc), f); c[1][2] = __dmul_rn(__dadd_rn(b, d), f);  c[1][3] = __dmul_rn(__dsub_rn(b, d), f);
+    c[2][0] = __dmul_rn(__dadd_rn(a, d), f);  c[2][1] = __dmul_rn(__dsub_rn(a, d), f);  c[2][2] = __dmul_rn(__dadd_rn(b, cc), f); c[2][3] = __dmul_rn(__dsub_rn(b, cc), f);
+    c[3][0] = __dmul_rn(__dadd_rn(__dadd_rn(__dadd_rn(a, b), cc), d), 0.5); c[3][1] = __dmul_rn(__dsub_rn(__dsub_rn(__dadd_rn(a, b), cc), d), 0.5);
+    c[3][2] = __dmul_rn(__dsub_rn(__dadd_rn(__dsub_rn(a, b), cc), d), 0.5); c[3][3] = __dmul_rn(__dadd_rn(__dsub_rn(__dsub_rn(a, b), cc), d), 0.5);
+    c[4][0] = __dmul_rn(__dsub_rn(__dadd_rn(__dadd_rn(a, b), cc), d), 0.5); c[4][1] = __dmul_rn(__dadd_rn(__dsub_rn(__dadd_rn(a, b), cc), d), 0.5);
+    c[4][2] = __dmul_rn(__dadd_rn(__dadd_rn(__dsub_rn(a, b), cc), d), 0.5); c[4][3] = __dmul_rn(__dsub_rn(__dsub_rn(__dsub_rn(a, b), cc), d), 0.5);
+    c[5][0] = a; c[5][1] = b; c[5][2] = cc; c[5][3] = d;
+}
+// disorientation angle; `exact_zero` when the host also returns exactly 0
+__device__ __forceinline__ double d_disori(const DomainArgs& A, const double p[4], const double q[4], int* mi_out) {
+    double c[6][4];
+    d_grimmer(A, p, q, c);
+    double om = 0.0;
+    int mi = 0;
+#pragma unroll
+    for (int i = 0; i < 6; ++i)
+#pragma unroll
+        for (int j = 0; j < 4; ++j)
+            if (fabs(c[i][j]) > om) { om = fabs(c[i][j]); mi = i; }
+    if (mi_out) *mi_out = mi;
+    if (om < (1.0 - 5.0e-16)) return 2.0 * acos(om);
+    return 0.0;
+}
+__device__ __noinline__ bool device_weight(const DomainArgs& A, uint32_t rxg, uint32_t defg, double& P) {
+    const double* p = A.rxq + 4 * (size_t)rxg;
+    const double* q = A.dfq + 4 * (size_t)defg;
+    const double pr[4] = {p[0], p[1], p[2], p[3]}, qd[4] = {q[0], q[1], q[2], q[3]};
+    const double theta = d_disori(A, pr, qd, nullptr);
+    const double m = A.pc_margin;
+    if (A.mobility_model == 2) {
+        if (theta > A.pc_theta_sat) { P = 1.0; return true; }
+        return false;
+    }
+    if (theta == 0.0 || theta < A.pc_lagb - m) { P = -1.0; return true; }
+    if (!(theta > A.pc_lagb + m)) return false;
+    // HAGB: distance of the disorientation to 40deg<111>
+    double c[6][4];
+    d_grimmer(A, pr, qd, c);
+    int mi = 0;
+    double mx = 0.0;
+#pragma unroll
+    for (int i = 0; i < 6; ++i)
+#pragma unroll
+        for (int j = 0; j < 4; ++j)
+            if (fabs(c[i][j]) > mx) { mx = fabs(c[i][j]); mi = i; }
+    double s[4] = {fabs(c[mi][0]), fabs(c[mi][1]), fabs(c[mi][2]), fabs(c[mi][3])};
+    // ascending sort of four values (the order of equal values is immaterial)
+#pragma unroll
+    for (int i = 0; i < 3; ++i)
+#pragma unroll
+        for (int k = 0; k < 3 - i; ++k)
+            if (s[k] > s[k + 1]) { const double t = s[k]; s[k] = s[k + 1]; s[k + 1] = t; }
+    const double qdis[4] = {s[3], s[2], s[1], s[0]};
+    const double dev = d_disori(A, qdis, A.pc_m40, nullptr);
+    if (dev > A.pc_maxdev + m) { P = 0.0; return true; }
+    return false;
+}
+
+// P of a new cell from the table; unknown entries are classified on the device when
+// exact, otherwise requested from the host
 __device__ __forceinline__ bool lookup_p(const DomainArgs& a, uint32_t rxg, uint32_t defg, double& P) {
     unsigned long long* e = &a.ptab[(unsigned long long)rxg * a.ndefg + defg];
     unsigned long long bits = *(volatile unsigned long long*)e;
     if (bits == kPtabEmpty) {
+        double v;
+        if (device_weight(a, rxg, defg, v)) {
+            const unsigned long long vb = (unsigned long long)__double_as_longlong(v);
+            const unsigned long long old = atomicCAS(e, kPtabEmpty, vb);
+            if (old == kPtabEmpty || old == vb) { P = v; return true; }
+            bits = old;
+            if (bits == kPtabPending) return false;
+            P = __longlong_as_double((long long)bits);
+            return true;
+        }
         unsigned long long old = atomicCAS(e, kPtabEmpty, kPtabPending);
         if (old == kPtabEmpty) {
             const uint32_t m = atomicAdd(&a.st->nmiss, 1u);
@@ -357,44 +448,21 @@ __device__ __forceinline__ bool lookup_p(const DomainArgs& a, uint32_t rxg, uint
 }
 
 // ------------------------------------------------------------------ K3 commit (+ finalize)
-// scan of the per-thread win counts (A: to Inside, B: to Border) over one tile of
-// kBlock full cells: per-warp inclusive scans, then the warp totals
-__device__ __forceinline__ void block_scan_pair(uint32_t cA, uint32_t cB, uint32_t* sA, uint32_t* sB, uint32_t& exA, uint32_t& exB,
-                                                uint32_t& totA, uint32_t& totB) {
-    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    uint32_t ia = cA, ib = cB;
-#pragma unroll
-    for (int o = 1; o < 32; o <<= 1) {
-        const uint32_t xa = __shfl_up_sync(0xFFFFFFFFu, ia, o), xb = __shfl_up_sync(0xFFFFFFFFu, ib, o);
-        if (lane >= o) { ia += xa; ib += xb; }
-    }
-    if (lane == 31) { sA[warp] = ia; sB[warp] = ib; }
-    __syncthreads();
-    uint32_t wa = 0, wb = 0, ta = 0, tb = 0;
-#pragma unroll
-    for (int w = 0; w < kWarps; ++w) {
-        const uint32_t va = sA[w], vb = sB[w];
-        if (w < warp) { wa += va; wb += vb; }
-        ta += va; tb += vb;
-    }
-    exA = wa + ia - cA; exB = wb + ib - cB;
-    totA = ta; totB = tb;
-}
-
+// One WARP per look-back tile of 32 full cells (full-cell order).
 template <bool FP32>
-__global__ void __launch_bounds__(kBlock) k_commit(DomainArgs a) {
+__global__ void __launch_bounds__(kBlock, 3) k_commit(DomainArgs a) {
     const uint32_t F0 = a.st->nfull[0], F = F0 + a.st->nfull[1];
     if (26ull * F >= 0xFFFFFFFFull) return;
     unsigned long long* status = a.status + a.status_off2;
-    const uint32_t ntiles = (F + kBlock - 1) / kBlock;
-    __shared__ uint32_t s_tile, s_exA, s_exB;
-    __shared__ uint32_t s_wA[kWarps], s_wB[kWarps];
+    const uint32_t ntiles = (F + 31) / 32;
+    if (blockIdx.x == 0 && threadIdx.x == 0) a.st->tiles_used[2] = ntiles;
+    const int lane = threadIdx.x & 31;
     for (;;) {
-        if (threadIdx.x == 0) s_tile = atomicAdd(a.tickets + 2, 1u);
-        __syncthreads();
-        const uint32_t tile = s_tile;
+        uint32_t tile = 0;
+        if (lane == 0) tile = atomicAdd(a.tickets + 2, 1u);
+        tile = __shfl_sync(0xFFFFFFFFu, tile, 0);
         if (tile >= ntiles) break;
-        const uint32_t f = tile * kBlock + threadIdx.x;
+        const uint32_t f = tile * 32 + lane;
         uint32_t win = 0, tob = 0, slot = 0, cell = 0;
         int L = 0, x = 0, y = 0, z = 0;
         if (f < F) {
@@ -430,20 +498,21 @@ __global__ void __launch_bounds__(kBlock) k_commit(DomainArgs a) {
             }
         }
         const uint32_t cB = __popc(tob), cA = __popc(win) - cB;
-        uint32_t exA, exB, totA, totB;
-        block_scan_pair(cA, cB, s_wA, s_wB, exA, exB, totA, totB);
-        if (threadIdx.x == 0) {
-            uint32_t pA, pB;
-            lookback2(status, tile, totA, totB, pA, pB, &a.st->err);
-            s_exA = pA; s_exB = pB;
-            if (tile == ntiles - 1) { a.st->nwin[0] = pA + totA; a.st->nwin[1] = pB + totB; }
+        uint32_t iA = cA, iB = cB;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            const uint32_t xa = __shfl_up_sync(0xFFFFFFFFu, iA, o), xb = __shfl_up_sync(0xFFFFFFFFu, iB, o);
+            if (lane >= o) { iA += xa; iB += xb; }
         }
-        __syncthreads();
+        const uint32_t totA = __shfl_sync(0xFFFFFFFFu, iA, 31), totB = __shfl_sync(0xFFFFFFFFu, iB, 31);
+        uint32_t pA, pB;
+        lookback2(status, tile, totA, totB, pA, pB, &a.st->err);
+        if (tile == ntiles - 1 && lane == 0) { a.st->nwin[0] = pA + totA; a.st->nwin[1] = pB + totB; }
         if (f < F) {
             const DFront& src = a.f[L];
             const uint32_t rsrc = src.rxg[slot], gsrc = src.defg[slot];
             if (win) {
-                uint32_t rA = s_exA + exA, rB = s_exB + exB;
+                uint32_t rA = pA + iA - cA, rB = pB + iB - cB;
                 double over = 0.0;
                 float over32 = 0.0f;
                 if (!FP32) over = __dsub_rn(((const double*)src.fill)[slot], 1.0);
@@ -503,14 +572,14 @@ __global__ void __launch_bounds__(kBlock) k_commit(DomainArgs a) {
             if (!FP32) ((double*)src.fill)[slot] = 0.0;
             else { ((float*)src.fill)[slot] = 0.0f; src.comp[slot] = 0.0f; }
         }
-        __syncthreads();
     }
 }
 
 // ------------------------------------------------------------------ K4 step end
 // Thread 0 of block 0 advances the high-water marks, snapshots the per-step fields
 // for the host and clears them and the tickets; all blocks clear the look-back words
-// (no kernel of this step reads them any more).
+// this step's scans used (no kernel of this step reads them any more), so every word
+// is zero again at the start of the next step.
 __global__ void __launch_bounds__(kBlock) k_step_end(DomainArgs a, DevState* snapshot) {
     if (blockIdx.x == 0 && threadIdx.x == 0) {
         DevState* st = a.st;
@@ -524,7 +593,12 @@ __global__ void __launch_bounds__(kBlock) k_step_end(DomainArgs a, DevState* sna
         for (size_t i = 0; i < sizeof(DevState) - kStepFieldsOffset; ++i) p[i] = 0;
         a.tickets[0] = a.tickets[1] = a.tickets[2] = 0;
     }
-    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < a.status_words; i += gridDim.x * blockDim.x) a.status[i] = 0ull;
+    const uint32_t off[3] = {0u, a.status_off1, a.status_off2};
+    const uint32_t lim[3] = {a.status_off1, a.status_off2, a.status_words};
+    for (int r = 0; r < 3; ++r) {
+        const uint32_t used = min(a.st->tiles_used[r] + 1u, lim[r] - off[r]);
+        for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < used; i += gridDim.x * blockDim.x) a.status[off[r] + i] = 0ull;
+    }
 }
 
 }  // namespace score

@@ -87,6 +87,22 @@ double mobility_weight(const score_params& prm, const double qr[4], const double
     return w;
 }
 
+void weight_constants(const score_params& prm, double* fac, double* lagb, double* maxdev, double m40[4], double* theta_sat) {
+    *fac = 1.0 / std::sqrt(2.0);
+    *lagb = (15.0) / (180.0) * (kPi);
+    *maxdev = (10.0) / (180.0) * (kPi);
+    const double sqrt3inv = 1 / std::sqrt(3.0);
+    const double oneNinth = 1.0 / 9.0;
+    m40[0] = std::cos(oneNinth * kPi);
+    m40[1] = m40[2] = m40[3] = sqrt3inv * std::sin(oneNinth * kPi);
+    // Rollett-Holm: once trans (theta/15deg)^expo exceeds 60, cut*exp(-60..) < 2^-60 for
+    // cut < 1e7, so 1 - cut*exp(..) rounds to exactly 1.0 whatever libm's last bit
+    *theta_sat = 1e300;
+    if (prm.mobility_model == SCORE_MOBILITY_ROLLETT_HOLM && prm.RH_trans > 0.0 && prm.RH_exponent > 0.0 &&
+        std::fabs(prm.RH_cut) < 1e7)
+        *theta_sat = *lagb * std::pow(60.0 / prm.RH_trans, 1.0 / prm.RH_exponent) * (1.0 + 1e-6);
+}
+
 // ---------------------------------------------------------------- physics
 
 void Physics::init(const score_params* p) {
