@@ -44,7 +44,7 @@ N_EDGE = 512
 N_GRAINS = 20000
 N_NUCLEI = 50000
 X_TARGET = 0.99
-# algorithmic bytes of one front-cell update in k_grow: FP64 reads the infector byte,
+# algorithmic bytes of one front-cell update in k_grow_fill: FP64 reads the infector byte,
 # the cached increment and the fill and writes the fill (1 + 8 + 8 + 8); FP32+Kahan
 # reads byte, velocity factor, fill and compensation and writes fill and compensation
 BYTES_PER_UPDATE = {0: 25.0, 1: 17.0}
@@ -262,7 +262,7 @@ def main():
     barrier(dist)
     launches0 = gm.timing().kernel_launches
     tot_sv, tot_steps, run_ms, grow_bytes, grow_launches = 0, 0, 0.0, 0.0, 0
-    phase = {"grow_ms": 0.0, "claim_ms": 0.0, "commit_ms": 0.0, "host_ms": 0.0}
+    phase = {"grow_ms": 0.0, "fill_ms": 0.0, "claim_ms": 0.0, "commit_ms": 0.0, "host_ms": 0.0}
     with ClockSampler(local) as clk:
         for _ in range(args.steps):
             sv, ns, tm = one_run()
@@ -273,7 +273,7 @@ def main():
             grow_launches += tm.grow_launches
             for k in phase:
                 phase[k] += getattr(tm, k)
-    grow_ms = phase["grow_ms"]
+    fill_ms = phase["fill_ms"]
     launches = gm.timing().kernel_launches - launches0
     barrier(dist)
     t_max = reduce_max(dist, run_ms / 1e3)
@@ -310,7 +310,7 @@ def main():
     if rank == 0:
         peak, peak_kind = measured_peak_gbs()
         bpu = BYTES_PER_UPDATE[args.precision]
-        achieved = grow_bytes / (grow_ms / 1e3) / 1e9 if grow_ms > 0 else 0.0
+        achieved = grow_bytes / (fill_ms / 1e3) / 1e9 if fill_ms > 0 else 0.0
         traffic = None
         tf = ROOT / "profiles" / "grow_traffic.json"
         if tf.exists():
@@ -331,7 +331,7 @@ def main():
                        "host_weight_misses_per_run": getattr(one_run, "misses", None)},
             "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                          "frac": achieved / peak if peak else None, "traffic": traffic,
-                         "kernel": "k_grow", "bytes_per_update": bpu, "peak_source": f"{peak_kind} (MEASURED_PEAKS.json hbm_gbs)"},
+                         "kernel": "k_grow_fill", "bytes_per_update": bpu, "peak_source": f"{peak_kind} (MEASURED_PEAKS.json hbm_gbs)"},
             "e2e": {"value": e_value, "unit": "updates/s", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
             "gpu_launches": int(launches),
             "clocks": clk.summary(),

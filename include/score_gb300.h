@@ -194,7 +194,8 @@ typedef struct score_timing {
     double grow_bytes;      /* algorithmic bytes of all grow launches */
     double step_bytes;      /* algorithmic bytes of all kernels */
     uint64_t kernel_launches;  /* kernels launched by this context since creation */
-    double run_ms;
+    double run_ms;          /* device span of the last restart .. score_run_until */
+    double fill_ms;         /* the fill-update kernels alone (part of grow_ms) */
 } score_timing;
 int  score_get_timing(score_ctx* ctx, score_timing* out);
 

@@ -7,9 +7,10 @@
 //   claim  u32[N]   attempt ordinal of the first infection of this step (0xFFFFFFFF free)
 //   front list L (SoA, slot-indexed): fill f64|f32, [comp f32], vel f64|f32, defg u32,
 //          rxg u32, xyz u32, dir u8
-//   full_L u32[cap_L], recyc_L u32[reccap_L], amask u32[N]  (rebuilt every step)
+//   full_L u32[cap_L], recyc_L u32[reccap_L]                 (rebuilt every step)
+//   fmask_L, imask_L u32[cap_L/32], tcnt_L u32[2 cap_L/2048]  grow bit masks, tile counts
+//   amask, tobm u32[N], ctcnt u32[2 N/256]                    per-full-cell attempt/win masks
 //   ptab   u64[nrxg*ndefg] mobility weights P(rxg,defg), filled on first use
-//   status u64 look-back words of the three scans, cleared by k_step_end
 #include <cuda_runtime.h>
 
 #include <algorithm>
@@ -103,22 +104,45 @@ __global__ void k_labels_front(DomainArgs a, int L, uint32_t n, uint32_t* lab) {
 }
 
 // stable compaction of ACTIVE slots of list L into scratch arrays (ompshar_defragmentation,
-// SCORE_Kernel.cpp:3877-3937); uses the list's grow look-back words and ticket
-template <bool FP32>
-__global__ void __launch_bounds__(kBlock) k_defrag_compact(DomainArgs a, int L, uint32_t n, DFront scratch, uint32_t* out_count) {
-    constexpr int ITEMS = 8;
-    constexpr uint32_t TILE = kBlock * ITEMS;
+// SCORE_Kernel.cpp:3877-3937), in three passes over tiles of kGrowTile slots like the
+// grow step: count, one-block scan (k_scan_defrag), move.  Uses the list's tile counts.
+__global__ void __launch_bounds__(kBlock) k_defrag_count(DomainArgs a, int L, uint32_t n) {
     const DFront fr = a.f[L];
-    unsigned long long* status = a.status + (L == 0 ? 0u : a.status_off1);
-    const uint32_t ntiles = (n + TILE - 1) / TILE;
-    __shared__ uint32_t s_tile, s_ex, s_cntA[ITEMS * kWarps], s_cntB[ITEMS * kWarps];
+    const uint32_t ntiles = (n + kGrowTile - 1) / kGrowTile;
+    __shared__ uint32_t s_c[kWarps];
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    for (;;) {
-        if (threadIdx.x == 0) s_tile = atomicAdd(a.tickets + L, 1u);
+    for (uint32_t tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
+        uint32_t c = 0;
+        for (int k = 0; k < kGrowItems; ++k) {
+            const uint32_t s = tile * kGrowTile + (uint32_t)(k * kBlock) + threadIdx.x;
+            c += __popc(__ballot_sync(0xFFFFFFFFu, s < n && fr.dir[s] != kInactive));
+        }
+        if (lane == 0) s_c[warp] = c;
         __syncthreads();
-        const uint32_t tile = s_tile;
-        if (tile >= ntiles) break;
-        const uint32_t base = tile * TILE;
+        if (threadIdx.x == 0) {
+            uint32_t t = 0;
+            for (int w = 0; w < kWarps; ++w) t += s_c[w];
+            fr.tcnt[2 * tile] = t;
+            fr.tcnt[2 * tile + 1] = 0;
+        }
+        __syncthreads();
+    }
+}
+__global__ void __launch_bounds__(1024) k_scan_defrag(DomainArgs a, int L, uint32_t n, uint32_t* out_count) {
+    uint32_t tA, tB;
+    scan_pairs_block(a.f[L].tcnt, (n + kGrowTile - 1) / kGrowTile, tA, tB);
+    if (threadIdx.x == 0) *out_count = tA;
+}
+template <bool FP32>
+__global__ void __launch_bounds__(kBlock) k_defrag_compact(DomainArgs a, int L, uint32_t n, DFront scratch) {
+    constexpr int ITEMS = kGrowItems;
+    const DFront fr = a.f[L];
+    const uint32_t ntiles = (n + kGrowTile - 1) / kGrowTile;
+    __shared__ uint32_t s_cntA[ITEMS * kWarps], s_cntB[ITEMS * kWarps];
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const uint32_t lt = lanemask_lt();
+    for (uint32_t tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
+        const uint32_t base = tile * kGrowTile;
         uint32_t am[ITEMS];
 #pragma unroll
         for (int k = 0; k < ITEMS; ++k) {
@@ -128,21 +152,16 @@ __global__ void __launch_bounds__(kBlock) k_defrag_compact(DomainArgs a, int L, 
         }
         __syncthreads();
         if (warp == 0) {
-            uint32_t tA, tB, eA, eB;
+            uint32_t tA, tB;
             scan64_pair(s_cntA, s_cntB, tA, tB);
-            lookback2(status, tile, tA, 0, eA, eB, &a.st->err);
-            if (lane == 0) {
-                s_ex = eA;
-                if (tile == ntiles - 1) *out_count = eA + tA;
-            }
         }
         __syncthreads();
-        const uint32_t lt = lanemask_lt();
+        const uint32_t ex = fr.tcnt[2 * tile];
 #pragma unroll
         for (int k = 0; k < ITEMS; ++k) {
             if (!((am[k] >> lane) & 1u)) continue;
             const uint32_t s = base + (uint32_t)(k * kBlock) + threadIdx.x;
-            const uint32_t r = s_ex + s_cntA[k * kWarps + warp] + __popc(am[k] & lt);
+            const uint32_t r = ex + s_cntA[k * kWarps + warp] + __popc(am[k] & lt);
             if (!FP32) {
                 ((double*)scratch.fill)[r] = ((const double*)fr.fill)[s];
                 ((double*)scratch.vel)[r] = ((const double*)fr.vel)[s];
@@ -224,7 +243,7 @@ struct score_ctx {
     uint32_t next_never[2] = {0, 0}, high_water[2] = {0, 0};
     score_step_stats last{};
 
-    cudaEvent_t ev[6] = {nullptr, nullptr, nullptr, nullptr, nullptr, nullptr};  // 0-3 step phases, 4-5 run span
+    cudaEvent_t ev[7] = {nullptr, nullptr, nullptr, nullptr, nullptr, nullptr, nullptr};  // 0-3 step phases, 4-5 run span, 6 end of fill
     score_timing tm{};
     uint64_t launches = 0;
 
@@ -250,7 +269,8 @@ void score_ctx::release_domain() {
     if (device >= 0) cudaSetDevice(device);
     void* ptrs[] = {a.f[0].inc, a.f[1].inc, scratch.inc, a.f[0].fill, a.f[0].comp, a.f[0].vel, a.f[0].defg, a.f[0].rxg, a.f[0].xyz, a.f[0].dir, a.f[0].full, a.f[0].recyc,
                     a.f[1].fill, a.f[1].comp, a.f[1].vel, a.f[1].defg, a.f[1].rxg, a.f[1].xyz, a.f[1].dir, a.f[1].full, a.f[1].recyc,
-                    a.grid, a.claim, a.amask, a.ptab, a.defg_cnt, a.rxg_cnt, a.depleted, a.miss, a.pending, a.status, a.tickets,
+                    a.grid, a.claim, a.amask, a.ptab, a.defg_cnt, a.rxg_cnt, a.depleted, a.miss, a.pending, a.tobm, a.ctcnt,
+                    a.f[0].fmask, a.f[0].imask, a.f[0].tcnt, a.f[1].fmask, a.f[1].imask, a.f[1].tcnt,
                     d_state, d_snap, d_pforce, d_u32tmp, d_stage, d_grid_init, d_defg_cnt_init, d_rxq, d_dfq,
                     scratch.fill, scratch.comp, scratch.vel, scratch.defg, scratch.rxg, scratch.xyz, scratch.dir};
     for (void* p : ptrs) if (p) cudaFree(p);
@@ -431,19 +451,15 @@ int defragment(score_ctx* c, int L) {
         c->scratch_cap = n;
     }
     uint32_t* d_cnt = c->d_u32tmp;
-    cudaMemsetAsync(d_cnt, 0, 8, c->stream);
-    const uint32_t grid = blocks_for((uint64_t)n, c->sms, 4);
-    if (c->fp32) k_defrag_compact<true><<<grid, kBlock, 0, c->stream>>>(c->a, L, n, c->scratch, d_cnt);
-    else k_defrag_compact<false><<<grid, kBlock, 0, c->stream>>>(c->a, L, n, c->scratch, d_cnt);
-    c->launches++;
+    const uint32_t ntiles = (n + kGrowTile - 1) / kGrowTile;
+    const uint32_t grid = std::min<uint32_t>(ntiles, (uint32_t)c->sms * 8);
+    k_defrag_count<<<grid, kBlock, 0, c->stream>>>(c->a, L, n);
+    k_scan_defrag<<<1, 1024, 0, c->stream>>>(c->a, L, n, d_cnt);
+    if (c->fp32) k_defrag_compact<true><<<grid, kBlock, 0, c->stream>>>(c->a, L, n, c->scratch);
+    else k_defrag_compact<false><<<grid, kBlock, 0, c->stream>>>(c->a, L, n, c->scratch);
+    c->launches += 3;
     uint32_t active = 0;
     cudaError_t e = cudaMemcpyAsync(&active, d_cnt, 4, cudaMemcpyDeviceToHost, c->stream);
-    // the grow scan of this step needs its look-back words and ticket cleared again
-    if (e == cudaSuccess) {
-        k_zero_u64<<<blocks_for(c->a.status_words, c->sms), kBlock, 0, c->stream>>>(c->a.status, c->a.status_words);
-        c->launches++;
-        e = cudaMemsetAsync(c->a.tickets, 0, 8 * sizeof(uint32_t), c->stream);
-    }
     if (e == cudaSuccess) e = cudaStreamSynchronize(c->stream);
     if (e != cudaSuccess) return c->cuda_fail(e, "defragment");
     if (active == n) {
@@ -495,8 +511,6 @@ int reset_state(score_ctx* c) {
     if (e == cudaSuccess) e = cudaMemcpyAsync(a.defg_cnt, c->d_defg_cnt_init, (size_t)c->ndefg * 4, cudaMemcpyDeviceToDevice, st);
     if (e == cudaSuccess) e = cudaMemsetAsync(a.rxg_cnt, 0, std::max<size_t>(c->nrxg, 1) * 4, st);
     if (e == cudaSuccess) e = cudaMemsetAsync(c->d_state, 0, sizeof(DevState), st);
-    if (e == cudaSuccess) e = cudaMemsetAsync(a.status, 0, (size_t)a.status_words * 8, st);
-    if (e == cudaSuccess) e = cudaMemsetAsync(a.tickets, 0, 8 * sizeof(uint32_t), st);
     if (e != cudaSuccess) return c->cuda_fail(e, "reset domain");
     c->rho = c->rho0;
     c->defg_cnt_host = c->defg_cnt_init_host;
@@ -657,17 +671,18 @@ int score_load_domain(score_ctx* c, const uint32_t* grid, const double* defg_qua
             if (e == cudaSuccess) e = dalloc(&f.dir, caps[L]);
             if (e == cudaSuccess) e = dalloc(&f.full, caps[L]);
             if (e == cudaSuccess) e = dalloc(&f.recyc, recs[L]);
+            const size_t tiles = (size_t)caps[L] / kGrowTile + 1;
+            if (e == cudaSuccess) e = dalloc(&f.fmask, tiles * (kGrowTile / 32));
+            if (e == cudaSuccess) e = dalloc(&f.imask, tiles * (kGrowTile / 32));
+            if (e == cudaSuccess) e = dalloc(&f.tcnt, 2 * tiles);
         }
-        // look-back words: grow tiles of both lists, commit tiles over at most N full cells
-        // one word per warp tile: grow tiles of 256 slots per list, commit tiles of 32 full cells
-        a.status_off1 = capI / kGrowTile + 2;
-        a.status_off2 = a.status_off1 + capB / kGrowTile + 2;
-        a.status_words = a.status_off2 + (uint32_t)(N / 32) + 2;
         a.misscap = a.pendcap = (uint32_t)std::min<uint64_t>(N, 1ull << 25);
         if (e == cudaSuccess) e = dalloc(&a.grid, N);
         if (e == cudaSuccess) e = dalloc(&c->d_grid_init, N);
         if (e == cudaSuccess) e = dalloc(&a.claim, N);
         if (e == cudaSuccess) e = dalloc(&a.amask, N);
+        if (e == cudaSuccess) e = dalloc(&a.tobm, N);
+        if (e == cudaSuccess) e = dalloc(&a.ctcnt, 2 * (N / kBlock + 1));
         if (e == cudaSuccess) e = dalloc(&a.ptab, ptab_words);
         if (e == cudaSuccess) e = dalloc(&a.defg_cnt, ndefg);
         if (e == cudaSuccess) e = dalloc(&c->d_defg_cnt_init, ndefg);
@@ -675,8 +690,6 @@ int score_load_domain(score_ctx* c, const uint32_t* grid, const double* defg_qua
         if (e == cudaSuccess) e = dalloc(&a.depleted, ndefg);
         if (e == cudaSuccess) e = dalloc(&a.miss, a.misscap);
         if (e == cudaSuccess) e = dalloc(&a.pending, a.pendcap);
-        if (e == cudaSuccess) e = dalloc(&a.status, a.status_words);
-        if (e == cudaSuccess) e = dalloc(&a.tickets, 8);
         if (e == cudaSuccess) e = dalloc(&c->d_state, 1);
         if (e == cudaSuccess) e = dalloc(&c->d_snap, 1);
         if (e == cudaSuccess) e = dalloc(&c->d_pforce, ndefg);
@@ -752,39 +765,48 @@ int score_step(score_ctx* c, score_step_stats* out) {
     c->dt_cached = c->ph.dt;
     cudaStream_t st = c->stream;
     cudaEventRecord(c->ev[0], st);
+    uint32_t max_tiles = 1;
     for (int L = 0; L < 2; ++L) {
-        const uint32_t tiles = (c->next_never[L] + kGrowTile - 1) / kGrowTile;  // warp tiles
-        const uint32_t grid = std::max<uint32_t>(1, std::min<uint32_t>((tiles + kWarps - 1) / kWarps, (uint32_t)c->sms * 4));
+        const uint32_t tiles = (c->next_never[L] + kGrowTile - 1) / kGrowTile;
+        max_tiles = std::max(max_tiles, tiles);
+        const uint32_t grid = std::max<uint32_t>(1, std::min<uint32_t>(tiles, (uint32_t)c->sms * 16));
         if (c->fp32) {
-            if (c->refresh) k_grow<true, true><<<grid, kBlock, 0, st>>>(a, L);
-            else k_grow<true, false><<<grid, kBlock, 0, st>>>(a, L);
+            if (c->refresh) k_grow_fill<true, true><<<grid, kBlock, 0, st>>>(a, L);
+            else k_grow_fill<true, false><<<grid, kBlock, 0, st>>>(a, L);
         } else {
-            if (c->refresh) k_grow<false, true><<<grid, kBlock, 0, st>>>(a, L);
-            else k_grow<false, false><<<grid, kBlock, 0, st>>>(a, L);
+            if (c->refresh) k_grow_fill<false, true><<<grid, kBlock, 0, st>>>(a, L);
+            else k_grow_fill<false, false><<<grid, kBlock, 0, st>>>(a, L);
         }
     }
+    cudaEventRecord(c->ev[6], st);
+    k_scan_tiles<0><<<2, 1024, 0, st>>>(a);
+    k_grow_lists<<<dim3(std::min<uint32_t>((max_tiles + kWarps - 1) / kWarps, (uint32_t)c->sms * 8), 2), kBlock, 0, st>>>(a);
     c->refresh = false;
     cudaEventRecord(c->ev[1], st);
     k_claim<<<(uint32_t)c->sms * 4, kBlock, 0, st>>>(a);
     cudaEventRecord(c->ev[2], st);
-    if (c->fp32) k_commit<true><<<(uint32_t)c->sms * 3, kBlock, 0, st>>>(a);
-    else k_commit<false><<<(uint32_t)c->sms * 3, kBlock, 0, st>>>(a);
-    k_step_end<<<(uint32_t)c->sms, kBlock, 0, st>>>(a, c->d_snap);
+    k_resolve<<<(uint32_t)c->sms * 4, kBlock, 0, st>>>(a);
+    k_scan_tiles<1><<<1, 1024, 0, st>>>(a);
+    if (c->fp32) k_commit<true><<<(uint32_t)c->sms * 4, kBlock, 0, st>>>(a);
+    else k_commit<false><<<(uint32_t)c->sms * 4, kBlock, 0, st>>>(a);
+    k_step_end<<<1, 1, 0, st>>>(a, c->d_snap);
     cudaEventRecord(c->ev[3], st);
-    c->launches += 5;
+    c->launches += 9;
     cudaError_t e = cudaMemcpyAsync(c->h_state, c->d_snap, sizeof(DevState), cudaMemcpyDeviceToHost, st);
     if (e == cudaSuccess) e = cudaStreamSynchronize(st);
     if (e != cudaSuccess) { c->failed = true; return c->cuda_fail(e, "growth step"); }
     const DevState hs = *c->h_state;
     if (hs.err) { c->failed = true; return check_device_errors(c, hs.err); }
-    float ms_grow = 0, ms_claim = 0, ms_commit = 0;
+    float ms_grow = 0, ms_claim = 0, ms_commit = 0, ms_fill = 0;
+    cudaEventElapsedTime(&ms_fill, c->ev[0], c->ev[6]);
+    c->tm.fill_ms += ms_fill;
     cudaEventElapsedTime(&ms_grow, c->ev[0], c->ev[1]);
     cudaEventElapsedTime(&ms_claim, c->ev[1], c->ev[2]);
     cudaEventElapsedTime(&ms_commit, c->ev[2], c->ev[3]);
     c->tm.grow_ms += ms_grow; c->tm.claim_ms += ms_claim; c->tm.commit_ms += ms_commit;
     c->tm.total_ms += ms_grow + ms_claim + ms_commit;
-    c->tm.grow_launches += 2;
-    c->tm.kernel_launches += 5;
+    c->tm.grow_launches += 2;  // fill-update launches (the grow_bytes kernels)
+    c->tm.kernel_launches += 9;
     // algorithmic bytes: grow 25 B (FP64: dir 1, vel 8, fill 8 r + 8 w) or 17 B (FP32: dir, vel 4, fill 4 + comp 4 r/w)
     const double bpu = c->fp32 ? 17.0 : 25.0;
     const uint64_t Sv = hs.sv[0] + hs.sv[1], nfull = (uint64_t)hs.nfull[0] + hs.nfull[1], nnew = (uint64_t)hs.nwin[0] + hs.nwin[1];

@@ -12,21 +12,25 @@
 // A cell whose driving force is <= 5e-16 stores vel = inc = -1 and is skipped, as the
 // reference skips it (calcGrowthStepInside, SCORE_Kernel.cpp:4046-4130).
 //
-//   k_grow    per list: fill update of every ACTIVE slot in [0, next_never), ordered
-//             compaction of full slots (FullRX list) and INACTIVE slots (recycle list,
-//             capped) with a decoupled look-back scan; Sv count.
+// Every ordered compaction (FullRX list, recycle list, slot ranks of new cells) is a
+// count pass, a one-block scan of the per-tile counts, and a write pass: no block
+// ever waits on another one.
+//   k_grow_fill   per list: fill update of every ACTIVE slot in [0, next_never);
+//                 1-bit masks of full and INACTIVE slots, per-tile counts; Sv count.
+//   k_scan_tiles  exclusive scan of the tile counts; list lengths into DevState.
+//   k_grow_lists  FullRX list and capped recycle list, in slot order.
 //   k_claim   one thread per full cell: the 26 infection attempts in the reference's
 //             order; a still-deformed target gets atomicMin(claim, attempt ordinal),
 //             where ordinal = 26 * (full-cell rank, Inside list first) + direction rank.
 //             The thread records which attempts it made (26-bit mask).
-//   k_commit  one thread per full cell, tiles in full-cell order: attempts whose claim
-//             holds the own ordinal won; winners are ranked per destination list by a
-//             look-back scan and take recycled slots first, then appended slots, like
+//   k_resolve one thread per full cell: attempts whose claim holds the own ordinal
+//             won; per-tile win counts per destination list.
+//   k_commit  winners are ranked per destination list in full-cell then direction
+//             order and take recycled slots first, then appended slots, like
 //             omp_getNextFreeSlotInRXFront*(CELLRECYCLE).  The full cell then becomes
 //             recrystallized (grid = ndefg + rxg, counts, slot INACTIVE) — the tail of
 //             updateFullRX{Inside,Border}, SCORE_Kernel.cpp:4559-4774.
-//   k_step_end  slot high-water marks, stats snapshot, reset of the per-step fields and
-//             of the look-back status words for the next step.
+//   k_step_end  slot high-water marks, stats snapshot, reset of the per-step fields.
 #pragma once
 #include <cstdint>
 #include "device_common.cuh"
@@ -44,6 +48,9 @@ struct DFront {
     uint8_t* dir;        // infector code 0..26 (| kStale), kInactive = INACTIVE
     uint32_t* full;      // FullRX list (slot indices, slot order)
     uint32_t* recyc;     // recycle list (slot indices, slot order, capped)
+    uint32_t* fmask;     // per 32 slots: full slots of this step (bit = slot % 32)
+    uint32_t* imask;     // per 32 slots: INACTIVE slots of this step
+    uint32_t* tcnt;      // per grow tile: (full, INACTIVE) counts, then their exclusive prefixes
     uint32_t cap;        // device capacity of the slot arrays
     uint32_t reccap;     // ntotalRecyclingList of the reference
 };
@@ -72,7 +79,9 @@ struct DomainArgs {
     DevState* st;
     uint32_t* grid;
     uint32_t* claim;
-    uint32_t* amask;            // per full cell: attempts made (bit d)
+    uint32_t* amask;            // per full cell: attempts made (bit d), then attempts won
+    uint32_t* tobm;             // per full cell: won attempts that go to the Border list
+    uint32_t* ctcnt;            // per commit tile: (Inside, Border) win counts, then prefixes
     unsigned long long* ptab;   // nrxg x ndefg mobility weights as bits (kPtabEmpty = unknown)
     const double* pforce;       // per deformed grain driving force (FP64)
     uint32_t* defg_cnt;
@@ -80,9 +89,6 @@ struct DomainArgs {
     uint32_t* depleted;
     unsigned long long* miss;   // table indices the host must fill
     uint32_t* pending;          // (list << 31) | slot of new cells waiting for P
-    unsigned long long* status; // look-back words: [0, s1) list 0, [s1, s2) list 1, [s2, s3) commit
-    uint32_t* tickets;          // tile tickets: 0,1 grow lists, 2 commit
-    uint32_t status_off1, status_off2, status_words;
     uint32_t misscap, pendcap;
     uint32_t nx, ny, nz, nxy;
     FastDiv dnx, dnxy;
@@ -148,7 +154,7 @@ __device__ __forceinline__ double velocity_factor(const DomainArgs& a, double P,
     return __dmul_rn(__dmul_rn(mobility(a, P), p), c_sf[code]);
 }
 
-// warp-0 exclusive scan of 2x64 tile counters laid out [item][warp]; tile totals in lane 0
+// warp-0 exclusive scan of 2x64 block-local counters laid out [item][warp]; totals in every lane
 __device__ __forceinline__ void scan64_pair(uint32_t* cntA, uint32_t* cntB, uint32_t& totA, uint32_t& totB) {
     const int lane = threadIdx.x & 31;
     uint32_t a0 = cntA[2 * lane], a1 = cntA[2 * lane + 1], b0 = cntB[2 * lane], b1 = cntB[2 * lane + 1];
@@ -166,35 +172,33 @@ __device__ __forceinline__ void scan64_pair(uint32_t* cntA, uint32_t* cntB, uint
 }
 
 // ------------------------------------------------------------------ K1 grow
-// One WARP per look-back tile of 32 x kGrowItems slots (slot = base + 32 k + lane):
-// warps never wait for each other except through the look-back words.
+// Three launches, none of which waits on another block:
+//   k_grow_fill   streams the slots of one list in tiles of kGrowTile (one block per
+//                 tile, grid-stride), updates the fills, and writes one bit per slot
+//                 (full / INACTIVE) plus the tile's two counts;
+//   k_scan_tiles  one block per scanned array: exclusive scan of the tile counts;
+//   k_grow_lists  one warp per tile expands the bit masks into the FullRX list and
+//                 the capped recycle list, in slot order.
 // REFRESH: recompute vel of every active slot from the P table and the current
 // physics (after T, rho or the drag changed) before growing it.
 constexpr int kGrowItems = 8;
-constexpr uint32_t kGrowTile = 32 * kGrowItems;
+constexpr uint32_t kGrowTile = kBlock * kGrowItems;  // 64 mask words per tile
 
 template <bool FP32, bool REFRESH>
-__global__ void __launch_bounds__(kBlock, 4) k_grow(DomainArgs a, int L) {
+__global__ void __launch_bounds__(kBlock, 4) k_grow_fill(DomainArgs a, int L) {
     constexpr int ITEMS = kGrowItems;
     const DFront fr = a.f[L];
-    unsigned long long* status = a.status + (L == 0 ? 0u : a.status_off1);
-    uint32_t* ticket = a.tickets + L;
     const uint32_t n = a.st->next_never[L];
     const uint32_t ntiles = (n + kGrowTile - 1) / kGrowTile;
-    if (blockIdx.x == 0 && threadIdx.x == 0) a.st->tiles_used[L] = ntiles;
-    const int lane = threadIdx.x & 31;
-    const uint32_t lt = lanemask_lt();
+    __shared__ uint32_t s_f[kWarps], s_i[kWarps];
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     unsigned long long sv = 0;
-    for (;;) {
-        uint32_t tile = 0;
-        if (lane == 0) tile = atomicAdd(ticket, 1u);
-        tile = __shfl_sync(0xFFFFFFFFu, tile, 0);
-        if (tile >= ntiles) break;
+    for (uint32_t tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
         const uint32_t base = tile * kGrowTile;
         uint8_t d[ITEMS];
 #pragma unroll
         for (int k = 0; k < ITEMS; ++k) {
-            const uint32_t slot = base + (uint32_t)(k * 32) + lane;
+            const uint32_t slot = base + (uint32_t)(k * kBlock) + threadIdx.x;
             d[k] = slot < n ? fr.dir[slot] : kInactive;
         }
         bool full[ITEMS];
@@ -202,7 +206,7 @@ __global__ void __launch_bounds__(kBlock, 4) k_grow(DomainArgs a, int L) {
             double w[ITEMS], fill[ITEMS];  // w: cached inc, or vel when the increment is stale
 #pragma unroll
             for (int k = 0; k < ITEMS; ++k) {
-                const uint32_t slot = base + (uint32_t)(k * 32) + lane;
+                const uint32_t slot = base + (uint32_t)(k * kBlock) + threadIdx.x;
                 w[k] = -1.0; fill[k] = 0.0;
                 if (d[k] != kInactive) {
                     if (REFRESH) {
@@ -223,7 +227,7 @@ __global__ void __launch_bounds__(kBlock, 4) k_grow(DomainArgs a, int L) {
                 full[k] = false;
                 if (d[k] != kInactive) {
                     ++sv;
-                    const uint32_t slot = base + (uint32_t)(k * 32) + lane;
+                    const uint32_t slot = base + (uint32_t)(k * kBlock) + threadIdx.x;
                     double inc = w[k];
                     if (REFRESH || a.dt_changed || (d[k] & kStale)) {
                         if (__double_as_longlong(w[k]) >= 0) inc = __dmul_rn(__dmul_rn(w[k], a.dt), a.cinv);
@@ -241,7 +245,7 @@ __global__ void __launch_bounds__(kBlock, 4) k_grow(DomainArgs a, int L) {
             float vel[ITEMS], fill[ITEMS], comp[ITEMS];
 #pragma unroll
             for (int k = 0; k < ITEMS; ++k) {
-                const uint32_t slot = base + (uint32_t)(k * 32) + lane;
+                const uint32_t slot = base + (uint32_t)(k * kBlock) + threadIdx.x;
                 vel[k] = -1.0f; fill[k] = 0.0f; comp[k] = 0.0f;
                 if (d[k] != kInactive) {
                     if (REFRESH) {
@@ -267,7 +271,7 @@ __global__ void __launch_bounds__(kBlock, 4) k_grow(DomainArgs a, int L) {
                         const float y = inc - comp[k];
                         const float t = fill[k] + y;
                         const float c = (t - fill[k]) - y;
-                        const uint32_t slot = base + (uint32_t)(k * 32) + lane;
+                        const uint32_t slot = base + (uint32_t)(k * kBlock) + threadIdx.x;
                         ((float*)fr.fill)[slot] = t;
                         fr.comp[slot] = c;
                         full[k] = (t - c) >= 1.0f;
@@ -275,36 +279,137 @@ __global__ void __launch_bounds__(kBlock, 4) k_grow(DomainArgs a, int L) {
                 }
             }
         }
-        uint32_t fm[ITEMS], im[ITEMS], totF = 0, totI = 0;
+        uint32_t cf = 0, ci = 0;
 #pragma unroll
         for (int k = 0; k < ITEMS; ++k) {
-            fm[k] = __ballot_sync(0xFFFFFFFFu, full[k]);
-            im[k] = __ballot_sync(0xFFFFFFFFu, d[k] == kInactive && base + (uint32_t)(k * 32) + lane < n);
-            totF += __popc(fm[k]);
-            totI += __popc(im[k]);
-        }
-        uint32_t exF, exI;
-        lookback2(status, tile, totF, totI, exF, exI, &a.st->err);
-        if (tile == ntiles - 1 && lane == 0) {
-            a.st->nfull[L] = exF + totF;
-            a.st->ninactive[L] = exI + totI;
-            a.st->nrec[L] = min(exI + totI, fr.reccap);
-        }
-#pragma unroll
-        for (int k = 0; k < ITEMS; ++k) {
-            const uint32_t slot = base + (uint32_t)(k * 32) + lane;
-            if ((fm[k] >> lane) & 1u) fr.full[exF + __popc(fm[k] & lt)] = slot;
-            if ((im[k] >> lane) & 1u) {
-                const uint32_t r = exI + __popc(im[k] & lt);
-                if (r < fr.reccap) fr.recyc[r] = slot;
+            const uint32_t fm = __ballot_sync(0xFFFFFFFFu, full[k]);
+            const uint32_t im = __ballot_sync(0xFFFFFFFFu, d[k] == kInactive && base + (uint32_t)(k * kBlock) + threadIdx.x < n);
+            if (lane == 0) {
+                const uint32_t word = tile * (kGrowTile / 32) + (uint32_t)(k * kWarps + warp);  // slots 32 word .. 32 word + 31
+                fr.fmask[word] = fm;
+                fr.imask[word] = im;
             }
-            exF += __popc(fm[k]);
-            exI += __popc(im[k]);
+            cf += __popc(fm);
+            ci += __popc(im);
         }
+        if (lane == 0) { s_f[warp] = cf; s_i[warp] = ci; }
+        __syncthreads();
+        if (threadIdx.x == 0) {
+            uint32_t tf = 0, ti = 0;
+#pragma unroll
+            for (int w = 0; w < kWarps; ++w) { tf += s_f[w]; ti += s_i[w]; }
+            fr.tcnt[2 * tile] = tf;
+            fr.tcnt[2 * tile + 1] = ti;
+        }
+        __syncthreads();
     }
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) sv += __shfl_down_sync(0xFFFFFFFFu, sv, o);
     if (lane == 0 && sv) atomicAdd(&a.st->sv[L], sv);
+}
+
+// In-place exclusive scan of `ntiles` (a, b) count pairs by one block of 1024 threads;
+// returns the totals in thread 0.
+__device__ __forceinline__ void scan_pairs_block(uint32_t* cnt, uint32_t ntiles, uint32_t& totA, uint32_t& totB) {
+    constexpr int T = 1024, PER = 4;
+    __shared__ uint32_t s_a[T / 32], s_b[T / 32];
+    __shared__ uint32_t s_carry[2];
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    if (threadIdx.x == 0) { s_carry[0] = 0; s_carry[1] = 0; }
+    __syncthreads();
+    for (uint32_t base = 0; base < ntiles; base += T * PER) {
+        uint32_t va[PER], vb[PER], sa = 0, sb = 0;
+#pragma unroll
+        for (int j = 0; j < PER; ++j) {
+            const uint32_t i = base + threadIdx.x * PER + j;
+            va[j] = i < ntiles ? cnt[2 * i] : 0u;
+            vb[j] = i < ntiles ? cnt[2 * i + 1] : 0u;
+            sa += va[j]; sb += vb[j];
+        }
+        uint32_t ia = sa, ib = sb;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            const uint32_t xa = __shfl_up_sync(0xFFFFFFFFu, ia, o), xb = __shfl_up_sync(0xFFFFFFFFu, ib, o);
+            if (lane >= o) { ia += xa; ib += xb; }
+        }
+        if (lane == 31) { s_a[warp] = ia; s_b[warp] = ib; }
+        __syncthreads();
+        if (warp == 0) {
+            uint32_t wa = s_a[lane], wb = s_b[lane];
+#pragma unroll
+            for (int o = 1; o < 32; o <<= 1) {
+                const uint32_t xa = __shfl_up_sync(0xFFFFFFFFu, wa, o), xb = __shfl_up_sync(0xFFFFFFFFu, wb, o);
+                if (lane >= o) { wa += xa; wb += xb; }
+            }
+            s_a[lane] = wa; s_b[lane] = wb;  // inclusive warp prefixes
+        }
+        __syncthreads();
+        uint32_t ea = s_carry[0] + (warp ? s_a[warp - 1] : 0u) + ia - sa;
+        uint32_t eb = s_carry[1] + (warp ? s_b[warp - 1] : 0u) + ib - sb;
+#pragma unroll
+        for (int j = 0; j < PER; ++j) {
+            const uint32_t i = base + threadIdx.x * PER + j;
+            if (i < ntiles) { cnt[2 * i] = ea; cnt[2 * i + 1] = eb; }
+            ea += va[j]; eb += vb[j];
+        }
+        __syncthreads();
+        if (threadIdx.x == 0) { s_carry[0] += s_a[31]; s_carry[1] += s_b[31]; }
+        __syncthreads();
+    }
+    totA = s_carry[0];
+    totB = s_carry[1];
+}
+
+// block L scans the grow tile counts of list L; blocks 2 scans the commit tiles
+template <int KIND>
+__global__ void __launch_bounds__(1024) k_scan_tiles(DomainArgs a) {
+    uint32_t tA, tB;
+    if (KIND == 0) {
+        const int L = blockIdx.x;
+        const uint32_t n = a.st->next_never[L];
+        scan_pairs_block(a.f[L].tcnt, (n + kGrowTile - 1) / kGrowTile, tA, tB);
+        if (threadIdx.x == 0) {
+            a.st->nfull[L] = tA;
+            a.st->ninactive[L] = tB;
+            a.st->nrec[L] = min(tB, a.f[L].reccap);
+        }
+    } else {
+        const uint32_t F = a.st->nfull[0] + a.st->nfull[1];
+        scan_pairs_block(a.ctcnt, (F + kBlock - 1) / kBlock, tA, tB);
+        if (threadIdx.x == 0) { a.st->nwin[0] = tA; a.st->nwin[1] = tB; }
+    }
+}
+
+// one warp per grow tile: lane l owns mask words 2l and 2l+1 of the tile
+__global__ void __launch_bounds__(kBlock) k_grow_lists(DomainArgs a) {
+    const int L = blockIdx.y;
+    const DFront fr = a.f[L];
+    const uint32_t n = a.st->next_never[L];
+    const uint32_t ntiles = (n + kGrowTile - 1) / kGrowTile;
+    const int lane = threadIdx.x & 31;
+    const uint32_t gw = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, nw = (gridDim.x * blockDim.x) >> 5;
+    const uint32_t lt = lanemask_lt();
+    for (uint32_t tile = gw; tile < ntiles; tile += nw) {
+        const uint32_t w0 = tile * (kGrowTile / 32) + 2 * lane;
+        const uint32_t f0 = fr.fmask[w0], f1 = fr.fmask[w0 + 1], i0 = fr.imask[w0], i1 = fr.imask[w0 + 1];
+        const uint32_t cf = __popc(f0) + __popc(f1), ci = __popc(i0) + __popc(i1);
+        uint32_t xf = cf, xi = ci;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            const uint32_t a1 = __shfl_up_sync(0xFFFFFFFFu, xf, o), b1 = __shfl_up_sync(0xFFFFFFFFu, xi, o);
+            if (lane >= o) { xf += a1; xi += b1; }
+        }
+        uint32_t rf = fr.tcnt[2 * tile] + xf - cf, ri = fr.tcnt[2 * tile + 1] + xi - ci;
+        (void)lt;
+        const uint32_t words[2][2] = {{f0, f1}, {i0, i1}};
+        for (int h = 0; h < 2; ++h) {
+            const uint32_t sbase = (w0 + h) * 32;
+            uint32_t m = words[0][h];
+            while (m) { const int b = __ffs(m) - 1; m &= m - 1; fr.full[rf++] = sbase + b; }
+            m = words[1][h];
+            while (m && ri < fr.reccap) { const int b = __ffs(m) - 1; m &= m - 1; fr.recyc[ri++] = sbase + b; }
+        }
+    }
 }
 
 // ------------------------------------------------------------------ K2 claim
@@ -448,30 +553,29 @@ __device__ __forceinline__ bool lookup_p(const DomainArgs& a, uint32_t rxg, uint
 }
 
 // ------------------------------------------------------------------ K3 commit (+ finalize)
-// One WARP per look-back tile of 32 full cells (full-cell order).
-template <bool FP32>
-__global__ void __launch_bounds__(kBlock, 3) k_commit(DomainArgs a) {
+// k_resolve: one thread per full cell (tiles of kBlock full cells, grid-stride): its
+// attempts whose claim holds the own ordinal won; writes the win mask, the mask of wins
+// that go to the Border list, and the tile's two win counts.
+// k_commit (after k_scan_tiles<1>): winners are ranked per destination list in
+// full-cell then direction order and take recycled slots first, then appended slots,
+// like omp_getNextFreeSlotInRXFront*(CELLRECYCLE); the full cell then becomes
+// recrystallized (grid = ndefg + rxg, counts, slot INACTIVE).
+__global__ void __launch_bounds__(kBlock, 2) k_resolve(DomainArgs a) {
     const uint32_t F0 = a.st->nfull[0], F = F0 + a.st->nfull[1];
     if (26ull * F >= 0xFFFFFFFFull) return;
-    unsigned long long* status = a.status + a.status_off2;
-    const uint32_t ntiles = (F + 31) / 32;
-    if (blockIdx.x == 0 && threadIdx.x == 0) a.st->tiles_used[2] = ntiles;
-    const int lane = threadIdx.x & 31;
-    for (;;) {
-        uint32_t tile = 0;
-        if (lane == 0) tile = atomicAdd(a.tickets + 2, 1u);
-        tile = __shfl_sync(0xFFFFFFFFu, tile, 0);
-        if (tile >= ntiles) break;
-        const uint32_t f = tile * 32 + lane;
-        uint32_t win = 0, tob = 0, slot = 0, cell = 0;
-        int L = 0, x = 0, y = 0, z = 0;
+    const uint32_t ntiles = (F + kBlock - 1) / kBlock;
+    __shared__ uint32_t s_a[kWarps], s_b[kWarps];
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    for (uint32_t tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
+        const uint32_t f = tile * kBlock + threadIdx.x;
+        uint32_t win = 0, tob = 0;
         if (f < F) {
             const uint32_t mask = a.amask[f];
-            L = f >= F0 ? 1 : 0;
-            slot = a.f[L].full[L ? f - F0 : f];
-            cell = a.f[L].xyz[slot];
-            decode(a, cell, x, y, z);
             if (mask) {
+                const int L = f >= F0 ? 1 : 0;
+                const uint32_t slot = a.f[L].full[L ? f - F0 : f];
+                int x, y, z;
+                decode(a, a.f[L].xyz[slot], x, y, z);
                 const bool allB = (L == 0) && !(x > 1 && x < (int)a.nx - 2 && y > 1 && y < (int)a.ny - 2 && z > 1 && z < (int)a.nz - 2);
                 uint32_t cl[26];
                 uint32_t inter_m = 0;
@@ -496,7 +600,35 @@ __global__ void __launch_bounds__(kBlock, 3) k_commit(DomainArgs a) {
                     }
                 }
             }
+            a.amask[f] = win;
+            a.tobm[f] = tob;
         }
+        uint32_t cB = __popc(tob), cA = __popc(win) - cB;
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) { cA += __shfl_down_sync(0xFFFFFFFFu, cA, o); cB += __shfl_down_sync(0xFFFFFFFFu, cB, o); }
+        if (lane == 0) { s_a[warp] = cA; s_b[warp] = cB; }
+        __syncthreads();
+        if (threadIdx.x == 0) {
+            uint32_t ta = 0, tb = 0;
+#pragma unroll
+            for (int w = 0; w < kWarps; ++w) { ta += s_a[w]; tb += s_b[w]; }
+            a.ctcnt[2 * tile] = ta;
+            a.ctcnt[2 * tile + 1] = tb;
+        }
+        __syncthreads();
+    }
+}
+
+template <bool FP32>
+__global__ void __launch_bounds__(kBlock, 2) k_commit(DomainArgs a) {
+    const uint32_t F0 = a.st->nfull[0], F = F0 + a.st->nfull[1];
+    if (26ull * F >= 0xFFFFFFFFull) return;
+    const uint32_t ntiles = (F + kBlock - 1) / kBlock;
+    __shared__ uint32_t s_a[kWarps], s_b[kWarps];
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    for (uint32_t tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
+        const uint32_t f = tile * kBlock + threadIdx.x;
+        const uint32_t win = f < F ? a.amask[f] : 0u, tob = f < F ? a.tobm[f] : 0u;
         const uint32_t cB = __popc(tob), cA = __popc(win) - cB;
         uint32_t iA = cA, iB = cB;
 #pragma unroll
@@ -504,15 +636,21 @@ __global__ void __launch_bounds__(kBlock, 3) k_commit(DomainArgs a) {
             const uint32_t xa = __shfl_up_sync(0xFFFFFFFFu, iA, o), xb = __shfl_up_sync(0xFFFFFFFFu, iB, o);
             if (lane >= o) { iA += xa; iB += xb; }
         }
-        const uint32_t totA = __shfl_sync(0xFFFFFFFFu, iA, 31), totB = __shfl_sync(0xFFFFFFFFu, iB, 31);
-        uint32_t pA, pB;
-        lookback2(status, tile, totA, totB, pA, pB, &a.st->err);
-        if (tile == ntiles - 1 && lane == 0) { a.st->nwin[0] = pA + totA; a.st->nwin[1] = pB + totB; }
+        if (lane == 31) { s_a[warp] = iA; s_b[warp] = iB; }
+        __syncthreads();
+        uint32_t rA = a.ctcnt[2 * tile] + iA - cA, rB = a.ctcnt[2 * tile + 1] + iB - cB;
+#pragma unroll
+        for (int w = 0; w < kWarps; ++w)
+            if (w < warp) { rA += s_a[w]; rB += s_b[w]; }
         if (f < F) {
+            const int L = f >= F0 ? 1 : 0;
             const DFront& src = a.f[L];
+            const uint32_t slot = src.full[L ? f - F0 : f];
+            const uint32_t cell = src.xyz[slot];
             const uint32_t rsrc = src.rxg[slot], gsrc = src.defg[slot];
             if (win) {
-                uint32_t rA = pA + iA - cA, rB = pB + iB - cB;
+                int x, y, z;
+                decode(a, cell, x, y, z);
                 double over = 0.0;
                 float over32 = 0.0f;
                 if (!FP32) over = __dsub_rn(((const double*)src.fill)[slot], 1.0);
@@ -572,33 +710,23 @@ __global__ void __launch_bounds__(kBlock, 3) k_commit(DomainArgs a) {
             if (!FP32) ((double*)src.fill)[slot] = 0.0;
             else { ((float*)src.fill)[slot] = 0.0f; src.comp[slot] = 0.0f; }
         }
+        __syncthreads();
     }
 }
 
 // ------------------------------------------------------------------ K4 step end
-// Thread 0 of block 0 advances the high-water marks, snapshots the per-step fields
-// for the host and clears them and the tickets; all blocks clear the look-back words
-// this step's scans used (no kernel of this step reads them any more), so every word
-// is zero again at the start of the next step.
-__global__ void __launch_bounds__(kBlock) k_step_end(DomainArgs a, DevState* snapshot) {
-    if (blockIdx.x == 0 && threadIdx.x == 0) {
-        DevState* st = a.st;
-        const uint32_t cap[2] = {a.f[0].cap, a.f[1].cap};
-        for (int D = 0; D < 2; ++D) {
-            if (st->nwin[D] > st->nrec[D]) st->next_never[D] += st->nwin[D] - st->nrec[D];
-            if (st->next_never[D] > cap[D]) { st->next_never[D] = cap[D]; st->err |= kErrCapacity; }
-        }
-        *snapshot = *st;
-        char* p = (char*)st + kStepFieldsOffset;
-        for (size_t i = 0; i < sizeof(DevState) - kStepFieldsOffset; ++i) p[i] = 0;
-        a.tickets[0] = a.tickets[1] = a.tickets[2] = 0;
+// Advances the high-water marks, snapshots the per-step fields for the host and
+// clears them for the next step.
+__global__ void k_step_end(DomainArgs a, DevState* snapshot) {
+    DevState* st = a.st;
+    const uint32_t cap[2] = {a.f[0].cap, a.f[1].cap};
+    for (int D = 0; D < 2; ++D) {
+        if (st->nwin[D] > st->nrec[D]) st->next_never[D] += st->nwin[D] - st->nrec[D];
+        if (st->next_never[D] > cap[D]) { st->next_never[D] = cap[D]; st->err |= kErrCapacity; }
     }
-    const uint32_t off[3] = {0u, a.status_off1, a.status_off2};
-    const uint32_t lim[3] = {a.status_off1, a.status_off2, a.status_words};
-    for (int r = 0; r < 3; ++r) {
-        const uint32_t used = min(a.st->tiles_used[r] + 1u, lim[r] - off[r]);
-        for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < used; i += gridDim.x * blockDim.x) a.status[off[r] + i] = 0ull;
-    }
+    *snapshot = *st;
+    char* p = (char*)st + kStepFieldsOffset;
+    for (size_t i = 0; i < sizeof(DevState) - kStepFieldsOffset; ++i) p[i] = 0;
 }
 
 }  // namespace score
