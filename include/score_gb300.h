@@ -36,6 +36,7 @@ extern "C" {
 #define SCORE_ERR_IO                -8  /* .uds file missing or malformed */
 #define SCORE_ERR_KEYLIMIT          -9  /* more infection attempts in one step than the 32-bit claim key can order */
 #define SCORE_ERR_NOT_BUILT        -10  /* CUDA path unavailable (no device) */
+#define SCORE_ERR_SCRATCH_LIMIT    -11  /* input larger than a no-allocation entry point's static scratch */
 
 #define SCORE_MAX_TABLE 256        /* max rows of the time tables (annealing, drag) and X logpoint lists */
 
@@ -202,6 +203,38 @@ int  score_get_timing(score_ctx* ctx, score_timing* out);
 /* FP64 mobility weight P(rxg,defg) on the host, the reference's formula
  * (SCORE_Kernel.cpp:2460-2527, SCORE_Math.cpp:558-622,1067-1130) */
 int  score_mobility_weight(const score_params* p, const double* rxg_q, const double* defg_q, double* P);
+
+/*
+ * No counterpart in the reference (it evaluates P pair by pair on the host,
+ * SCORE_Kernel.cpp:2460-2527).  Device FP64 table of P(rxg, defg) for all
+ * nrxg x ndefg pairs and its maximum, for callers that cannot allocate device
+ * memory.  cudaMalloc and cudaFree synchronize the whole device and can fail once
+ * another allocator (a framework's caching allocator, a fixed per-process budget)
+ * holds the memory; a caller that runs beside other streams' work, or inside such
+ * a budget, can call this instead of building the table through a context.
+ *
+ *   d_rxg_quat  device, nrxg x 4 quaternions      d_defg_quat  device, ndefg x 4
+ *   d_table     device, nrxg x ndefg doubles (row rxg, column defg), written
+ *   d_pmax      device, one double, written with the maximum of the table
+ *   stream      cudaStream_t the kernel is launched on (NULL = legacy default stream)
+ * Runs on the calling thread's current device and returns after the launch; the
+ * results are ready when the stream reaches that point.  Allocates nothing: its
+ * only scratch is a static 512 KiB device array with one word per row, so nrxg is
+ * at most 65536 (SCORE_ERR_SCRATCH_LIMIT above that, nothing launched).  The
+ * scratch holds a completion counter that must be 0 when a launch starts; the
+ * library's last block of every launch resets it, so it stays 0 between calls.
+ * The first call on a device resolves the scratch address (cudaGetSymbolAddress,
+ * which may load the library's device code); a caller that captures streams into
+ * graphs makes that first call before it begins a capture.  Calls on the same
+ * device share the scratch: calls that overlap in time (two streams, two host
+ * threads) race and must be serialized by the caller.  Entries agree with
+ * score_mobility_weight to a few ulp (CUDA's acos/cos/exp/pow instead of libm);
+ * a pair within a few ulp of the 15-degree or 10-degree threshold can fall into
+ * the other class.
+ */
+int  score_mobility_table_noalloc(const score_params* p, const double* d_rxg_quat, uint32_t nrxg,
+                                  const double* d_defg_quat, uint32_t ndefg, double* d_table,
+                                  double* d_pmax, void* stream);
 
 /*
  * Deterministic synthetic domain (identical bits on x86-64 and aarch64): periodic

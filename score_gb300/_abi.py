@@ -106,6 +106,7 @@ SIGNATURES = {
     "score_grain_counts": (C.c_int, [_vp, _vp, _vp]),
     "score_get_timing": (C.c_int, [_vp, _P(Timing)]),
     "score_mobility_weight": (C.c_int, [_P(Params), _vp, _vp, _P(_d)]),
+    "score_mobility_table_noalloc": (C.c_int, [_P(Params), _vp, _u32, _vp, _u32, _vp, _vp, _vp]),
     "score_gen_default": (C.c_int, [_P(GenParams)]),
     "score_generate_domain": (C.c_int, [_P(GenParams), _vp, _vp, _vp, _vp, _vp, _vp]),
 }

@@ -19,6 +19,7 @@
 #include <cstddef>
 #include <cstdio>
 #include <cstring>
+#include <mutex>
 #include <string>
 #include <thread>
 #include <unordered_set>
@@ -562,6 +563,7 @@ const char* score_status_string(int s) {
         case SCORE_ERR_IO: return "input file error";
         case SCORE_ERR_KEYLIMIT: return "too many infection attempts in one step";
         case SCORE_ERR_NOT_BUILT: return "CUDA device unavailable";
+        case SCORE_ERR_SCRATCH_LIMIT: return "input larger than the static scratch of a no-allocation entry point (nrxg > 65536)";
         default: return "unknown status";
     }
 }
@@ -964,3 +966,153 @@ int score_get_timing(score_ctx* c, score_timing* out) {
 }
 
 }  // extern "C"
+
+// ------------------------------------------------------------------ no-allocation table
+// Device FP64 mobility-weight table P(rxg, defg) for all pairs, with the grid-wide
+// maximum, in a form that allocates no memory: the only scratch is the file-scope
+// static device array below, whose address is resolved once per device.
+//
+// The table is the reference's formula (SCORE_Kernel.cpp:2460-2527: Sebald-Gottstein
+// -1 / 0 / cos^2 near 40deg<111>, or the Rollett-Holm sigmoid) evaluated with CUDA's
+// FP64 math functions (acos, cos, exp, pow) instead of the host libm, so entries agree
+// with score_mobility_weight to a few ulp; pairs whose disorientation lies within a
+// few ulp of a class threshold (15 deg, 10 deg from 40deg<111>) can land in the other
+// class.  The growth step itself does not use this table: it keeps the host's values.
+namespace {
+
+// Static scratch of the entry point: 256 B of header + one word per table row.
+//   word 0          blocks of the current launch that have finished.  MUST be 0 when a
+//                   launch starts: it is 0 after module load, and the last block of
+//                   every launch sets it back to 0.
+//   words 32 .. 32 + nrxg - 1   maximum P of each row (FP64 bits), written before read.
+constexpr uint32_t kTableMaxRows = 65536;
+constexpr uint32_t kTableHeaderWords = 32;
+static __device__ __align__(256) unsigned long long g_table_scratch[kTableHeaderWords + kTableMaxRows];  // 512 KiB + 256 B
+
+struct TableArgs {
+    int32_t model;                  // SCORE_MOBILITY_*
+    double fac, lagb, maxdev, m40[4];
+    double rh_cut, rh_trans, rh_expo;
+};
+
+__device__ double d_weight(const DomainArgs& A, const TableArgs& t, const double pr[4], const double qd[4]) {
+    const double theta = d_disori(A, pr, qd, nullptr);
+    if (t.model == SCORE_MOBILITY_ROLLETT_HOLM)
+        return 1.0 - (t.rh_cut * exp(-1.0 * t.rh_trans * pow(theta / t.lagb, t.rh_expo)));
+    if (theta <= t.lagb) return -1.0;
+    // disorientation quaternion of the best symmetry candidate, components sorted descending
+    double c[6][4];
+    d_grimmer(A, pr, qd, c);
+    int mi = 0;
+    double mx = 0.0;
+#pragma unroll
+    for (int i = 0; i < 6; ++i)
+#pragma unroll
+        for (int j = 0; j < 4; ++j)
+            if (fabs(c[i][j]) > mx) { mx = fabs(c[i][j]); mi = i; }
+    double s[4] = {fabs(c[mi][0]), fabs(c[mi][1]), fabs(c[mi][2]), fabs(c[mi][3])};
+#pragma unroll
+    for (int i = 0; i < 3; ++i)
+#pragma unroll
+        for (int k = 0; k < 3 - i; ++k)
+            if (s[k] > s[k + 1]) { const double x = s[k]; s[k] = s[k + 1]; s[k + 1] = x; }
+    const double qdis[4] = {s[3], s[2], s[1], s[0]};
+    const double dev = d_disori(A, qdis, t.m40, nullptr);
+    if (dev < t.maxdev) {
+        const double cs = cos(0.5 * kPi * dev / t.maxdev);
+        return cs * cs;
+    }
+    return 0.0;
+}
+
+// one block per row rxg; the last block to finish reduces the row maxima
+__global__ void __launch_bounds__(256) k_mobility_table(TableArgs t, const double* __restrict__ rxq, uint32_t nrxg,
+                                                        const double* __restrict__ dfq, uint32_t ndefg,
+                                                        double* __restrict__ table, double* __restrict__ pmax,
+                                                        unsigned long long* scratch) {
+    DomainArgs A{};
+    A.pc_fac = t.fac;
+    __shared__ double s_max[8];
+    __shared__ bool s_last;
+    const uint32_t row = blockIdx.x;
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const double pr[4] = {rxq[4 * (size_t)row], rxq[4 * (size_t)row + 1], rxq[4 * (size_t)row + 2], rxq[4 * (size_t)row + 3]};
+    double m = -HUGE_VAL;
+    for (uint32_t j = threadIdx.x; j < ndefg; j += blockDim.x) {
+        const double qd[4] = {dfq[4 * (size_t)j], dfq[4 * (size_t)j + 1], dfq[4 * (size_t)j + 2], dfq[4 * (size_t)j + 3]};
+        const double P = d_weight(A, t, pr, qd);
+        table[(size_t)row * ndefg + j] = P;
+        m = fmax(m, P);
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) m = fmax(m, __shfl_xor_sync(0xFFFFFFFFu, m, o));
+    if (lane == 0) s_max[warp] = m;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        double bm = s_max[0];
+        for (int w = 1; w < (int)(blockDim.x >> 5); ++w) bm = fmax(bm, s_max[w]);
+        scratch[kTableHeaderWords + row] = (unsigned long long)__double_as_longlong(bm);
+        __threadfence();
+        const unsigned long long done = atomicAdd(&scratch[0], 1ull);
+        s_last = (done == (unsigned long long)nrxg - 1);
+    }
+    __syncthreads();
+    if (!s_last) return;
+    __threadfence();
+    double g = -HUGE_VAL;
+    for (uint32_t r = threadIdx.x; r < nrxg; r += blockDim.x)
+        g = fmax(g, __longlong_as_double((long long)__ldcg(&scratch[kTableHeaderWords + r])));
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) g = fmax(g, __shfl_xor_sync(0xFFFFFFFFu, g, o));
+    if (lane == 0) s_max[warp] = g;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        double bm = s_max[0];
+        for (int w = 1; w < (int)(blockDim.x >> 5); ++w) bm = fmax(bm, s_max[w]);
+        *pmax = bm;
+        scratch[0] = 0ull;  // ready for the next launch
+    }
+}
+
+// scratch address per device ordinal, resolved once with that device current
+constexpr int kMaxDevices = 64;
+std::mutex g_setup_mu;
+unsigned long long* g_scratch_of[kMaxDevices] = {};
+
+int table_scratch(int device, unsigned long long** out) {
+    std::lock_guard<std::mutex> lock(g_setup_mu);
+    if (!g_scratch_of[device]) {
+        void* p = nullptr;
+        const cudaError_t e = cudaGetSymbolAddress(&p, g_table_scratch);
+        if (e != cudaSuccess || !p) return SCORE_ERR_CUDA;
+        g_scratch_of[device] = (unsigned long long*)p;
+    }
+    *out = g_scratch_of[device];
+    return SCORE_OK;
+}
+
+}  // namespace
+
+extern "C" int score_mobility_table_noalloc(const score_params* p, const double* d_rxg_quat, uint32_t nrxg,
+                                            const double* d_defg_quat, uint32_t ndefg, double* d_table,
+                                            double* d_pmax, void* stream) {
+    if (!p || !d_rxg_quat || !d_defg_quat || !d_table || !d_pmax || nrxg == 0 || ndefg == 0) return SCORE_ERR_ARG;
+    if (nrxg > kTableMaxRows) return SCORE_ERR_SCRATCH_LIMIT;
+    if (p->mobility_model != SCORE_MOBILITY_SEBALD_GOTTSTEIN && p->mobility_model != SCORE_MOBILITY_ROLLETT_HOLM)
+        return SCORE_ERR_ARG;
+    int device = -1;
+    if (cudaGetDevice(&device) != cudaSuccess || device < 0) return SCORE_ERR_NOT_BUILT;
+    if (device >= kMaxDevices) return SCORE_ERR_ARG;
+    unsigned long long* scratch = nullptr;
+    const int s = table_scratch(device, &scratch);
+    if (s != SCORE_OK) return s;
+    TableArgs t{};
+    t.model = p->mobility_model;
+    double theta_sat = 0.0;
+    weight_constants(*p, &t.fac, &t.lagb, &t.maxdev, t.m40, &theta_sat);
+    t.rh_cut = p->RH_cut;
+    t.rh_trans = p->RH_trans;
+    t.rh_expo = p->RH_exponent;
+    k_mobility_table<<<nrxg, 256, 0, (cudaStream_t)stream>>>(t, d_rxg_quat, nrxg, d_defg_quat, ndefg, d_table, d_pmax, scratch);
+    return cudaGetLastError() == cudaSuccess ? SCORE_OK : SCORE_ERR_CUDA;
+}
