@@ -189,10 +189,10 @@ def cpu_baseline(n: int = 256) -> dict:
 
 
 def run_reference_arm(args) -> None:
+    """The reference's CPU algorithm on the host cores; under torchrun only rank 0
+    works and prints, the other ranks exit at once (no process group needed)."""
     rank, world, _ = dist_env()
-    dist = init_dist(world)
     if rank != 0:
-        barrier(dist)
         return
     import oracle
     oracle.build_oracle()
@@ -220,7 +220,6 @@ def run_reference_arm(args) -> None:
                                        f"{cores} processes x one {n}^3 domain each, to X>0.99"},
             "e2e": {"value": v, "unit": "updates/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line), flush=True)
-    barrier(dist)
 
 
 def main():

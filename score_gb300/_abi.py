@@ -21,6 +21,7 @@ ERR_STATE = -7
 ERR_IO = -8
 ERR_KEYLIMIT = -9
 ERR_NOT_BUILT = -10
+ERR_SCRATCH_LIMIT = -11
 
 MOBILITY_SEBALD_GOTTSTEIN = 1
 MOBILITY_ROLLETT_HOLM = 2

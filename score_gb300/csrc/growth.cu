@@ -595,7 +595,7 @@ int score_create(score_ctx** out, const score_params* p, int device) {
     *out = nullptr;
     if (p->nx < 3 || p->ny < 3 || p->nz < 3) return SCORE_ERR_ARG;
     const uint64_t N = (uint64_t)p->nx * p->ny * p->nz;
-    if (N >= 0x7FFFFFFFull) return SCORE_ERR_ARG;  // 31-bit slot counters in the look-back words
+    if (N >= 0x7FFFFFFFull) return SCORE_ERR_ARG;  // pending-list entries keep the list id in bit 31 of a slot index
     if (p->n_schedule < 1) return SCORE_ERR_ARG;
     int ndev = 0;
     if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) return SCORE_ERR_NOT_BUILT;

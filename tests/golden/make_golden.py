@@ -1,0 +1,106 @@
+"""Generate the golden fixtures of tests/golden/ from the SCORE reference itself.
+
+Each growth case: a small synthetic domain (this package's deterministic generator; the reference
+accepts edges of 50 cells and more, SCORE_Defs_Functionality.h:84),
+a .uds parameter file (UdsSpec), and the reference's own growth loop run on them by
+the harness in oracle/ref (reference sources compiled by oracle/ref/Makefile,
+OMP_NUM_THREADS=1, the canonical order).  The fixture stores the inputs (the .uds
+text and the domain arrays, so tests do not depend on the generator) and the
+reference's per-step trace and final labels.
+
+The ptab case stores the reference's mobility weights P(rxg, defg) for every pair
+(reg_calc_mobilityweight, SCORE_Kernel.cpp:2460-2527) of a small grain set.
+
+Run from the repository root where the reference sources exist:
+    python tests/golden/make_golden.py
+"""
+from __future__ import annotations
+
+import sys
+import tempfile
+from pathlib import Path
+
+import numpy as np
+
+HERE = Path(__file__).resolve().parent
+ROOT = HERE.parent.parent
+sys.path.insert(0, str(ROOT))
+
+import oracle  # noqa: E402
+import score_gb300 as sg  # noqa: E402
+
+# name: (UdsSpec overrides, (nx, ny, nz, grains, nuclei, seed), generator overrides)
+CASES = {
+    "base": ({}, (50, 50, 50, 20, 12, 101), {}),
+    "noncubic": ({}, (50, 64, 56, 30, 20, 102), {}),
+    "distinct_mob": ({"LAGBm0": "30.0", "GSm0": "600.0"}, (50, 50, 50, 30, 24, 103), {}),
+    "rollett_holm": ({"mobility_model": 2}, (50, 50, 50, 30, 24, 104), {}),
+    "defrag": ({"defragmentation": 1, "defrag_x": ["0.2", "0.5", "0.8"]}, (50, 50, 50, 25, 16, 105), {}),
+    "recovery_mp": ({"recovery": 3}, (50, 50, 50, 25, 16, 106), {}),
+    "zener_timedep": ({"zener": 2, "zener_table": [("0.0", "0.0"), ("0.1", "4.0e5"), ("360000.0", "4.0e5")]},
+                      (50, 50, 50, 25, 16, 107), {}),
+    "heating": ({"schedule": [("0.0", "700.0"), ("0.05", "760.0"), ("360000.0", "760.0")]}, (50, 50, 50, 25, 16, 108), {}),
+    "many_nuclei_small_cache": ({"initial_cache": "0.05"}, (56, 56, 56, 30, 150, 109), {}),
+    "texture_bimodal": ({}, (50, 50, 50, 40, 30, 110),
+                        {"ori_mode": 1, "ncomp": 3, "scatter_deg": 10.0, "rho_mode": 1, "rho_lo": 1e14, "rho_hi": 5e15}),
+}
+PTAB = (40, 80, 111)  # nrxg, ndefg, seed
+
+
+def narrow(a: np.ndarray) -> np.ndarray:
+    """u32 ids stored as u16 when they fit (the tests widen them again)."""
+    return a.astype(np.uint16) if a.size and int(a.max()) < 65536 else a
+
+
+def domain_arrays(d: sg.Domain) -> dict:
+    return {"dims": np.array([d.nx, d.ny, d.nz], dtype=np.uint32), "grid": narrow(d.grid), "defg_quat": d.defg_quat,
+            "defg_rho0": d.defg_rho0, "rxg_quat": d.rxg_quat, "rxg_site": d.rxg_site, "rxg_tincub": d.rxg_tincub}
+
+
+def make_case(name: str, kw: dict, geo: tuple, gkw: dict, wd: Path) -> Path:
+    nx, ny, nz, ng, nn, seed = geo
+    d = sg.generate_domain(nx, ny, nz, ng, nn, seed=seed, **gkw)
+    spec = sg.UdsSpec(nx=nx, ny=ny, nz=nz, **kw)
+    uds = spec.write(wd / f"{name}.uds")
+    r = oracle.run_ref("loop", uds, d, workdir=wd / name)
+    tr = r["trace"][1:]  # record 0 is the state before the first step
+    out = HERE / f"growth_{name}.npz"
+    np.savez_compressed(
+        out, uds=np.array(spec.text()), **domain_arrays(d),
+        t=tr["t"], dt=tr["dt"], Xcells=tr["Xcells"], Sv=tr["Sv"], n_full=tr["nfull"], Pmax=tr["Pmax"], rhomax=tr["rhomax"],
+        labels=narrow(r["labels"]),
+        rxg_counts=np.array([r["rxg"].get(i, 0) for i in range(d.nrxg)], dtype=np.uint32),
+        defg_counts=np.array([r["defg"].get(i, 0) for i in range(d.ndefg)], dtype=np.uint32))
+    print(f"{out.name}: {len(tr)} steps, X={tr['Xcells'][-1] / d.ncells:.4f}, {out.stat().st_size // 1024} KiB")
+    return out
+
+
+def make_ptab(wd: Path) -> Path:
+    nrxg, ndefg, seed = PTAB
+    d = sg.generate_domain(50, 50, 50, ndefg, nrxg, seed=seed)
+    out = {}
+    for model in (1, 2):
+        spec = sg.UdsSpec(nx=50, ny=50, nz=50, mobility_model=model)
+        uds = spec.write(wd / f"ptab{model}.uds")
+        r = oracle.run_ref("ptab", uds, d, workdir=wd / f"ptab{model}")
+        out[f"uds{model}"] = np.array(spec.text())
+        out[f"P{model}"] = r["ptab"]
+    path = HERE / "mobility_weights.npz"
+    np.savez_compressed(path, defg_quat=d.defg_quat, rxg_quat=d.rxg_quat, **out)
+    print(f"{path.name}: {nrxg}x{ndefg} pairs, {path.stat().st_size // 1024} KiB")
+    return path
+
+
+def main() -> None:
+    if not oracle.reference_available():
+        sys.exit("the reference sources are required to generate the golden fixtures")
+    oracle.build_ref()
+    with tempfile.TemporaryDirectory() as td:
+        wd = Path(td)
+        for name, (kw, geo, gkw) in CASES.items():
+            make_case(name, kw, geo, gkw, wd)
+        make_ptab(wd)
+
+
+if __name__ == "__main__":
+    main()

@@ -148,3 +148,19 @@ def test_fp32_kahan_error_is_small(gpu, tmp_uds):
     assert mismatch < 1e-3, mismatch
     assert dx < 5e-3, dx
     assert gs_err < 1e-3, gs_err
+
+
+# ---------------------------------------------------------------- against the reference's own outputs
+from _golden import TRACE_FIELDS, first_difference, growth_cases, load_case  # noqa: E402
+
+
+@pytest.mark.parametrize("name", growth_cases())
+def test_gpu_reproduces_reference_golden(gpu, tmp_path, name):
+    """The sm_103a path against the fixtures the reference's growth loop produced."""
+    p, d, g = load_case(name, tmp_path)
+    tr, lab, rc, dc = run_gpu(p, d)
+    for f in TRACE_FIELDS:
+        a = np.array([getattr(s, f) for s in tr])
+        assert np.array_equal(a, g[f]), f"{f}: {first_difference(a, g[f])}"
+    assert np.array_equal(lab.ravel(), g["labels"]), "final labels"
+    assert np.array_equal(rc, g["rxg_counts"]) and np.array_equal(dc, g["defg_counts"])
