@@ -54,9 +54,16 @@ __device__ __forceinline__ uint32_t lanemask_lt() {
 // Moore stencil in the order the reference issues infections
 // (updateFullRXInside, SCORE_Kernel.cpp:4611-4638): offsets, direction code
 // stored as the new cell's infector, and overshoot class (1 face, 2 edge, 3 corner).
-__constant__ int8_t c_dx[26] = {-1, 0, 1, -1, 1, -1, 0, 1, -1, 0, 1, -1, 0, 1, -1, 0, 1, -1, 0, 1, -1, 0, 1, -1, 0, 1};
-__constant__ int8_t c_dy[26] = {-1, -1, -1, 0, 0, 1, 1, 1, 1, 1, 1, -1, -1, -1, 0, 0, 0, -1, -1, -1, 0, 0, 0, 1, 1, 1};
-__constant__ int8_t c_dz[26] = {0, 0, 0, 0, 0, 0, 0, 0, -1, -1, -1, -1, -1, -1, -1, -1, -1, 1, 1, 1, 1, 1, 1, 1, 1, 1};
+#define SCORE_STENCIL_DX {-1, 0, 1, -1, 1, -1, 0, 1, -1, 0, 1, -1, 0, 1, -1, 0, 1, -1, 0, 1, -1, 0, 1, -1, 0, 1}
+#define SCORE_STENCIL_DY {-1, -1, -1, 0, 0, 1, 1, 1, 1, 1, 1, -1, -1, -1, 0, 0, 0, -1, -1, -1, 0, 0, 0, 1, 1, 1}
+#define SCORE_STENCIL_DZ {0, 0, 0, 0, 0, 0, 0, 0, -1, -1, -1, -1, -1, -1, -1, -1, -1, 1, 1, 1, 1, 1, 1, 1, 1, 1}
+__constant__ int8_t c_dx[26] = SCORE_STENCIL_DX;
+__constant__ int8_t c_dy[26] = SCORE_STENCIL_DY;
+__constant__ int8_t c_dz[26] = SCORE_STENCIL_DZ;
+// the same offsets for host code (linear neighbour offsets of interior cells)
+constexpr int8_t kStencilDx[26] = SCORE_STENCIL_DX;
+constexpr int8_t kStencilDy[26] = SCORE_STENCIL_DY;
+constexpr int8_t kStencilDz[26] = SCORE_STENCIL_DZ;
 __constant__ uint8_t c_code[26] = {16, 15, 14, 13, 12, 11, 10, 9, 19, 18, 17, 25, 24, 23, 22, 21, 20, 8, 7, 6, 5, 4, 3, 2, 1, 0};
 __constant__ uint8_t c_cls[26] = {2, 1, 2, 1, 1, 2, 1, 2, 3, 2, 3, 3, 2, 3, 2, 1, 2, 3, 2, 3, 2, 1, 2, 3, 2, 3};
 // velocity shape factor indexed by infector code (calcGrowthStepInside, SCORE_Kernel.cpp:4053-4055); 26 = nucleus

@@ -226,8 +226,9 @@ struct score_ctx {
 
     DomainArgs a{};
     DevState* d_state = nullptr;
-    DevState* d_snap = nullptr;        // per-step snapshot written by k_step_end
-    DevState* h_state = nullptr;       // pinned host copy of the snapshot
+    DevState* h_state = nullptr;       // pinned host copy of the device scalars (load checks)
+    HostBox* h_box = nullptr;          // pinned, device-mapped step mailbox
+    HostBox* d_box = nullptr;          // its device address
     double* d_pforce = nullptr;
     uint32_t* d_grid_init = nullptr;       // the loaded deformed grid (restart source)
     double* d_rxq = nullptr;               // orientation quaternions on the device
@@ -272,12 +273,12 @@ void score_ctx::release_domain() {
                     a.f[1].fill, a.f[1].comp, a.f[1].vel, a.f[1].defg, a.f[1].rxg, a.f[1].xyz, a.f[1].dir, a.f[1].full, a.f[1].recyc,
                     a.grid, a.claim, a.amask, a.ptab, a.defg_cnt, a.rxg_cnt, a.depleted, a.miss, a.pending, a.tobm, a.ctcnt,
                     a.f[0].fmask, a.f[0].imask, a.f[0].tcnt, a.f[1].fmask, a.f[1].imask, a.f[1].tcnt,
-                    d_state, d_snap, d_pforce, d_u32tmp, d_stage, d_grid_init, d_defg_cnt_init, d_rxq, d_dfq,
+                    d_state, d_pforce, d_u32tmp, d_stage, d_grid_init, d_defg_cnt_init, d_rxq, d_dfq,
                     scratch.fill, scratch.comp, scratch.vel, scratch.defg, scratch.rxg, scratch.xyz, scratch.dir};
     for (void* p : ptrs) if (p) cudaFree(p);
     a = DomainArgs{};
     scratch = DFront{};
-    d_state = nullptr; d_snap = nullptr; d_pforce = nullptr; d_u32tmp = nullptr; d_stage = nullptr;
+    d_state = nullptr; d_pforce = nullptr; d_u32tmp = nullptr; d_stage = nullptr;
     d_grid_init = nullptr; d_defg_cnt_init = nullptr; d_rxq = nullptr; d_dfq = nullptr;
     stage_cap = 0; scratch_cap = 0;
     loaded = false;
@@ -287,6 +288,8 @@ void score_ctx::release_stream() {
     if (device >= 0) cudaSetDevice(device);
     if (h_state) cudaFreeHost(h_state);
     h_state = nullptr;
+    if (h_box) cudaFreeHost(h_box);
+    h_box = nullptr; d_box = nullptr;
     for (auto& e : ev) if (e) { cudaEventDestroy(e); e = nullptr; }
     if (stream) cudaStreamDestroy(stream);
     stream = nullptr;
@@ -610,6 +613,8 @@ int score_create(score_ctx** out, const score_params* p, int device) {
     if (e == cudaSuccess) e = cudaDeviceGetAttribute(&c->sms, cudaDevAttrMultiProcessorCount, device);
     for (auto& ev : c->ev) if (e == cudaSuccess) e = cudaEventCreate(&ev);
     if (e == cudaSuccess) e = cudaMallocHost((void**)&c->h_state, sizeof(DevState));
+    if (e == cudaSuccess) e = cudaHostAlloc((void**)&c->h_box, sizeof(HostBox), cudaHostAllocMapped);
+    if (e == cudaSuccess) e = cudaHostGetDevicePointer((void**)&c->d_box, c->h_box, 0);
     if (e != cudaSuccess) { delete c; return SCORE_ERR_CUDA; }
     *out = c;
     return SCORE_OK;
@@ -649,6 +654,9 @@ int score_load_domain(score_ctx* c, const uint32_t* grid, const double* defg_qua
     if (!reuse) {
         a.nx = c->nx; a.ny = c->ny; a.nz = c->nz; a.nxy = c->nx * c->ny;
         a.dnx = make_fastdiv(c->nx); a.dnxy = make_fastdiv(c->nx * c->ny);
+        a.ncells = (uint32_t)N;
+        for (int d = 0; d < 26; ++d)
+            a.noff[d] = kStencilDx[d] + (int32_t)c->nx * kStencilDy[d] + (int32_t)(c->nx * c->ny) * kStencilDz[d];
         a.ndefg = ndefg; a.nrxg = nrxg;
         a.border_ref_cap = 2 * ((c->nx * c->ny) + (c->nx * c->nz) + (c->ny * c->nz));
         a.border_policy = p.border_policy; a.boundary = p.boundary; a.mobility_model = p.mobility_model;
@@ -693,7 +701,6 @@ int score_load_domain(score_ctx* c, const uint32_t* grid, const double* defg_qua
         if (e == cudaSuccess) e = dalloc(&a.miss, a.misscap);
         if (e == cudaSuccess) e = dalloc(&a.pending, a.pendcap);
         if (e == cudaSuccess) e = dalloc(&c->d_state, 1);
-        if (e == cudaSuccess) e = dalloc(&c->d_snap, 1);
         if (e == cudaSuccess) e = dalloc(&c->d_pforce, ndefg);
         if (e == cudaSuccess) e = dalloc(&c->d_u32tmp, 64);
         if (e == cudaSuccess) e = dalloc(&c->d_rxq, 4 * (size_t)nrxg);
@@ -789,15 +796,19 @@ int score_step(score_ctx* c, score_step_stats* out) {
     cudaEventRecord(c->ev[2], st);
     k_resolve<<<(uint32_t)c->sms * 4, kBlock, 0, st>>>(a);
     k_scan_tiles<1><<<1, 1024, 0, st>>>(a);
-    if (c->fp32) k_commit<true><<<(uint32_t)c->sms * 4, kBlock, 0, st>>>(a);
-    else k_commit<false><<<(uint32_t)c->sms * 4, kBlock, 0, st>>>(a);
-    k_step_end<<<1, 1, 0, st>>>(a, c->d_snap);
+    if (c->fp32) {
+        k_commit<true><<<(uint32_t)c->sms * 4, kBlock, 0, st>>>(a);
+        k_new_vel<true><<<(uint32_t)c->sms * 8, kBlock, 0, st>>>(a);
+    } else {
+        k_commit<false><<<(uint32_t)c->sms * 4, kBlock, 0, st>>>(a);
+        k_new_vel<false><<<(uint32_t)c->sms * 8, kBlock, 0, st>>>(a);
+    }
+    k_step_end<<<1, kBlock, 0, st>>>(a, c->d_box);
     cudaEventRecord(c->ev[3], st);
-    c->launches += 9;
-    cudaError_t e = cudaMemcpyAsync(c->h_state, c->d_snap, sizeof(DevState), cudaMemcpyDeviceToHost, st);
-    if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+    c->launches += 10;
+    cudaError_t e = cudaStreamSynchronize(st);  // the one wait of the step: k_step_end filled the mailbox
     if (e != cudaSuccess) { c->failed = true; return c->cuda_fail(e, "growth step"); }
-    const DevState hs = *c->h_state;
+    const DevState hs = c->h_box->snap;
     if (hs.err) { c->failed = true; return check_device_errors(c, hs.err); }
     float ms_grow = 0, ms_claim = 0, ms_commit = 0, ms_fill = 0;
     cudaEventElapsedTime(&ms_fill, c->ev[0], c->ev[6]);
@@ -808,7 +819,7 @@ int score_step(score_ctx* c, score_step_stats* out) {
     c->tm.grow_ms += ms_grow; c->tm.claim_ms += ms_claim; c->tm.commit_ms += ms_commit;
     c->tm.total_ms += ms_grow + ms_claim + ms_commit;
     c->tm.grow_launches += 2;  // fill-update launches (the grow_bytes kernels)
-    c->tm.kernel_launches += 9;
+    c->tm.kernel_launches += 10;
     // algorithmic bytes: grow 25 B (FP64: dir 1, vel 8, fill 8 r + 8 w) or 17 B (FP32: dir, vel 4, fill 4 + comp 4 r/w)
     const double bpu = c->fp32 ? 17.0 : 25.0;
     const uint64_t Sv = hs.sv[0] + hs.sv[1], nfull = (uint64_t)hs.nfull[0] + hs.nfull[1], nnew = (uint64_t)hs.nwin[0] + hs.nwin[1];
@@ -821,18 +832,35 @@ int score_step(score_ctx* c, score_step_stats* out) {
     if (hs.nmiss > 0 || hs.npending > 0) {
         std::vector<unsigned long long> idx(hs.nmiss);
         std::vector<double> val;
-        e = cudaMemcpyAsync(idx.data(), a.miss, (size_t)hs.nmiss * 8, cudaMemcpyDeviceToHost, st);
-        if (e == cudaSuccess) e = cudaStreamSynchronize(st);
-        if (e != cudaSuccess) return c->cuda_fail(e, "read misses");
+        if (hs.nmiss <= kBoxMiss) {
+            memcpy(idx.data(), c->h_box->miss, (size_t)hs.nmiss * 8);
+        } else {
+            e = cudaMemcpyAsync(idx.data(), a.miss, (size_t)hs.nmiss * 8, cudaMemcpyDeviceToHost, st);
+            if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+            if (e != cudaSuccess) return c->cuda_fail(e, "read misses");
+        }
         resolve_weights(c, idx, val);
         for (double v : val) if (v > pmax_new) pmax_new = v;
         if (hs.nmiss > 0) {
-            if (!c->stage((size_t)hs.nmiss * 16)) return c->fail(SCORE_ERR_NOMEM, "staging buffer");
-            unsigned long long* d_i = (unsigned long long*)c->d_stage;
-            double* d_v = (double*)(d_i + hs.nmiss);
-            e = cudaMemcpyAsync(d_i, idx.data(), (size_t)hs.nmiss * 8, cudaMemcpyHostToDevice, st);
-            if (e == cudaSuccess) e = cudaMemcpyAsync(d_v, val.data(), (size_t)hs.nmiss * 8, cudaMemcpyHostToDevice, st);
-            if (e != cudaSuccess) return c->cuda_fail(e, "upload weights");
+            const unsigned long long* d_i;
+            const double* d_v;
+            if (hs.nmiss <= kBoxMiss) {
+                // the previous step's k_fill_ptab finished before this step's k_step_end
+                memcpy(c->h_box->ans_idx, idx.data(), (size_t)hs.nmiss * 8);
+                memcpy(c->h_box->ans_val, val.data(), (size_t)hs.nmiss * 8);
+                d_i = c->d_box->ans_idx;
+                d_v = c->d_box->ans_val;
+            } else {
+                if (!c->stage((size_t)hs.nmiss * 16)) return c->fail(SCORE_ERR_NOMEM, "staging buffer");
+                unsigned long long* si = (unsigned long long*)c->d_stage;
+                double* sv = (double*)(si + hs.nmiss);
+                e = cudaMemcpyAsync(si, idx.data(), (size_t)hs.nmiss * 8, cudaMemcpyHostToDevice, st);
+                if (e == cudaSuccess) e = cudaMemcpyAsync(sv, val.data(), (size_t)hs.nmiss * 8, cudaMemcpyHostToDevice, st);
+                if (e == cudaSuccess) e = cudaStreamSynchronize(st);  // pageable sources go out of scope
+                if (e != cudaSuccess) return c->cuda_fail(e, "upload weights");
+                d_i = si;
+                d_v = sv;
+            }
             k_fill_ptab<<<blocks_for(hs.nmiss, c->sms), kBlock, 0, st>>>(a.ptab, d_i, d_v, hs.nmiss);
             c->launches++;
         }
@@ -840,16 +868,19 @@ int score_step(score_ctx* c, score_step_stats* out) {
         if (c->fp32) k_fix_pending<true><<<blocks_for(np, c->sms), kBlock, 0, st>>>(a, np);
         else k_fix_pending<false><<<blocks_for(np, c->sms), kBlock, 0, st>>>(a, np);
         c->launches++;
-        e = cudaStreamSynchronize(st);
-        if (e != cudaSuccess) return c->cuda_fail(e, "fix pending weights");
     }
     // deformed grains that ran out of cells this step (synchronize_mydefpool_counts)
     if (hs.ndepleted > 0) {
-        std::vector<uint32_t> dep(hs.ndepleted);
-        e = cudaMemcpyAsync(dep.data(), a.depleted, (size_t)hs.ndepleted * 4, cudaMemcpyDeviceToHost, st);
-        if (e == cudaSuccess) e = cudaStreamSynchronize(st);
-        if (e != cudaSuccess) return c->cuda_fail(e, "read depleted grains");
-        for (uint32_t g : dep) c->defg_cnt_host[g] = 0;
+        const uint32_t nd = std::min(hs.ndepleted, c->ndefg);
+        if (nd <= kBoxDep) {
+            for (uint32_t i = 0; i < nd; ++i) c->defg_cnt_host[c->h_box->depleted[i]] = 0;
+        } else {
+            std::vector<uint32_t> dep(nd);
+            e = cudaMemcpyAsync(dep.data(), a.depleted, (size_t)nd * 4, cudaMemcpyDeviceToHost, st);
+            if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+            if (e != cudaSuccess) return c->cuda_fail(e, "read depleted grains");
+            for (uint32_t g : dep) c->defg_cnt_host[g] = 0;
+        }
         c->rhomax_version = ~0ull;  // the set of grains with cells left changed
     }
     for (int L = 0; L < 2; ++L) {

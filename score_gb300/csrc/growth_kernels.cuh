@@ -30,6 +30,7 @@
 //             omp_getNextFreeSlotInRXFront*(CELLRECYCLE).  The full cell then becomes
 //             recrystallized (grid = ndefg + rxg, counts, slot INACTIVE) — the tail of
 //             updateFullRX{Inside,Border}, SCORE_Kernel.cpp:4559-4774.
+//   k_new_vel one thread per new cell: mobility weight P and cached velocity factor.
 //   k_step_end  slot high-water marks, stats snapshot, reset of the per-step fields.
 #pragma once
 #include <cstdint>
@@ -91,6 +92,8 @@ struct DomainArgs {
     uint32_t* pending;          // (list << 31) | slot of new cells waiting for P
     uint32_t misscap, pendcap;
     uint32_t nx, ny, nz, nxy;
+    uint32_t ncells;
+    int32_t noff[26];           // linear offset of neighbour d of an interior cell
     FastDiv dnx, dnxy;
     uint32_t ndefg, nrxg;
     uint32_t border_ref_cap;
@@ -413,32 +416,56 @@ __global__ void __launch_bounds__(kBlock) k_grow_lists(DomainArgs a) {
 }
 
 // ------------------------------------------------------------------ K2 claim
-__global__ void __launch_bounds__(kBlock) k_claim(DomainArgs a) {
+// Attempts LO..HI-1 of one full cell: the grid loads are all issued before the atomics
+// (claims are a min, so the order of the atomics does not matter).  Inside cells are
+// strictly interior (every list insertion checks it), so their targets are the cell
+// index plus a fixed offset; Border cells wrap through target_of.
+template <int LO, int HI, bool INSIDE>
+__device__ __forceinline__ uint32_t claim_plane(const DomainArgs& a, uint32_t cell, int x, int y, int z, uint32_t f) {
+    uint32_t tg[HI - LO], gv[HI - LO];
+#pragma unroll
+    for (int k = 0; k < HI - LO; ++k) {
+        gv[k] = 0xFFFFFFFFu;
+        if (INSIDE) {
+            tg[k] = cell + (uint32_t)a.noff[LO + k];
+            if (tg[k] < a.ncells) gv[k] = a.grid[tg[k]];
+            else atomicOr(&a.st->err, kErrBounds);
+        } else {
+            bool inter;
+            if (target_of(a, 1, x, y, z, LO + k, tg[k], inter)) gv[k] = a.grid[tg[k]];
+        }
+    }
+    uint32_t mask = 0;
+#pragma unroll
+    for (int k = 0; k < HI - LO; ++k) {
+        if (gv[k] < a.ndefg) {
+            atomicMin(&a.claim[tg[k]], f * 26u + (uint32_t)(LO + k));
+            mask |= 1u << (LO + k);
+        }
+    }
+    return mask;
+}
+
+__global__ void __launch_bounds__(kBlock, 4) k_claim(DomainArgs a) {
     const uint32_t F0 = a.st->nfull[0], F = F0 + a.st->nfull[1];
     if (26ull * F >= 0xFFFFFFFFull) {
         if (blockIdx.x == 0 && threadIdx.x == 0) atomicOr(&a.st->err, kErrKeyLimit);
         return;
     }
     for (uint32_t f = blockIdx.x * blockDim.x + threadIdx.x; f < F; f += gridDim.x * blockDim.x) {
-        const int L = f >= F0 ? 1 : 0;
-        const uint32_t slot = a.f[L].full[L ? f - F0 : f];
-        int x, y, z;
-        decode(a, a.f[L].xyz[slot], x, y, z);
-        uint32_t tg[26], gv[26];
-        // every neighbour load is issued before the first atomic
-#pragma unroll
-        for (int d = 0; d < 26; ++d) {
-            bool inter;
-            gv[d] = 0xFFFFFFFFu;
-            if (target_of(a, L, x, y, z, d, tg[d], inter)) gv[d] = __ldg(&a.grid[tg[d]]);
-        }
-        uint32_t mask = 0;
-#pragma unroll
-        for (int d = 0; d < 26; ++d) {
-            if (gv[d] < a.ndefg) {
-                atomicMin(&a.claim[tg[d]], f * 26u + (uint32_t)d);
-                mask |= 1u << d;
-            }
+        uint32_t mask;
+        if (f < F0) {
+            const uint32_t cell = a.f[0].xyz[a.f[0].full[f]];
+            mask = claim_plane<0, 8, true>(a, cell, 0, 0, 0, f);
+            mask |= claim_plane<8, 17, true>(a, cell, 0, 0, 0, f);
+            mask |= claim_plane<17, 26, true>(a, cell, 0, 0, 0, f);
+        } else {
+            const uint32_t cell = a.f[1].xyz[a.f[1].full[f - F0]];
+            int x, y, z;
+            decode(a, cell, x, y, z);
+            mask = claim_plane<0, 8, false>(a, cell, x, y, z, f);
+            mask |= claim_plane<8, 17, false>(a, cell, x, y, z, f);
+            mask |= claim_plane<17, 26, false>(a, cell, x, y, z, f);
         }
         a.amask[f] = mask;
     }
@@ -560,7 +587,7 @@ __device__ __forceinline__ bool lookup_p(const DomainArgs& a, uint32_t rxg, uint
 // full-cell then direction order and take recycled slots first, then appended slots,
 // like omp_getNextFreeSlotInRXFront*(CELLRECYCLE); the full cell then becomes
 // recrystallized (grid = ndefg + rxg, counts, slot INACTIVE).
-__global__ void __launch_bounds__(kBlock, 2) k_resolve(DomainArgs a) {
+__global__ void __launch_bounds__(kBlock, 4) k_resolve(DomainArgs a) {
     const uint32_t F0 = a.st->nfull[0], F = F0 + a.st->nfull[1];
     if (26ull * F >= 0xFFFFFFFFull) return;
     const uint32_t ntiles = (F + kBlock - 1) / kBlock;
@@ -620,7 +647,7 @@ __global__ void __launch_bounds__(kBlock, 2) k_resolve(DomainArgs a) {
 }
 
 template <bool FP32>
-__global__ void __launch_bounds__(kBlock, 2) k_commit(DomainArgs a) {
+__global__ void __launch_bounds__(kBlock, 4) k_commit(DomainArgs a) {
     const uint32_t F0 = a.st->nfull[0], F = F0 + a.st->nfull[1];
     if (26ull * F >= 0xFFFFFFFFull) return;
     const uint32_t ntiles = (F + kBlock - 1) / kBlock;
@@ -671,31 +698,20 @@ __global__ void __launch_bounds__(kBlock, 2) k_commit(DomainArgs a) {
                     if (D == 1 && a.border_policy == 0 && r >= nrec && ns >= a.border_ref_cap) atomicOr(&a.st->err, kErrBorderRef);
                     const uint32_t gt = a.grid[t];
                     const int cls = c_cls[d];
-                    double P = 0.0;
-                    const bool known = lookup_p(a, rsrc, gt, P);
                     if (!FP32) {
                         const double fac = cls == 1 ? 0.0682 : (cls == 2 ? 0.0542 : 0.0484);
                         ((double*)dst.fill)[ns] = __dmul_rn(over, fac);
-                        ((double*)dst.vel)[ns] = known ? velocity_factor(a, P, gt, c_code[d]) : -1.0;
                     } else {
                         const float fac = cls == 1 ? 0.0682f : (cls == 2 ? 0.0542f : 0.0484f);
                         ((float*)dst.fill)[ns] = over32 * fac;
                         dst.comp[ns] = 0.0f;
-                        ((float*)dst.vel)[ns] = known ? (float)velocity_factor(a, P, gt, c_code[d]) : -1.0f;
                     }
-                    dst.dir[ns] = c_code[d] | kStale;
+                    dst.dir[ns] = c_code[d] | kStale;  // vel follows in k_new_vel
                     dst.defg[ns] = gt;
                     dst.rxg[ns] = rsrc;
                     dst.xyz[ns] = t;
                     a.grid[t] = 4096002000u;  // CURRENTLY_INFECTED
                     a.claim[t] = kClaimFree;
-                    if (!known) {
-                        const uint32_t q = atomicAdd(&a.st->npending, 1u);
-                        if (q < a.pendcap) a.pending[q] = ((uint32_t)D << 31) | ns;
-                        else atomicOr(&a.st->err, kErrMissCap);
-                    } else if (P > 0.0) {
-                        atomicMax(&a.st->pmax_bits, (unsigned long long)__double_as_longlong(P));
-                    }
                 }
             }
             // the full cell is now recrystallized
@@ -714,19 +730,74 @@ __global__ void __launch_bounds__(kBlock, 2) k_commit(DomainArgs a) {
     }
 }
 
-// ------------------------------------------------------------------ K4 step end
-// Advances the high-water marks, snapshots the per-step fields for the host and
-// clears them for the next step.
-__global__ void k_step_end(DomainArgs a, DevState* snapshot) {
-    DevState* st = a.st;
-    const uint32_t cap[2] = {a.f[0].cap, a.f[1].cap};
-    for (int D = 0; D < 2; ++D) {
-        if (st->nwin[D] > st->nrec[D]) st->next_never[D] += st->nwin[D] - st->nrec[D];
-        if (st->next_never[D] > cap[D]) { st->next_never[D] = cap[D]; st->err |= kErrCapacity; }
+// k_new_vel: one thread per cell infected this step (both lists, in rank order):
+// P(rxg, defg) from the table (classified on the device when exact, else requested
+// from the host: vel = -1 and the slot goes on the pending list) and the cached
+// velocity factor; the running P max over the new weights.
+template <bool FP32>
+__global__ void __launch_bounds__(kBlock) k_new_vel(DomainArgs a) {
+    const uint32_t n0 = a.st->nwin[0], n = n0 + a.st->nwin[1];
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        const int D = i >= n0 ? 1 : 0;
+        const uint32_t r = D ? i - n0 : i;
+        const DFront& dst = a.f[D];
+        const uint32_t nrec = a.st->nrec[D];
+        const uint32_t ns = r < nrec ? dst.recyc[r] : a.st->next_never[D] + (r - nrec);
+        if (ns >= dst.cap) continue;  // k_commit flagged the overflow
+        const uint32_t gt = dst.defg[ns];
+        const int code = dst.dir[ns] & kCodeMask;
+        double P = 0.0;
+        const bool known = lookup_p(a, dst.rxg[ns], gt, P);
+        if (!FP32) ((double*)dst.vel)[ns] = known ? velocity_factor(a, P, gt, code) : -1.0;
+        else ((float*)dst.vel)[ns] = known ? (float)velocity_factor(a, P, gt, code) : -1.0f;
+        if (!known) {
+            const uint32_t q = atomicAdd(&a.st->npending, 1u);
+            if (q < a.pendcap) a.pending[q] = ((uint32_t)D << 31) | ns;
+            else atomicOr(&a.st->err, kErrMissCap);
+        } else if (P > 0.0) {
+            atomicMax(&a.st->pmax_bits, (unsigned long long)__double_as_longlong(P));
+        }
     }
-    *snapshot = *st;
-    char* p = (char*)st + kStepFieldsOffset;
-    for (size_t i = 0; i < sizeof(DevState) - kStepFieldsOffset; ++i) p[i] = 0;
+}
+
+// ------------------------------------------------------------------ K4 step end
+// Host mailbox in pinned, device-mapped memory: k_step_end writes the step's scalars,
+// the mobility-weight requests and the depleted grains straight into host memory, so
+// the host needs one stream synchronization per step and no copies; the host writes
+// the requested weights back into ans_* for k_fill_ptab.
+constexpr uint32_t kBoxMiss = 65536;
+constexpr uint32_t kBoxDep = 65536;
+struct HostBox {
+    DevState snap;
+    unsigned long long miss[kBoxMiss];
+    uint32_t depleted[kBoxDep];
+    unsigned long long ans_idx[kBoxMiss];
+    double ans_val[kBoxMiss];
+};
+
+// Advances the high-water marks, posts the step to the mailbox and clears the
+// per-step fields for the next step.  One block.
+__global__ void __launch_bounds__(kBlock) k_step_end(DomainArgs a, HostBox* box) {
+    DevState* st = a.st;
+    __shared__ uint32_t s_nm, s_nd;
+    if (threadIdx.x == 0) {
+        const uint32_t cap[2] = {a.f[0].cap, a.f[1].cap};
+        for (int D = 0; D < 2; ++D) {
+            if (st->nwin[D] > st->nrec[D]) st->next_never[D] += st->nwin[D] - st->nrec[D];
+            if (st->next_never[D] > cap[D]) { st->next_never[D] = cap[D]; st->err |= kErrCapacity; }
+        }
+        box->snap = *st;
+        s_nm = min(min(st->nmiss, a.misscap), kBoxMiss);
+        s_nd = min(min(st->ndepleted, a.ndefg), kBoxDep);
+    }
+    __syncthreads();
+    for (uint32_t i = threadIdx.x; i < s_nm; i += blockDim.x) box->miss[i] = a.miss[i];
+    for (uint32_t i = threadIdx.x; i < s_nd; i += blockDim.x) box->depleted[i] = a.depleted[i];
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        char* p = (char*)st + kStepFieldsOffset;
+        for (size_t i = 0; i < sizeof(DevState) - kStepFieldsOffset; ++i) p[i] = 0;
+    }
 }
 
 }  // namespace score
