@@ -261,7 +261,8 @@ def main():
     barrier(dist)
     launches0 = gm.timing().kernel_launches
     tot_sv, tot_steps, run_ms, grow_bytes, grow_launches = 0, 0, 0.0, 0.0, 0
-    phase = {"grow_ms": 0.0, "fill_ms": 0.0, "claim_ms": 0.0, "commit_ms": 0.0, "host_ms": 0.0}
+    phase = {"grow_ms": 0.0, "fill_ms": 0.0, "claim_ms": 0.0, "commit_ms": 0.0, "host_ms": 0.0, "wait_ms": 0.0,
+             "weights_ms": 0.0}
     with ClockSampler(local) as clk:
         for _ in range(args.steps):
             sv, ns, tm = one_run()

@@ -197,8 +197,64 @@ typedef struct score_timing {
     uint64_t kernel_launches;  /* kernels launched by this context since creation */
     double run_ms;          /* device span of the last restart .. score_run_until */
     double fill_ms;         /* the fill-update kernels alone (part of grow_ms) */
+    double wait_ms;         /* host time blocked on the step's stream synchronization */
+    double weights_ms;      /* host time computing requested mobility weights (libm FP64) */
 } score_timing;
 int  score_get_timing(score_ctx* ctx, score_timing* out);
+
+/*
+ * Launch configuration of the step kernels.  Results do not depend on it (every
+ * compaction keeps slot order, every claim is decided by its ordinal); only speed does.
+ */
+typedef struct score_tune {
+    int32_t items;                 /* grow tile = 256 * items front slots: 4, 8 or 16 */
+    int32_t fill_blocks_per_sm;    /* k_grow_fill grid = SMs * this */
+    int32_t claim_blocks_per_sm;   /* k_claim grid */
+    int32_t commit_blocks_per_sm;  /* k_resolve / k_commit grid */
+    int32_t use_graph;             /* 1: each step replays one captured CUDA graph */
+    uint32_t steps;                /* autotuner: steps it ran */
+    double fill_ns_per_slot;       /* autotuner: best grow time per front slot [ns] */
+    double claim_ns_per_cell;      /* autotuner: best claim time per full cell [ns] */
+    double commit_ns_per_cell;     /* autotuner: best resolve+commit time per full cell [ns] */
+} score_tune;
+int  score_get_tune(score_ctx* ctx, score_tune* out);
+int  score_set_tune(score_ctx* ctx, const score_tune* t);
+/* Restart, place nuclei, run up to max_steps steps (0: to x_target, < 0: XMAX) cycling
+ * candidate configurations, keep the fastest per kernel group, then restart and place
+ * the nuclei again: the context is ready for score_run_until. */
+int  score_autotune(score_ctx* ctx, double x_target, uint32_t max_steps, score_tune* out);
+
+/*
+ * Batched ensemble: many independent domains (own sizes, grains, nuclei, parameters;
+ * one precision) stepped together.  Each step is one sequence of kernels over all
+ * running domains, replayed as one CUDA graph; a domain that meets its stop rule
+ * leaves the launches.  Mirrors the reference's ensemble of solitary units that its
+ * ranks step one after another (SCORE_Kernel.cpp:1640-1756).  Domain d of a batch
+ * accepts the single-domain functions' arguments.  The domains of all live contexts
+ * and batches of one device share 64 argument slots: a batch holds at most 64 domains,
+ * and score_create / score_batch_create return SCORE_ERR_CAPACITY when the device's
+ * slots are taken.
+ */
+typedef struct score_batch score_batch;
+int  score_batch_create(score_batch** out, const score_params* params, uint32_t ndomains, int device);
+void score_batch_destroy(score_batch* b);
+const char* score_batch_last_error(const score_batch* b);
+int  score_batch_load_domain(score_batch* b, uint32_t d, const uint32_t* grid, const double* defg_quat,
+                             const double* defg_rho0, uint32_t ndefg, const double* rxg_quat,
+                             const uint32_t* rxg_site, const double* rxg_tincub, uint32_t nrxg, const double* ptable);
+int  score_batch_restart(score_batch* b);
+int  score_batch_place_nuclei(score_batch* b);
+/* step all domains until each meets its stop rule (x_target < 0: its XMAX) or max_steps (0: no limit) */
+int  score_batch_run_until(score_batch* b, double x_target, uint32_t max_steps, uint32_t* steps_done);
+int  score_batch_get_stats(score_batch* b, uint32_t d, score_step_stats* out);
+/* per-step stats of domain d in the last score_batch_run_until */
+int  score_batch_trace(score_batch* b, uint32_t d, score_step_stats* trace, uint32_t cap, uint32_t* n_steps);
+int  score_batch_export_labels(score_batch* b, uint32_t d, uint32_t* labels);
+int  score_batch_grain_counts(score_batch* b, uint32_t d, uint32_t* rxg_counts, uint32_t* defg_counts);
+int  score_batch_get_timing(score_batch* b, score_timing* out);
+int  score_batch_get_tune(score_batch* b, score_tune* out);
+int  score_batch_set_tune(score_batch* b, const score_tune* t);
+int  score_batch_autotune(score_batch* b, double x_target, uint32_t max_steps, score_tune* out);
 
 /* FP64 mobility weight P(rxg,defg) on the host, the reference's formula
  * (SCORE_Kernel.cpp:2460-2527, SCORE_Math.cpp:558-622,1067-1130) */

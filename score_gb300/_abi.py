@@ -72,7 +72,15 @@ class Timing(C.Structure):
     _fields_ = [
         ("total_ms", _d), ("grow_ms", _d), ("claim_ms", _d), ("commit_ms", _d), ("host_ms", _d),
         ("grow_launches", C.c_uint64), ("grow_bytes", _d), ("step_bytes", _d), ("kernel_launches", C.c_uint64),
-        ("run_ms", _d), ("fill_ms", _d),
+        ("run_ms", _d), ("fill_ms", _d), ("wait_ms", _d), ("weights_ms", _d),
+    ]
+
+
+class Tune(C.Structure):
+    _fields_ = [
+        ("items", _i32), ("fill_blocks_per_sm", _i32), ("claim_blocks_per_sm", _i32), ("commit_blocks_per_sm", _i32),
+        ("use_graph", _i32), ("steps", _u32), ("fill_ns_per_slot", _d), ("claim_ns_per_cell", _d),
+        ("commit_ns_per_cell", _d),
     ]
 
 
@@ -106,6 +114,24 @@ SIGNATURES = {
     "score_export_labels": (C.c_int, [_vp, _vp]),
     "score_grain_counts": (C.c_int, [_vp, _vp, _vp]),
     "score_get_timing": (C.c_int, [_vp, _P(Timing)]),
+    "score_get_tune": (C.c_int, [_vp, _P(Tune)]),
+    "score_set_tune": (C.c_int, [_vp, _P(Tune)]),
+    "score_autotune": (C.c_int, [_vp, _d, _u32, _P(Tune)]),
+    "score_batch_create": (C.c_int, [_P(_vp), _P(Params), _u32, C.c_int]),
+    "score_batch_destroy": (None, [_vp]),
+    "score_batch_last_error": (C.c_char_p, [_vp]),
+    "score_batch_load_domain": (C.c_int, [_vp, _u32, _vp, _vp, _vp, _u32, _vp, _vp, _vp, _u32, _vp]),
+    "score_batch_restart": (C.c_int, [_vp]),
+    "score_batch_place_nuclei": (C.c_int, [_vp]),
+    "score_batch_run_until": (C.c_int, [_vp, _d, _u32, _P(_u32)]),
+    "score_batch_get_stats": (C.c_int, [_vp, _u32, _P(StepStats)]),
+    "score_batch_trace": (C.c_int, [_vp, _u32, _P(StepStats), _u32, _P(_u32)]),
+    "score_batch_export_labels": (C.c_int, [_vp, _u32, _vp]),
+    "score_batch_grain_counts": (C.c_int, [_vp, _u32, _vp, _vp]),
+    "score_batch_get_timing": (C.c_int, [_vp, _P(Timing)]),
+    "score_batch_get_tune": (C.c_int, [_vp, _P(Tune)]),
+    "score_batch_set_tune": (C.c_int, [_vp, _P(Tune)]),
+    "score_batch_autotune": (C.c_int, [_vp, _d, _u32, _P(Tune)]),
     "score_mobility_weight": (C.c_int, [_P(Params), _vp, _vp, _P(_d)]),
     "score_mobility_table_noalloc": (C.c_int, [_P(Params), _vp, _u32, _vp, _u32, _vp, _vp, _vp]),
     "score_gen_default": (C.c_int, [_P(GenParams)]),

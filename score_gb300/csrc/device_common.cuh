@@ -29,7 +29,8 @@ struct DevState {
     uint32_t next_never[2];     // slots ever used per list (Inside, Border)
     uint32_t err;               // sticky error flags
     uint32_t err_info;
-    uint32_t reserved[4];
+    uint32_t npend_prev;        // pending cells of the last step (fixed at the start of the next)
+    uint32_t reserved[3];
     // ---- per step ----
     uint32_t nfull[2];          // FullRX list lengths
     uint32_t ninactive[2];      // INACTIVE slots seen by the scan (uncapped)

@@ -79,20 +79,6 @@ __global__ void k_fill_ptab(unsigned long long* ptab, const unsigned long long* 
 
 // new cells whose P arrived from the host: their velocity factor
 template <bool FP32>
-__global__ void k_fix_pending(DomainArgs a, uint32_t n) {
-    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
-        const uint32_t q = a.pending[i];
-        const DFront& f = a.f[q >> 31];
-        const uint32_t s = q & 0x7FFFFFFFu;
-        const uint32_t g = f.defg[s];
-        const double P = __longlong_as_double((long long)a.ptab[(unsigned long long)f.rxg[s] * a.ndefg + g]);
-        const double v = velocity_factor(a, P, g, f.dir[s] & kCodeMask);
-        if (!FP32) ((double*)f.vel)[s] = v;
-        else ((float*)f.vel)[s] = (float)v;
-    }
-}
-
-template <bool FP32>
 __global__ void k_labels_front(DomainArgs a, int L, uint32_t n, uint32_t* lab) {
     const DFront& f = a.f[L];
     for (uint32_t s = blockIdx.x * blockDim.x + threadIdx.x; s < n; s += gridDim.x * blockDim.x) {
@@ -199,6 +185,8 @@ cudaError_t dalloc(T** p, size_t count) {
 }  // namespace
 
 // ------------------------------------------------------------------ context
+struct Engine;
+
 struct score_ctx {
     score_params prm{};
     int device = 0;
@@ -239,15 +227,18 @@ struct score_ctx {
     size_t stage_cap = 0;
     DFront scratch{};
     uint32_t scratch_cap = 0;
+    size_t scnt_words[2] = {0, 0}, csct_words = 0;  // supertile counter arrays (zeroed on reset)
 
     double Xcells = 0.0;
     uint32_t step = 0, defrag_cnt = 0, n_nuclei = 0;
     uint32_t next_never[2] = {0, 0}, high_water[2] = {0, 0};
     score_step_stats last{};
 
-    cudaEvent_t ev[7] = {nullptr, nullptr, nullptr, nullptr, nullptr, nullptr, nullptr};  // 0-3 step phases, 4-5 run span, 6 end of fill
-    score_timing tm{};
-    uint64_t launches = 0;
+    Engine* eng = nullptr;             // launches this domain's steps (its own, or a batch's)
+    bool own_eng = false;
+    bool running = false;              // steps in the next batched step
+    uint64_t launches = 0;             // kernels launched outside the step sequence
+    std::vector<score_step_stats> trace;  // per-step stats of the last batched run
 
     ~score_ctx() { release_domain(); release_stream(); }
     void release_domain();
@@ -273,6 +264,7 @@ void score_ctx::release_domain() {
                     a.f[1].fill, a.f[1].comp, a.f[1].vel, a.f[1].defg, a.f[1].rxg, a.f[1].xyz, a.f[1].dir, a.f[1].full, a.f[1].recyc,
                     a.grid, a.claim, a.amask, a.ptab, a.defg_cnt, a.rxg_cnt, a.depleted, a.miss, a.pending, a.tobm, a.ctcnt,
                     a.f[0].fmask, a.f[0].imask, a.f[0].tcnt, a.f[1].fmask, a.f[1].imask, a.f[1].tcnt,
+                    a.f[0].scnt, a.f[1].scnt, a.csct,
                     d_state, d_pforce, d_u32tmp, d_stage, d_grid_init, d_defg_cnt_init, d_rxq, d_dfq,
                     scratch.fill, scratch.comp, scratch.vel, scratch.defg, scratch.rxg, scratch.xyz, scratch.dir};
     for (void* p : ptrs) if (p) cudaFree(p);
@@ -290,10 +282,116 @@ void score_ctx::release_stream() {
     h_state = nullptr;
     if (h_box) cudaFreeHost(h_box);
     h_box = nullptr; d_box = nullptr;
-    for (auto& e : ev) if (e) { cudaEventDestroy(e); e = nullptr; }
-    if (stream) cudaStreamDestroy(stream);
-    stream = nullptr;
+    if (own_eng) delete eng;
+    eng = nullptr;
+    stream = nullptr;  // owned by the engine
 }
+
+// ------------------------------------------------------------------ step engine
+// Launches one growth step of every running domain of a set (one domain, or a batch of
+// independent domains) as one sequence of kernels over all of them, on one stream:
+// the per-domain argument blocks go to the device in one copy, the sequence runs as
+// a CUDA graph (captured once per domain count and tile configuration) or as direct
+// launches, and the step ends with one stream synchronization.
+struct TuneCfg {
+    int items = 8;          // grow tile = kBlock * items slots
+    int fill_bpsm = 16;     // k_grow_fill blocks per SM
+    int claim_bpsm = 4;     // k_claim blocks per SM
+    int commit_bpsm = 4;    // k_resolve / k_commit blocks per SM
+    bool operator==(const TuneCfg& o) const {
+        return items == o.items && fill_bpsm == o.fill_bpsm && claim_bpsm == o.claim_bpsm && commit_bpsm == o.commit_bpsm;
+    }
+};
+
+// Slots of the constant-memory argument array c_args, per device: each engine holds a
+// contiguous range for as long as it lives.
+std::mutex g_slot_mu;
+uint64_t g_slots_used[64] = {};
+
+int alloc_slots(int device, int n, int* base) {
+    if (device < 0 || device >= 64 || n < 1 || n > kMaxDomains) return SCORE_ERR_ARG;
+    std::lock_guard<std::mutex> lock(g_slot_mu);
+    for (int b = 0; b + n <= kMaxDomains; ++b) {
+        const uint64_t m = (n == 64 ? ~0ull : ((1ull << n) - 1)) << b;
+        if (!(g_slots_used[device] & m)) {
+            g_slots_used[device] |= m;
+            *base = b;
+            return SCORE_OK;
+        }
+    }
+    return SCORE_ERR_CAPACITY;
+}
+
+void free_slots(int device, int base, int n) {
+    if (base < 0 || n < 1) return;
+    std::lock_guard<std::mutex> lock(g_slot_mu);
+    g_slots_used[device] &= ~((n == 64 ? ~0ull : ((1ull << n) - 1)) << base);
+}
+
+struct Engine {
+    int device = 0, sms = 1;
+    cudaStream_t stream = nullptr;
+    bool fp32 = false;
+    std::vector<score_ctx*> dom;
+    int base = -1, nslots = 0;         // this engine's slots of c_args
+    DomainArgs* d_args = nullptr;      // device address of c_args[base]
+    DomainArgs* h_args = nullptr;      // pinned staging of the argument blocks
+    TuneCfg cfg;
+    bool use_graph = true;
+    bool capturing = false;
+    cudaGraphExec_t gexec = nullptr;
+    TuneCfg gcfg;
+    int gndom = -1;
+    bool gfp32 = false;
+    // 0 start, 1 end of fill, 2 end of lists, 3 end of claim, 4 end of step, 5/6 run span
+    cudaEvent_t ev[7] = {nullptr, nullptr, nullptr, nullptr, nullptr, nullptr, nullptr};
+    score_timing tm{};
+    uint64_t launches = 0;
+    std::string err;
+
+    ~Engine() { release(); }
+    int init(int dev, int ndom) {
+        device = dev;
+        int s = alloc_slots(dev, ndom, &base);
+        if (s != SCORE_OK) return s;
+        nslots = ndom;
+        cudaError_t e = cudaSetDevice(dev);
+        if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&stream, cudaStreamNonBlocking);
+        if (e == cudaSuccess) e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+        for (auto& x : ev) if (e == cudaSuccess) e = cudaEventCreate(&x);
+        void* sym = nullptr;
+        if (e == cudaSuccess) e = cudaGetSymbolAddress(&sym, c_args);
+        if (e == cudaSuccess) d_args = (DomainArgs*)sym + base;
+        if (e == cudaSuccess) e = cudaMallocHost((void**)&h_args, (size_t)ndom * sizeof(DomainArgs));
+        return e == cudaSuccess ? SCORE_OK : SCORE_ERR_CUDA;
+    }
+    void drop_graph() {
+        if (gexec) cudaGraphExecDestroy(gexec);
+        gexec = nullptr;
+        gndom = -1;
+    }
+    void release() {
+        cudaSetDevice(device);
+        drop_graph();
+        if (h_args) cudaFreeHost(h_args);
+        d_args = nullptr; h_args = nullptr;
+        free_slots(device, base, nslots);
+        base = -1; nslots = 0;
+        for (auto& x : ev) if (x) { cudaEventDestroy(x); x = nullptr; }
+        if (stream) cudaStreamDestroy(stream);
+        stream = nullptr;
+    }
+    int fail(int code, const std::string& m) { err = m; return code; }
+    void launch_sequence(int n);
+    cudaError_t enqueue_step(int n);
+    int step(bool timed);
+    int run_until(double x_target, uint32_t max_steps, uint32_t* steps_done);
+    int autotune(double x_target, uint32_t max_steps, score_tune* out);
+    void get_tune(score_tune* out) const;
+    int set_tune(const score_tune* t);
+    void mark_run_start() { cudaEventRecord(ev[5], stream); }
+    int mark_run_end();
+};
 
 // ------------------------------------------------------------------ helpers
 namespace {
@@ -505,7 +603,6 @@ int reset_state(score_ctx* c) {
     DomainArgs& a = c->a;
     const uint64_t N = c->N;
     cudaStream_t st = c->stream;
-    cudaEventRecord(c->ev[4], st);  // start of the run span reported as score_timing.run_ms
     cudaError_t e = cudaMemcpyAsync(a.grid, c->d_grid_init, N * 4, cudaMemcpyDeviceToDevice, st);
     if (e == cudaSuccess) e = cudaMemsetAsync(a.claim, 0xFF, N * 4, st);
     for (int L = 0; L < 2 && e == cudaSuccess; ++L)
@@ -515,7 +612,13 @@ int reset_state(score_ctx* c) {
     if (e == cudaSuccess) e = cudaMemcpyAsync(a.defg_cnt, c->d_defg_cnt_init, (size_t)c->ndefg * 4, cudaMemcpyDeviceToDevice, st);
     if (e == cudaSuccess) e = cudaMemsetAsync(a.rxg_cnt, 0, std::max<size_t>(c->nrxg, 1) * 4, st);
     if (e == cudaSuccess) e = cudaMemsetAsync(c->d_state, 0, sizeof(DevState), st);
+    for (int L = 0; L < 2 && e == cudaSuccess; ++L) e = cudaMemsetAsync(a.f[L].scnt, 0, c->scnt_words[L] * 4, st);
+    if (e == cudaSuccess) e = cudaMemsetAsync(a.csct, 0, c->csct_words * 4, st);
     if (e != cudaSuccess) return c->cuda_fail(e, "reset domain");
+    a.n_ans = 0;
+    memset(&c->h_box->snap, 0, sizeof(DevState));
+    c->running = false;
+    c->trace.clear();
     c->rho = c->rho0;
     c->defg_cnt_host = c->defg_cnt_init_host;
     c->placed.assign(c->nrxg, 0);
@@ -537,7 +640,8 @@ int reset_state(score_ctx* c) {
     c->Xcells = 0.0; c->step = 0; c->defrag_cnt = 0; c->n_nuclei = 0;
     c->next_never[0] = c->next_never[1] = 0;
     c->high_water[0] = c->high_water[1] = 0;
-    c->tm = score_timing{};
+    c->eng->tm = score_timing{};
+    c->eng->mark_run_start();
     c->last = score_step_stats{};
     c->last.dt = ph.dt;
     c->last.rhomax = ph.rhomax;
@@ -547,6 +651,448 @@ int reset_state(score_ctx* c) {
 }
 
 }  // namespace
+
+// ------------------------------------------------------------------ step of one domain, host side
+namespace {
+
+// The weights answered after the last step and the cells that waited for them are
+// normally applied by the first kernels of the next step; a defragmentation moves
+// slots, so before one they are applied at once, for this domain alone.
+int flush_pending(score_ctx* c) {
+    if (c->a.n_ans == 0 && c->h_box->snap.npend_prev == 0) return SCORE_OK;
+    Engine& E = *c->eng;
+    size_t i = 0;
+    while (i < E.dom.size() && E.dom[i] != c) ++i;
+    DomainArgs a = c->a;
+    a.active = 1;
+    E.h_args[i] = a;
+    cudaError_t e = cudaMemcpyAsync(E.d_args + i, E.h_args + i, sizeof(DomainArgs), cudaMemcpyHostToDevice, c->stream);
+    if (e != cudaSuccess) return c->cuda_fail(e, "apply weights");
+    k_apply_answers<<<(uint32_t)c->sms * 2, kBlock, 0, c->stream>>>(E.base + (int)i, 1);
+    if (c->fp32) k_fix_pending<true><<<(uint32_t)c->sms * 2, kBlock, 0, c->stream>>>(E.base + (int)i, 1);
+    else k_fix_pending<false><<<(uint32_t)c->sms * 2, kBlock, 0, c->stream>>>(E.base + (int)i, 1);
+    c->launches += 2;
+    e = cudaMemsetAsync((char*)c->d_state + offsetof(DevState, npend_prev), 0, 4, c->stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(c->stream);
+    if (e != cudaSuccess) return c->cuda_fail(e, "apply weights");
+    c->a.n_ans = 0;
+    c->h_box->snap.npend_prev = 0;
+    return SCORE_OK;
+}
+
+// Before the launch: time-dependent nucleation, defragmentation at X logpoints and the
+// argument block of this step.
+int pre_step(score_ctx* c, uint32_t* newnuc) {
+    Physics& ph = c->ph;
+    int s = place_nuclei_upto(c, ph.t, newnuc);  // time-dependent nucleation (no-op when site-saturated)
+    if (s != SCORE_OK) return s;
+    // on-the-fly defragmentation at user X logpoints (SCORE_Kernel.cpp:6625-6630, thresholds in cells)
+    if (c->prm.defragmentation && c->defrag_cnt < c->prm.n_defrag && c->Xcells >= c->prm.defrag_x[c->defrag_cnt] * (double)c->N) {
+        s = flush_pending(c);
+        if (s != SCORE_OK) return s;
+        for (int L = 0; L < 2; ++L) { s = defragment(c, L); if (s != SCORE_OK) return s; }
+        c->defrag_cnt++;
+    }
+    set_step_args(c);
+    DomainArgs& a = c->a;
+    a.dt_changed = (ph.dt != c->dt_cached) ? 1 : 0;
+    a.refresh = c->refresh ? 1 : 0;
+    a.active = 1;
+    c->dt_cached = ph.dt;
+    c->refresh = false;
+    return SCORE_OK;
+}
+
+// After the step: the mailbox (scalars, weight requests, depleted grains), the host's
+// weights for the requests (applied at the start of the next step), and the master
+// block of solve_RXGROWTH (SCORE_Kernel.cpp:6691-6740).
+int post_step(score_ctx* c, uint32_t newnuc, score_step_stats* out) {
+    Physics& ph = c->ph;
+    DomainArgs& a = c->a;
+    cudaStream_t st = c->stream;
+    const DevState hs = c->h_box->snap;
+    if (hs.err) { c->failed = true; return check_device_errors(c, hs.err); }
+    const uint64_t Sv = hs.sv[0] + hs.sv[1], nfull = (uint64_t)hs.nfull[0] + hs.nfull[1], nnew = (uint64_t)hs.nwin[0] + hs.nwin[1];
+
+    // mobility weights requested this step: computed on the host (FP64, libm)
+    double pmax_new = 0.0;
+    if (hs.pmax_bits) memcpy(&pmax_new, &hs.pmax_bits, 8);
+    a.n_ans = 0;
+    if (hs.nmiss > 0) {
+        std::vector<unsigned long long> idx(hs.nmiss);
+        std::vector<double> val;
+        cudaError_t e = cudaSuccess;
+        if (hs.nmiss <= kBoxMiss) {
+            memcpy(idx.data(), c->h_box->miss, (size_t)hs.nmiss * 8);
+        } else {
+            e = cudaMemcpyAsync(idx.data(), a.miss, (size_t)hs.nmiss * 8, cudaMemcpyDeviceToHost, st);
+            if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+            if (e != cudaSuccess) return c->cuda_fail(e, "read misses");
+        }
+        const auto w_t0 = std::chrono::steady_clock::now();
+        resolve_weights(c, idx, val);
+        c->eng->tm.weights_ms += std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - w_t0).count();
+        for (double v : val) if (v > pmax_new) pmax_new = v;
+        if (hs.nmiss <= kBoxMiss) {
+            // read by the next step's k_apply_answers; the previous one finished before this step ended
+            memcpy(c->h_box->ans_idx, idx.data(), (size_t)hs.nmiss * 8);
+            memcpy(c->h_box->ans_val, val.data(), (size_t)hs.nmiss * 8);
+            a.ans_idx = c->d_box->ans_idx;
+            a.ans_val = c->d_box->ans_val;
+        } else {
+            if (!c->stage((size_t)hs.nmiss * 16)) return c->fail(SCORE_ERR_NOMEM, "staging buffer");
+            unsigned long long* si = (unsigned long long*)c->d_stage;
+            double* sv = (double*)(si + hs.nmiss);
+            e = cudaMemcpyAsync(si, idx.data(), (size_t)hs.nmiss * 8, cudaMemcpyHostToDevice, st);
+            if (e == cudaSuccess) e = cudaMemcpyAsync(sv, val.data(), (size_t)hs.nmiss * 8, cudaMemcpyHostToDevice, st);
+            if (e == cudaSuccess) e = cudaStreamSynchronize(st);  // pageable sources go out of scope
+            if (e != cudaSuccess) return c->cuda_fail(e, "upload weights");
+            a.ans_idx = si;
+            a.ans_val = sv;
+        }
+        a.n_ans = hs.nmiss;
+    }
+    // deformed grains that ran out of cells this step (synchronize_mydefpool_counts)
+    if (hs.ndepleted > 0) {
+        const uint32_t nd = std::min(hs.ndepleted, c->ndefg);
+        if (nd <= kBoxDep) {
+            for (uint32_t i = 0; i < nd; ++i) c->defg_cnt_host[c->h_box->depleted[i]] = 0;
+        } else {
+            std::vector<uint32_t> dep(nd);
+            cudaError_t e = cudaMemcpyAsync(dep.data(), a.depleted, (size_t)nd * 4, cudaMemcpyDeviceToHost, st);
+            if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+            if (e != cudaSuccess) return c->cuda_fail(e, "read depleted grains");
+            for (uint32_t g : dep) c->defg_cnt_host[g] = 0;
+        }
+        c->rhomax_version = ~0ull;  // the set of grains with cells left changed
+    }
+    for (int L = 0; L < 2; ++L) {
+        c->next_never[L] = hs.next_never[L];
+        c->high_water[L] = std::max(c->high_water[L], c->next_never[L]);
+    }
+
+    // master block, SCORE_Kernel.cpp:6691-6740
+    const double dt_used = ph.dt;
+    if (pmax_new >= ph.Pmax) ph.Pmax = pmax_new;  // running max over every P ever assigned, floored at 0
+    c->Xcells = c->Xcells + (double)nfull;
+    const double X = (c->Xcells / (double)c->N);
+    if (c->rhomax_version != c->rho_version) {  // rho max only moves when rho or the grain set changes
+        ph.rhomax = rhomax_of(c->rho, c->defg_cnt_host);
+        c->rhomax_version = c->rho_version;
+    }
+    const double rhomax_step = ph.rhomax;
+    ph.t += ph.dt;
+    ph.update_temperature();
+    ph.update_atomistic();
+    ph.update_microchemistry();
+    ph.update_mobilities();
+    if (c->prm.recovery_model != SCORE_RECOVERY_NONE && c->prm.recovery_model != SCORE_RECOVERY_NES_SOLUTEDRAG) {
+        ph.update_substructure(c->rho, c->rho0);
+        c->rho_version++;
+    }
+    ph.dt = ph.dt_minimum();
+    c->step++;
+    int s = upload_physics(c);
+    if (s != SCORE_OK) return s;
+
+    score_step_stats& o = c->last;
+    o = score_step_stats{};
+    o.step = c->step; o.n_nuclei = newnuc; o.t = ph.t; o.dt = ph.dt; o.dt_used = dt_used;
+    o.Xcells = c->Xcells; o.X = X; o.Sv = Sv; o.n_full = nfull; o.n_new = nnew;
+    o.Pmax = ph.Pmax; o.rhomax = rhomax_step; o.dXstep = 0.0;
+    o.next_never[0] = c->next_never[0]; o.next_never[1] = c->next_never[1];
+    o.n_recycled[0] = hs.nrec[0]; o.n_recycled[1] = hs.nrec[1];
+    o.p_misses = hs.nmiss;
+    if (out) *out = o;
+    return SCORE_OK;
+}
+
+// the stop rule at the top of the step loop, SCORE_Kernel.cpp:6619
+bool domain_done(const score_ctx* c, double xt) {
+    const double X = c->Xcells / (double)c->N;
+    return (c->Xcells >= (double)c->N) || (X > xt) || (c->step > c->prm.nmax) || (c->ph.t > c->ph.t_end) || (c->ph.t > c->prm.tmax);
+}
+
+// phase boundary: a real event record node when the sequence is captured into a graph
+inline void record(const Engine& E, int k) {
+    if (E.capturing) cudaEventRecordWithFlags(E.ev[k], E.stream, cudaEventRecordExternal);
+    else cudaEventRecord(E.ev[k], E.stream);
+}
+
+template <bool FP32, int ITEMS>
+void launch_grow(const Engine& E, int n) {
+    k_grow_fill<FP32, ITEMS><<<(uint32_t)(E.sms * E.cfg.fill_bpsm), kBlock, 0, E.stream>>>(E.base, n);
+    record(E, 1);
+    k_grow_lists<ITEMS><<<(uint32_t)E.sms * 8, kBlock, 0, E.stream>>>(E.base, n);
+}
+
+template <bool FP32>
+void launch_sequence_t(const Engine& E, int n) {
+    cudaStream_t st = E.stream;
+    const int d = E.base;
+    const uint32_t S = (uint32_t)E.sms;
+    k_apply_answers<<<S * 2, kBlock, 0, st>>>(d, n);
+    k_fix_pending<FP32><<<S * 2, kBlock, 0, st>>>(d, n);
+    record(E, 0);
+    if (E.cfg.items == 4) launch_grow<FP32, 4>(E, n);
+    else if (E.cfg.items == 16) launch_grow<FP32, 16>(E, n);
+    else launch_grow<FP32, 8>(E, n);
+    record(E, 2);
+    k_claim<<<S * (uint32_t)E.cfg.claim_bpsm, kBlock, 0, st>>>(d, n);
+    record(E, 3);
+    k_resolve<<<S * (uint32_t)E.cfg.commit_bpsm, kBlock, 0, st>>>(d, n);
+    k_commit<FP32><<<S * (uint32_t)E.cfg.commit_bpsm, kBlock, 0, st>>>(d, n);
+    k_new_vel<FP32><<<S * 8, kBlock, 0, st>>>(d, n);
+    k_step_end<<<(uint32_t)n, kBlock, 0, st>>>(d, n, (uint32_t)(kBlock * E.cfg.items));
+    record(E, 4);
+}
+
+constexpr int kStepKernels = 10;
+
+}  // namespace
+
+void Engine::launch_sequence(int n) {
+    if (fp32) launch_sequence_t<true>(*this, n);
+    else launch_sequence_t<false>(*this, n);
+}
+
+// the argument copy and the kernels of one step, as a graph replay or direct launches
+cudaError_t Engine::enqueue_step(int n) {
+    cudaError_t e = cudaMemcpyAsync(d_args, h_args, (size_t)n * sizeof(DomainArgs), cudaMemcpyHostToDevice, stream);
+    if (e != cudaSuccess) return e;
+    if (!use_graph) {
+        launch_sequence(n);
+        launches += kStepKernels;
+        return cudaGetLastError();
+    }
+    if (!gexec || gndom != n || !(gcfg == cfg) || gfp32 != fp32) {
+        drop_graph();
+        cudaGraph_t g = nullptr;
+        e = cudaStreamBeginCapture(stream, cudaStreamCaptureModeThreadLocal);
+        if (e != cudaSuccess) return e;
+        capturing = true;
+        launch_sequence(n);
+        capturing = false;
+        e = cudaStreamEndCapture(stream, &g);
+        if (e == cudaSuccess) e = cudaGraphInstantiate(&gexec, g, 0);
+        if (g) cudaGraphDestroy(g);
+        if (e != cudaSuccess) { gexec = nullptr; return e; }
+        gndom = n; gcfg = cfg; gfp32 = fp32;
+    }
+    launches += kStepKernels;
+    return cudaGraphLaunch(gexec, stream);
+}
+
+// One step of every running domain.
+int Engine::step(bool timed) {
+    cudaSetDevice(device);
+    const auto host_t0 = std::chrono::steady_clock::now();
+    const int n = (int)dom.size();
+    std::vector<uint32_t> newnuc(n, 0);
+    int nrun = 0;
+    for (int i = 0; i < n; ++i) {
+        score_ctx* c = dom[i];
+        if (c->running) {
+            const int s = pre_step(c, &newnuc[i]);
+            if (s != SCORE_OK) return fail(s, c->err);
+            ++nrun;
+        } else {
+            c->a.active = 0;
+        }
+        h_args[i] = c->a;
+    }
+    if (nrun == 0) return SCORE_OK;
+    cudaError_t e = enqueue_step(n);
+    const auto wait_t0 = std::chrono::steady_clock::now();
+    if (e == cudaSuccess) e = cudaStreamSynchronize(stream);  // the one wait of the step: the mailboxes are filled
+    tm.wait_ms += std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - wait_t0).count();
+    if (e != cudaSuccess) {
+        for (score_ctx* c : dom) c->failed = true;
+        return fail(SCORE_ERR_CUDA, std::string("growth step: ") + cudaGetErrorString(e));
+    }
+    if (timed) {
+        float f = 0, g = 0, cl = 0, cm = 0;
+        e = cudaEventElapsedTime(&f, ev[0], ev[1]);
+        if (e == cudaSuccess) e = cudaEventElapsedTime(&g, ev[0], ev[2]);
+        if (e == cudaSuccess) e = cudaEventElapsedTime(&cl, ev[2], ev[3]);
+        if (e == cudaSuccess) e = cudaEventElapsedTime(&cm, ev[3], ev[4]);
+        if (e != cudaSuccess) return fail(SCORE_ERR_CUDA, std::string("phase timing: ") + cudaGetErrorString(e));
+        tm.fill_ms += f; tm.grow_ms += g; tm.claim_ms += cl; tm.commit_ms += cm;
+        tm.total_ms += g + cl + cm;
+    }
+    tm.grow_launches += 1;
+    const double bpu = fp32 ? 17.0 : 25.0;  // algorithmic bytes per front-cell update of k_grow_fill
+    for (int i = 0; i < n; ++i) {
+        score_ctx* c = dom[i];
+        if (!c->running) continue;
+        score_step_stats st;
+        const int s = post_step(c, newnuc[i], &st);
+        if (s != SCORE_OK) return fail(s, c->err);
+        tm.grow_bytes += bpu * (double)st.Sv;
+        tm.step_bytes += bpu * (double)st.Sv + 120.0 * (double)st.n_full + 37.0 * (double)st.n_new;
+    }
+    tm.host_ms += std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - host_t0).count();
+    return SCORE_OK;
+}
+
+int Engine::mark_run_end() {
+    cudaEventRecord(ev[6], stream);
+    cudaError_t e = cudaEventSynchronize(ev[6]);
+    float ms = 0.0f;
+    if (e == cudaSuccess) e = cudaEventElapsedTime(&ms, ev[5], ev[6]);
+    if (e != cudaSuccess) return fail(SCORE_ERR_CUDA, std::string("run timing: ") + cudaGetErrorString(e));
+    tm.run_ms = ms;
+    return SCORE_OK;
+}
+
+// Step every domain until each meets its stop rule (X > x_target, time or step limits);
+// a domain that stops leaves the launches, the others go on.  Each domain's per-step
+// stats are kept in its trace.
+int Engine::run_until(double x_target, uint32_t max_steps, uint32_t* steps_done) {
+    uint32_t k = 0;
+    for (;;) {
+        int nrun = 0;
+        for (score_ctx* c : dom) {
+            const double xt = x_target < 0 ? c->prm.xmax : x_target;
+            c->running = c->loaded && !c->failed && !domain_done(c, xt);
+            nrun += c->running;
+        }
+        if (nrun == 0 || (max_steps && k >= max_steps)) break;
+        const int s = step(true);
+        if (s != SCORE_OK) { if (steps_done) *steps_done = k; return s; }
+        for (score_ctx* c : dom) if (c->running) c->trace.push_back(c->last);
+        ++k;
+    }
+    for (score_ctx* c : dom) c->running = false;
+    if (steps_done) *steps_done = k;
+    return mark_run_end();
+}
+
+// ------------------------------------------------------------------ contexts
+namespace {
+
+int check_params(const score_params* p, int device) {
+    if (p->nx < 3 || p->ny < 3 || p->nz < 3) return SCORE_ERR_ARG;
+    const uint64_t N = (uint64_t)p->nx * p->ny * p->nz;
+    if (N >= 0x7FFFFFFFull) return SCORE_ERR_ARG;  // pending-list entries keep the list id in bit 31 of a slot index
+    if (p->n_schedule < 1) return SCORE_ERR_ARG;
+    int ndev = 0;
+    if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) { cudaGetLastError(); return SCORE_ERR_NOT_BUILT; }
+    if (device < 0 || device >= ndev) return SCORE_ERR_ARG;
+    return SCORE_OK;
+}
+
+// a domain context stepped by `eng` (owned: a single-domain context; else a batch member)
+int make_ctx(const score_params* p, Engine* eng, bool own, score_ctx** out) {
+    score_ctx* c = new score_ctx();
+    c->prm = *p;
+    c->device = eng->device;
+    c->nx = p->nx; c->ny = p->ny; c->nz = p->nz; c->N = (uint64_t)p->nx * p->ny * p->nz;
+    c->fp32 = p->precision == SCORE_PRECISION_FP32_KAHAN;
+    c->eng = eng;
+    c->own_eng = own;
+    eng->dom.push_back(c);
+    c->stream = eng->stream;
+    c->sms = eng->sms;
+    cudaError_t e = cudaMallocHost((void**)&c->h_state, sizeof(DevState));
+    if (e == cudaSuccess) e = cudaHostAlloc((void**)&c->h_box, sizeof(HostBox), cudaHostAllocMapped);
+    if (e == cudaSuccess) e = cudaHostGetDevicePointer((void**)&c->d_box, c->h_box, 0);
+    if (e != cudaSuccess) {
+        eng->dom.pop_back();
+        if (!own) c->eng = nullptr;
+        delete c;
+        return SCORE_ERR_CUDA;
+    }
+    memset(c->h_box, 0, sizeof(DevState));
+    *out = c;
+    return SCORE_OK;
+}
+
+}  // namespace
+
+// ------------------------------------------------------------------ autotuner
+// Runs real steps (results do not depend on the tile configuration: every compaction
+// keeps slot order and claims are decided by ordinal) while cycling candidate
+// configurations step by step, and keeps per kernel group the candidate with the least
+// time per unit of work: k_grow_fill + k_grow_lists per front slot, k_claim per full
+// cell, k_resolve + k_commit + k_new_vel per full cell.  Direct launches while tuning.
+int Engine::autotune(double x_target, uint32_t max_steps, score_tune* out) {
+    static const int kItems[3] = {4, 8, 16};
+    static const int kFill[4] = {4, 8, 16, 32};
+    static const int kOther[4] = {2, 4, 8, 16};
+    double ft[12] = {0}, fu[12] = {0}, ct[4] = {0}, cu[4] = {0}, mt[4] = {0}, mu[4] = {0};
+    const bool graph = use_graph;
+    use_graph = false;
+    uint32_t k = 0;
+    int status = SCORE_OK;
+    for (;; ++k) {
+        int nrun = 0;
+        double slots = 0.0;
+        for (score_ctx* c : dom) {
+            const double xt = x_target < 0 ? c->prm.xmax : x_target;
+            c->running = c->loaded && !c->failed && !domain_done(c, xt);
+            if (c->running) { ++nrun; slots += (double)c->next_never[0] + (double)c->next_never[1]; }
+        }
+        if (nrun == 0 || (max_steps && k >= max_steps)) break;
+        const int fi = (int)(k % 12), ci = (int)(k % 4), mi = (int)((k / 4) % 4);
+        cfg.items = kItems[fi / 4];
+        cfg.fill_bpsm = kFill[fi % 4];
+        cfg.claim_bpsm = kOther[ci];
+        cfg.commit_bpsm = kOther[mi];
+        const score_timing before = tm;
+        status = step(true);
+        if (status != SCORE_OK) break;
+        double full = 0.0;
+        for (score_ctx* c : dom) if (c->running) full += (double)c->last.n_full;
+        ft[fi] += tm.grow_ms - before.grow_ms; fu[fi] += slots;
+        ct[ci] += tm.claim_ms - before.claim_ms; cu[ci] += full;
+        mt[mi] += tm.commit_ms - before.commit_ms; mu[mi] += full;
+    }
+    for (score_ctx* c : dom) c->running = false;
+    use_graph = graph;
+    if (status != SCORE_OK) return status;
+    auto best = [](const double* t, const double* u, int n) {
+        int b = -1;
+        for (int i = 0; i < n; ++i)
+            if (u[i] > 0 && (b < 0 || t[i] / u[i] < t[b] / u[b])) b = i;
+        return b;
+    };
+    const int bf = best(ft, fu, 12), bc = best(ct, cu, 4), bm = best(mt, mu, 4);
+    TuneCfg t = TuneCfg{};
+    if (bf >= 0) { t.items = kItems[bf / 4]; t.fill_bpsm = kFill[bf % 4]; }
+    if (bc >= 0) t.claim_bpsm = kOther[bc];
+    if (bm >= 0) t.commit_bpsm = kOther[bm];
+    cfg = t;
+    if (out) {
+        get_tune(out);
+        out->fill_ns_per_slot = bf >= 0 ? 1e6 * ft[bf] / fu[bf] : 0.0;
+        out->claim_ns_per_cell = bc >= 0 ? 1e6 * ct[bc] / cu[bc] : 0.0;
+        out->commit_ns_per_cell = bm >= 0 ? 1e6 * mt[bm] / mu[bm] : 0.0;
+        out->steps = k;
+    }
+    return SCORE_OK;
+}
+
+void Engine::get_tune(score_tune* out) const {
+    *out = score_tune{};
+    out->items = cfg.items;
+    out->fill_blocks_per_sm = cfg.fill_bpsm;
+    out->claim_blocks_per_sm = cfg.claim_bpsm;
+    out->commit_blocks_per_sm = cfg.commit_bpsm;
+    out->use_graph = use_graph ? 1 : 0;
+}
+
+int Engine::set_tune(const score_tune* t) {
+    if (t->items != 4 && t->items != 8 && t->items != 16) return fail(SCORE_ERR_ARG, "items must be 4, 8 or 16");
+    for (int v : {t->fill_blocks_per_sm, t->claim_blocks_per_sm, t->commit_blocks_per_sm})
+        if (v < 1 || v > 64) return fail(SCORE_ERR_ARG, "blocks per SM must be in 1..64");
+    cfg.items = t->items;
+    cfg.fill_bpsm = t->fill_blocks_per_sm;
+    cfg.claim_bpsm = t->claim_blocks_per_sm;
+    cfg.commit_bpsm = t->commit_blocks_per_sm;
+    use_graph = t->use_graph != 0;
+    return SCORE_OK;
+}
 
 // ------------------------------------------------------------------ C ABI
 extern "C" {
@@ -596,26 +1142,15 @@ const char* score_last_error(const score_ctx* c) { return c ? c->err.c_str() : "
 int score_create(score_ctx** out, const score_params* p, int device) {
     if (!out || !p) return SCORE_ERR_ARG;
     *out = nullptr;
-    if (p->nx < 3 || p->ny < 3 || p->nz < 3) return SCORE_ERR_ARG;
-    const uint64_t N = (uint64_t)p->nx * p->ny * p->nz;
-    if (N >= 0x7FFFFFFFull) return SCORE_ERR_ARG;  // pending-list entries keep the list id in bit 31 of a slot index
-    if (p->n_schedule < 1) return SCORE_ERR_ARG;
-    int ndev = 0;
-    if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) return SCORE_ERR_NOT_BUILT;
-    if (device < 0 || device >= ndev) return SCORE_ERR_ARG;
-    score_ctx* c = new score_ctx();
-    c->prm = *p;
-    c->device = device;
-    c->nx = p->nx; c->ny = p->ny; c->nz = p->nz; c->N = N;
-    c->fp32 = p->precision == SCORE_PRECISION_FP32_KAHAN;
-    cudaError_t e = cudaSetDevice(device);
-    if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking);
-    if (e == cudaSuccess) e = cudaDeviceGetAttribute(&c->sms, cudaDevAttrMultiProcessorCount, device);
-    for (auto& ev : c->ev) if (e == cudaSuccess) e = cudaEventCreate(&ev);
-    if (e == cudaSuccess) e = cudaMallocHost((void**)&c->h_state, sizeof(DevState));
-    if (e == cudaSuccess) e = cudaHostAlloc((void**)&c->h_box, sizeof(HostBox), cudaHostAllocMapped);
-    if (e == cudaSuccess) e = cudaHostGetDevicePointer((void**)&c->d_box, c->h_box, 0);
-    if (e != cudaSuccess) { delete c; return SCORE_ERR_CUDA; }
+    int s = check_params(p, device);
+    if (s != SCORE_OK) return s;
+    Engine* eng = new Engine();
+    s = eng->init(device, 1);
+    if (s != SCORE_OK) { delete eng; return s; }
+    eng->fp32 = p->precision == SCORE_PRECISION_FP32_KAHAN;
+    score_ctx* c = nullptr;
+    s = make_ctx(p, eng, true, &c);
+    if (s != SCORE_OK) return s;
     *out = c;
     return SCORE_OK;
 }
@@ -681,18 +1216,24 @@ int score_load_domain(score_ctx* c, const uint32_t* grid, const double* defg_qua
             if (e == cudaSuccess) e = dalloc(&f.dir, caps[L]);
             if (e == cudaSuccess) e = dalloc(&f.full, caps[L]);
             if (e == cudaSuccess) e = dalloc(&f.recyc, recs[L]);
-            const size_t tiles = (size_t)caps[L] / kGrowTile + 1;
-            if (e == cudaSuccess) e = dalloc(&f.fmask, tiles * (kGrowTile / 32));
-            if (e == cudaSuccess) e = dalloc(&f.imask, tiles * (kGrowTile / 32));
+            // sized for the smallest grow tile (kBlock * 4 slots) and the largest (kBlock * 16)
+            const size_t tiles = (size_t)caps[L] / (kBlock * 4) + 2;
+            const size_t words = (size_t)caps[L] / 32 + 2 * GrowShape<16>::kWords;
+            c->scnt_words[L] = 2 * (tiles / kSuper + 2);
+            if (e == cudaSuccess) e = dalloc(&f.fmask, words);
+            if (e == cudaSuccess) e = dalloc(&f.imask, words);
             if (e == cudaSuccess) e = dalloc(&f.tcnt, 2 * tiles);
+            if (e == cudaSuccess) e = dalloc(&f.scnt, c->scnt_words[L]);
         }
+        c->csct_words = 2 * ((N / kBlock + 2) / kSuper + 2);
         a.misscap = a.pendcap = (uint32_t)std::min<uint64_t>(N, 1ull << 25);
         if (e == cudaSuccess) e = dalloc(&a.grid, N);
         if (e == cudaSuccess) e = dalloc(&c->d_grid_init, N);
         if (e == cudaSuccess) e = dalloc(&a.claim, N);
         if (e == cudaSuccess) e = dalloc(&a.amask, N);
         if (e == cudaSuccess) e = dalloc(&a.tobm, N);
-        if (e == cudaSuccess) e = dalloc(&a.ctcnt, 2 * (N / kBlock + 1));
+        if (e == cudaSuccess) e = dalloc(&a.ctcnt, 2 * (N / kBlock + 2));
+        if (e == cudaSuccess) e = dalloc(&a.csct, c->csct_words);
         if (e == cudaSuccess) e = dalloc(&a.ptab, ptab_words);
         if (e == cudaSuccess) e = dalloc(&a.defg_cnt, ndefg);
         if (e == cudaSuccess) e = dalloc(&c->d_defg_cnt_init, ndefg);
@@ -708,6 +1249,7 @@ int score_load_domain(score_ctx* c, const uint32_t* grid, const double* defg_qua
         if (e != cudaSuccess) { c->release_domain(); return c->fail(SCORE_ERR_NOMEM, std::string("device allocation: ") + cudaGetErrorString(e)); }
         a.pforce = c->d_pforce;
         a.st = c->d_state;
+        a.box = c->d_box;
         a.rxq = c->d_rxq; a.dfq = c->d_dfq;
         weight_constants(p, &a.pc_fac, &a.pc_lagb, &a.pc_maxdev, a.pc_m40, &a.pc_theta_sat);
         a.pc_margin = 1e-9;
@@ -757,197 +1299,25 @@ int score_step(score_ctx* c, score_step_stats* out) {
     if (!c) return SCORE_ERR_ARG;
     if (!c->loaded) return c->fail(SCORE_ERR_STATE, "no domain loaded");
     if (c->failed) return SCORE_ERR_STATE;  // a device error left the front lists undefined
-    cudaSetDevice(c->device);
-    Physics& ph = c->ph;
-    const auto host_t0 = std::chrono::steady_clock::now();
-    uint32_t newnuc = 0;
-    int s = place_nuclei_upto(c, ph.t, &newnuc);  // time-dependent nucleation (no-op when site-saturated)
-    if (s != SCORE_OK) return s;
-    // on-the-fly defragmentation at user X logpoints (SCORE_Kernel.cpp:6625-6630, thresholds in cells)
-    if (c->prm.defragmentation && c->defrag_cnt < c->prm.n_defrag && c->Xcells >= c->prm.defrag_x[c->defrag_cnt] * (double)c->N) {
-        for (int L = 0; L < 2; ++L) { s = defragment(c, L); if (s != SCORE_OK) return s; }
-        c->defrag_cnt++;
-    }
-    set_step_args(c);
-    DomainArgs& a = c->a;
-    a.dt_changed = (c->ph.dt != c->dt_cached) ? 1 : 0;
-    c->dt_cached = c->ph.dt;
-    cudaStream_t st = c->stream;
-    cudaEventRecord(c->ev[0], st);
-    uint32_t max_tiles = 1;
-    for (int L = 0; L < 2; ++L) {
-        const uint32_t tiles = (c->next_never[L] + kGrowTile - 1) / kGrowTile;
-        max_tiles = std::max(max_tiles, tiles);
-        const uint32_t grid = std::max<uint32_t>(1, std::min<uint32_t>(tiles, (uint32_t)c->sms * 16));
-        if (c->fp32) {
-            if (c->refresh) k_grow_fill<true, true><<<grid, kBlock, 0, st>>>(a, L);
-            else k_grow_fill<true, false><<<grid, kBlock, 0, st>>>(a, L);
-        } else {
-            if (c->refresh) k_grow_fill<false, true><<<grid, kBlock, 0, st>>>(a, L);
-            else k_grow_fill<false, false><<<grid, kBlock, 0, st>>>(a, L);
-        }
-    }
-    cudaEventRecord(c->ev[6], st);
-    k_scan_tiles<0><<<2, 1024, 0, st>>>(a);
-    k_grow_lists<<<dim3(std::min<uint32_t>((max_tiles + kWarps - 1) / kWarps, (uint32_t)c->sms * 8), 2), kBlock, 0, st>>>(a);
-    c->refresh = false;
-    cudaEventRecord(c->ev[1], st);
-    k_claim<<<(uint32_t)c->sms * 4, kBlock, 0, st>>>(a);
-    cudaEventRecord(c->ev[2], st);
-    k_resolve<<<(uint32_t)c->sms * 4, kBlock, 0, st>>>(a);
-    k_scan_tiles<1><<<1, 1024, 0, st>>>(a);
-    if (c->fp32) {
-        k_commit<true><<<(uint32_t)c->sms * 4, kBlock, 0, st>>>(a);
-        k_new_vel<true><<<(uint32_t)c->sms * 8, kBlock, 0, st>>>(a);
-    } else {
-        k_commit<false><<<(uint32_t)c->sms * 4, kBlock, 0, st>>>(a);
-        k_new_vel<false><<<(uint32_t)c->sms * 8, kBlock, 0, st>>>(a);
-    }
-    k_step_end<<<1, kBlock, 0, st>>>(a, c->d_box);
-    cudaEventRecord(c->ev[3], st);
-    c->launches += 10;
-    cudaError_t e = cudaStreamSynchronize(st);  // the one wait of the step: k_step_end filled the mailbox
-    if (e != cudaSuccess) { c->failed = true; return c->cuda_fail(e, "growth step"); }
-    const DevState hs = c->h_box->snap;
-    if (hs.err) { c->failed = true; return check_device_errors(c, hs.err); }
-    float ms_grow = 0, ms_claim = 0, ms_commit = 0, ms_fill = 0;
-    cudaEventElapsedTime(&ms_fill, c->ev[0], c->ev[6]);
-    c->tm.fill_ms += ms_fill;
-    cudaEventElapsedTime(&ms_grow, c->ev[0], c->ev[1]);
-    cudaEventElapsedTime(&ms_claim, c->ev[1], c->ev[2]);
-    cudaEventElapsedTime(&ms_commit, c->ev[2], c->ev[3]);
-    c->tm.grow_ms += ms_grow; c->tm.claim_ms += ms_claim; c->tm.commit_ms += ms_commit;
-    c->tm.total_ms += ms_grow + ms_claim + ms_commit;
-    c->tm.grow_launches += 2;  // fill-update launches (the grow_bytes kernels)
-    c->tm.kernel_launches += 10;
-    // algorithmic bytes: grow 25 B (FP64: dir 1, vel 8, fill 8 r + 8 w) or 17 B (FP32: dir, vel 4, fill 4 + comp 4 r/w)
-    const double bpu = c->fp32 ? 17.0 : 25.0;
-    const uint64_t Sv = hs.sv[0] + hs.sv[1], nfull = (uint64_t)hs.nfull[0] + hs.nfull[1], nnew = (uint64_t)hs.nwin[0] + hs.nwin[1];
-    c->tm.grow_bytes += bpu * (double)Sv;
-    c->tm.step_bytes += bpu * (double)Sv + 120.0 * (double)nfull + 37.0 * (double)nnew;
-
-    // mobility weights requested this step: compute on the host (FP64, libm), patch table + cells
-    double pmax_new = 0.0;
-    if (hs.pmax_bits) memcpy(&pmax_new, &hs.pmax_bits, 8);
-    if (hs.nmiss > 0 || hs.npending > 0) {
-        std::vector<unsigned long long> idx(hs.nmiss);
-        std::vector<double> val;
-        if (hs.nmiss <= kBoxMiss) {
-            memcpy(idx.data(), c->h_box->miss, (size_t)hs.nmiss * 8);
-        } else {
-            e = cudaMemcpyAsync(idx.data(), a.miss, (size_t)hs.nmiss * 8, cudaMemcpyDeviceToHost, st);
-            if (e == cudaSuccess) e = cudaStreamSynchronize(st);
-            if (e != cudaSuccess) return c->cuda_fail(e, "read misses");
-        }
-        resolve_weights(c, idx, val);
-        for (double v : val) if (v > pmax_new) pmax_new = v;
-        if (hs.nmiss > 0) {
-            const unsigned long long* d_i;
-            const double* d_v;
-            if (hs.nmiss <= kBoxMiss) {
-                // the previous step's k_fill_ptab finished before this step's k_step_end
-                memcpy(c->h_box->ans_idx, idx.data(), (size_t)hs.nmiss * 8);
-                memcpy(c->h_box->ans_val, val.data(), (size_t)hs.nmiss * 8);
-                d_i = c->d_box->ans_idx;
-                d_v = c->d_box->ans_val;
-            } else {
-                if (!c->stage((size_t)hs.nmiss * 16)) return c->fail(SCORE_ERR_NOMEM, "staging buffer");
-                unsigned long long* si = (unsigned long long*)c->d_stage;
-                double* sv = (double*)(si + hs.nmiss);
-                e = cudaMemcpyAsync(si, idx.data(), (size_t)hs.nmiss * 8, cudaMemcpyHostToDevice, st);
-                if (e == cudaSuccess) e = cudaMemcpyAsync(sv, val.data(), (size_t)hs.nmiss * 8, cudaMemcpyHostToDevice, st);
-                if (e == cudaSuccess) e = cudaStreamSynchronize(st);  // pageable sources go out of scope
-                if (e != cudaSuccess) return c->cuda_fail(e, "upload weights");
-                d_i = si;
-                d_v = sv;
-            }
-            k_fill_ptab<<<blocks_for(hs.nmiss, c->sms), kBlock, 0, st>>>(a.ptab, d_i, d_v, hs.nmiss);
-            c->launches++;
-        }
-        const uint32_t np = std::min(hs.npending, a.pendcap);
-        if (c->fp32) k_fix_pending<true><<<blocks_for(np, c->sms), kBlock, 0, st>>>(a, np);
-        else k_fix_pending<false><<<blocks_for(np, c->sms), kBlock, 0, st>>>(a, np);
-        c->launches++;
-    }
-    // deformed grains that ran out of cells this step (synchronize_mydefpool_counts)
-    if (hs.ndepleted > 0) {
-        const uint32_t nd = std::min(hs.ndepleted, c->ndefg);
-        if (nd <= kBoxDep) {
-            for (uint32_t i = 0; i < nd; ++i) c->defg_cnt_host[c->h_box->depleted[i]] = 0;
-        } else {
-            std::vector<uint32_t> dep(nd);
-            e = cudaMemcpyAsync(dep.data(), a.depleted, (size_t)nd * 4, cudaMemcpyDeviceToHost, st);
-            if (e == cudaSuccess) e = cudaStreamSynchronize(st);
-            if (e != cudaSuccess) return c->cuda_fail(e, "read depleted grains");
-            for (uint32_t g : dep) c->defg_cnt_host[g] = 0;
-        }
-        c->rhomax_version = ~0ull;  // the set of grains with cells left changed
-    }
-    for (int L = 0; L < 2; ++L) {
-        c->next_never[L] = hs.next_never[L];
-        c->high_water[L] = std::max(c->high_water[L], c->next_never[L]);
-    }
-
-    // master block, SCORE_Kernel.cpp:6691-6740
-    const double dt_used = ph.dt;
-    if (pmax_new >= ph.Pmax) ph.Pmax = pmax_new;  // running max over every P ever assigned, floored at 0
-    c->Xcells = c->Xcells + (double)nfull;
-    const double X = (c->Xcells / (double)c->N);
-    if (c->rhomax_version != c->rho_version) {  // rho max only moves when rho or the grain set changes
-        ph.rhomax = rhomax_of(c->rho, c->defg_cnt_host);
-        c->rhomax_version = c->rho_version;
-    }
-    const double rhomax_step = ph.rhomax;
-    ph.t += ph.dt;
-    ph.update_temperature();
-    ph.update_atomistic();
-    ph.update_microchemistry();
-    ph.update_mobilities();
-    if (c->prm.recovery_model != SCORE_RECOVERY_NONE && c->prm.recovery_model != SCORE_RECOVERY_NES_SOLUTEDRAG) {
-        ph.update_substructure(c->rho, c->rho0);
-        c->rho_version++;
-    }
-    ph.dt = ph.dt_minimum();
-    c->step++;
-    s = upload_physics(c);
-    if (s != SCORE_OK) return s;
-
-    score_step_stats& o = c->last;
-    o = score_step_stats{};
-    o.step = c->step; o.n_nuclei = newnuc; o.t = ph.t; o.dt = ph.dt; o.dt_used = dt_used;
-    o.Xcells = c->Xcells; o.X = X; o.Sv = Sv; o.n_full = nfull; o.n_new = nnew;
-    o.Pmax = ph.Pmax; o.rhomax = rhomax_step; o.dXstep = 0.0;
-    o.next_never[0] = c->next_never[0]; o.next_never[1] = c->next_never[1];
-    o.n_recycled[0] = hs.nrec[0]; o.n_recycled[1] = hs.nrec[1];
-    o.p_misses = hs.nmiss;
-    c->tm.host_ms += std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - host_t0).count();
-    if (out) *out = o;
+    c->running = true;
+    const int s = c->eng->step(true);
+    c->running = false;
+    if (s != SCORE_OK) { if (c->err.empty()) c->err = c->eng->err; return s; }
+    if (out) *out = c->last;
     return SCORE_OK;
 }
 
 int score_run_until(score_ctx* c, double x_target, score_step_stats* trace, uint32_t trace_cap, uint32_t* n_steps) {
     if (!c) return SCORE_ERR_ARG;
     if (!c->loaded) return c->fail(SCORE_ERR_STATE, "no domain loaded");
-    const double xt = x_target < 0 ? c->prm.xmax : x_target;
+    if (c->failed) return SCORE_ERR_STATE;
+    c->trace.clear();
     uint32_t k = 0;
-    for (;;) {
-        const double X = c->Xcells / (double)c->N;
-        // stop rule at the top of the step loop, SCORE_Kernel.cpp:6619
-        if ((c->Xcells >= (double)c->N) || (X > xt) || (c->step > c->prm.nmax) || (c->ph.t > c->ph.t_end) || (c->ph.t > c->prm.tmax)) break;
-        score_step_stats st;
-        int s = score_step(c, &st);
-        if (s != SCORE_OK) { if (n_steps) *n_steps = k; return s; }
-        if (trace && k < trace_cap) trace[k] = st;
-        ++k;
-    }
+    const int s = c->eng->run_until(x_target, 0, &k);
+    if (trace) for (uint32_t i = 0; i < k && i < trace_cap && i < c->trace.size(); ++i) trace[i] = c->trace[i];
     if (n_steps) *n_steps = k;
-    cudaEventRecord(c->ev[5], c->stream);
-    cudaError_t e = cudaEventSynchronize(c->ev[5]);
-    float ms = 0.0f;
-    if (e == cudaSuccess) e = cudaEventElapsedTime(&ms, c->ev[4], c->ev[5]);
-    if (e != cudaSuccess) return c->cuda_fail(e, "run timing");
-    c->tm.run_ms = ms;
-    return SCORE_OK;
+    if (s != SCORE_OK && c->err.empty()) c->err = c->eng->err;
+    return s;
 }
 
 int score_get_stats(score_ctx* c, score_step_stats* out) {
@@ -991,9 +1361,170 @@ int score_grain_counts(score_ctx* c, uint32_t* rxg_counts, uint32_t* defg_counts
 
 int score_get_timing(score_ctx* c, score_timing* out) {
     if (!c || !out) return SCORE_ERR_ARG;
-    *out = c->tm;
-    out->kernel_launches = c->launches;
+    *out = c->eng->tm;
+    out->kernel_launches = c->launches + c->eng->launches;
     return SCORE_OK;
+}
+
+int score_get_tune(score_ctx* c, score_tune* out) {
+    if (!c || !out) return SCORE_ERR_ARG;
+    c->eng->get_tune(out);
+    return SCORE_OK;
+}
+
+int score_set_tune(score_ctx* c, const score_tune* t) {
+    if (!c || !t) return SCORE_ERR_ARG;
+    const int s = c->eng->set_tune(t);
+    if (s != SCORE_OK) c->err = c->eng->err;
+    return s;
+}
+
+int score_autotune(score_ctx* c, double x_target, uint32_t max_steps, score_tune* out) {
+    if (!c) return SCORE_ERR_ARG;
+    int s = score_restart(c);
+    if (s == SCORE_OK) s = score_place_nuclei(c, nullptr);
+    if (s == SCORE_OK) s = c->eng->autotune(x_target, max_steps, out);
+    if (s != SCORE_OK) { if (c->err.empty()) c->err = c->eng->err; return s; }
+    s = score_restart(c);
+    if (s == SCORE_OK) s = score_place_nuclei(c, nullptr);
+    return s;
+}
+
+}  // extern "C"
+
+// ------------------------------------------------------------------ batched ensemble
+struct score_batch {
+    Engine eng;
+    std::vector<score_ctx*> dom;
+    std::string err;
+    ~score_batch() {
+        for (score_ctx* c : dom) delete c;
+        dom.clear();
+    }
+    int fail(int code, const std::string& m) { err = m; return code; }
+    int dom_fail(score_ctx* c, int code) { err = c->err; return code; }
+};
+
+extern "C" {
+
+int score_batch_create(score_batch** out, const score_params* params, uint32_t n, int device) {
+    if (!out || !params || n == 0 || n > (uint32_t)kMaxDomains) return SCORE_ERR_ARG;
+    *out = nullptr;
+    for (uint32_t i = 0; i < n; ++i) {
+        const int s = check_params(&params[i], device);
+        if (s != SCORE_OK) return s;
+        if (params[i].precision != params[0].precision) return SCORE_ERR_ARG;  // one precision per batch
+    }
+    score_batch* b = new score_batch();
+    const int si = b->eng.init(device, (int)n);
+    if (si != SCORE_OK) { delete b; return si; }
+    b->eng.fp32 = params[0].precision == SCORE_PRECISION_FP32_KAHAN;
+    for (uint32_t i = 0; i < n; ++i) {
+        score_ctx* c = nullptr;
+        const int s = make_ctx(&params[i], &b->eng, false, &c);
+        if (s != SCORE_OK) { delete b; return s; }
+        b->dom.push_back(c);
+    }
+    *out = b;
+    return SCORE_OK;
+}
+
+void score_batch_destroy(score_batch* b) { delete b; }
+
+const char* score_batch_last_error(const score_batch* b) { return b ? b->err.c_str() : "null batch"; }
+
+int score_batch_load_domain(score_batch* b, uint32_t d, const uint32_t* grid, const double* defg_quat,
+                            const double* defg_rho0, uint32_t ndefg, const double* rxg_quat, const uint32_t* rxg_site,
+                            const double* rxg_tincub, uint32_t nrxg, const double* ptable) {
+    if (!b || d >= b->dom.size()) return SCORE_ERR_ARG;
+    const int s = score_load_domain(b->dom[d], grid, defg_quat, defg_rho0, ndefg, rxg_quat, rxg_site, rxg_tincub, nrxg, ptable);
+    return s == SCORE_OK ? s : b->dom_fail(b->dom[d], s);
+}
+
+int score_batch_restart(score_batch* b) {
+    if (!b) return SCORE_ERR_ARG;
+    for (score_ctx* c : b->dom) {
+        if (!c->a.grid) continue;
+        const int s = score_restart(c);
+        if (s != SCORE_OK) return b->dom_fail(c, s);
+    }
+    b->eng.mark_run_start();
+    return SCORE_OK;
+}
+
+int score_batch_place_nuclei(score_batch* b) {
+    if (!b) return SCORE_ERR_ARG;
+    for (score_ctx* c : b->dom) {
+        if (!c->loaded) continue;
+        const int s = score_place_nuclei(c, nullptr);
+        if (s != SCORE_OK) return b->dom_fail(c, s);
+    }
+    return SCORE_OK;
+}
+
+int score_batch_run_until(score_batch* b, double x_target, uint32_t max_steps, uint32_t* steps_done) {
+    if (!b) return SCORE_ERR_ARG;
+    for (score_ctx* c : b->dom) c->trace.clear();
+    const int s = b->eng.run_until(x_target, max_steps, steps_done);
+    return s == SCORE_OK ? s : b->fail(s, b->eng.err);
+}
+
+int score_batch_get_stats(score_batch* b, uint32_t d, score_step_stats* out) {
+    if (!b || d >= b->dom.size()) return SCORE_ERR_ARG;
+    return score_get_stats(b->dom[d], out);
+}
+
+int score_batch_trace(score_batch* b, uint32_t d, score_step_stats* trace, uint32_t cap, uint32_t* n_steps) {
+    if (!b || d >= b->dom.size()) return SCORE_ERR_ARG;
+    const std::vector<score_step_stats>& t = b->dom[d]->trace;
+    if (trace) for (uint32_t i = 0; i < cap && i < t.size(); ++i) trace[i] = t[i];
+    if (n_steps) *n_steps = (uint32_t)t.size();
+    return SCORE_OK;
+}
+
+int score_batch_export_labels(score_batch* b, uint32_t d, uint32_t* labels) {
+    if (!b || d >= b->dom.size()) return SCORE_ERR_ARG;
+    const int s = score_export_labels(b->dom[d], labels);
+    return s == SCORE_OK ? s : b->dom_fail(b->dom[d], s);
+}
+
+int score_batch_grain_counts(score_batch* b, uint32_t d, uint32_t* rxg_counts, uint32_t* defg_counts) {
+    if (!b || d >= b->dom.size()) return SCORE_ERR_ARG;
+    const int s = score_grain_counts(b->dom[d], rxg_counts, defg_counts);
+    return s == SCORE_OK ? s : b->dom_fail(b->dom[d], s);
+}
+
+int score_batch_get_timing(score_batch* b, score_timing* out) {
+    if (!b || !out) return SCORE_ERR_ARG;
+    *out = b->eng.tm;
+    uint64_t extra = 0;
+    for (score_ctx* c : b->dom) extra += c->launches;
+    out->kernel_launches = b->eng.launches + extra;
+    return SCORE_OK;
+}
+
+int score_batch_get_tune(score_batch* b, score_tune* out) {
+    if (!b || !out) return SCORE_ERR_ARG;
+    b->eng.get_tune(out);
+    return SCORE_OK;
+}
+
+int score_batch_set_tune(score_batch* b, const score_tune* t) {
+    if (!b || !t) return SCORE_ERR_ARG;
+    const int s = b->eng.set_tune(t);
+    return s == SCORE_OK ? s : b->fail(s, b->eng.err);
+}
+
+int score_batch_autotune(score_batch* b, double x_target, uint32_t max_steps, score_tune* out) {
+    if (!b) return SCORE_ERR_ARG;
+    int s = score_batch_restart(b);
+    if (s == SCORE_OK) s = score_batch_place_nuclei(b);
+    if (s != SCORE_OK) return s;
+    s = b->eng.autotune(x_target, max_steps, out);
+    if (s != SCORE_OK) return b->fail(s, b->eng.err);
+    s = score_batch_restart(b);
+    if (s == SCORE_OK) s = score_batch_place_nuclei(b);
+    return s;
 }
 
 }  // extern "C"

@@ -51,7 +51,8 @@ struct DFront {
     uint32_t* recyc;     // recycle list (slot indices, slot order, capped)
     uint32_t* fmask;     // per 32 slots: full slots of this step (bit = slot % 32)
     uint32_t* imask;     // per 32 slots: INACTIVE slots of this step
-    uint32_t* tcnt;      // per grow tile: (full, INACTIVE) counts, then their exclusive prefixes
+    uint32_t* tcnt;      // per grow tile: (full, INACTIVE) counts
+    uint32_t* scnt;      // per supertile of kSuper grow tiles: the same counts (zero between steps)
     uint32_t cap;        // device capacity of the slot arrays
     uint32_t reccap;     // ntotalRecyclingList of the reference
 };
@@ -75,6 +76,8 @@ __device__ __forceinline__ uint32_t fdiv(uint32_t n, const FastDiv& f) {
     return f.d == 1 ? n : (__umulhi(n, f.mul) >> f.shr);
 }
 
+struct HostBox;
+
 struct DomainArgs {
     DFront f[2];
     DevState* st;
@@ -82,7 +85,8 @@ struct DomainArgs {
     uint32_t* claim;
     uint32_t* amask;            // per full cell: attempts made (bit d), then attempts won
     uint32_t* tobm;             // per full cell: won attempts that go to the Border list
-    uint32_t* ctcnt;            // per commit tile: (Inside, Border) win counts, then prefixes
+    uint32_t* ctcnt;            // per commit tile: (Inside, Border) win counts
+    uint32_t* csct;             // per supertile of kSuper commit tiles: the same counts (zero between steps)
     unsigned long long* ptab;   // nrxg x ndefg mobility weights as bits (kPtabEmpty = unknown)
     const double* pforce;       // per deformed grain driving force (FP64)
     uint32_t* defg_cnt;
@@ -99,6 +103,12 @@ struct DomainArgs {
     uint32_t border_ref_cap;
     int32_t border_policy, boundary, mobility_model;
     int32_t dt_changed;         // dt differs from the dt the cached increments were made with
+    int32_t refresh;            // recompute every vel this step (T, rho or the drag changed)
+    int32_t active;             // the domain steps in this launch
+    uint32_t n_ans;             // weights the host computed for the last step's requests
+    const unsigned long long* ans_idx;  // their table indices (device view of the mailbox)
+    const double* ans_val;
+    HostBox* box;               // device view of the domain's mailbox
     double mLAGB, mHAGB, mGS, mRH, dt, cinv;
     float dtc32;
     // device classification of mobility weights whose value is an exact constant
@@ -174,142 +184,327 @@ __device__ __forceinline__ void scan64_pair(uint32_t* cntA, uint32_t* cntB, uint
     totB = __shfl_sync(0xFFFFFFFFu, bi, 31);
 }
 
+// ------------------------------------------------------------------ work over many domains
+// Every step kernel takes the array of per-domain argument blocks and walks a global
+// list of work units (tiles, full cells, new cells) that concatenates the domains'
+// (and lists') units; a block first builds the exclusive prefix of the unit counts of
+// all segments in shared memory and maps a unit to its segment by binary search.
+// One domain is the batch of size one.
+constexpr int kMaxDomains = 64;
+constexpr int kMaxSegs = 2 * kMaxDomains;
+
+// Argument blocks of every domain that steps on this device, in constant memory: a
+// field read is a constant-cache access that stores never invalidate.  Each engine
+// owns a range of slots; its kernels take the range's base.
+__constant__ DomainArgs c_args[kMaxDomains];
+
+// Block-wide (kBlock threads) exclusive scan of the unit counts of `nseg` segments
+// into s_pre[0..nseg]; count(seg) is evaluated once per segment.  Returns the total.
+template <class Count>
+__device__ __forceinline__ uint32_t seg_prefix(uint32_t* s_pre, int nseg, Count count) {
+    __shared__ uint32_t s_warp[kWarps];
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    constexpr int PER = (kMaxSegs + kBlock - 1) / kBlock;  // segments per thread
+    uint32_t v[PER], sum = 0;
+#pragma unroll
+    for (int j = 0; j < PER; ++j) {
+        const int s = threadIdx.x * PER + j;
+        v[j] = s < nseg ? count(s) : 0u;
+        sum += v[j];
+    }
+    uint32_t inc = sum;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        const uint32_t x = __shfl_up_sync(0xFFFFFFFFu, inc, o);
+        if (lane >= o) inc += x;
+    }
+    if (lane == 31) s_warp[warp] = inc;
+    __syncthreads();
+    uint32_t before = 0, total = 0;
+#pragma unroll
+    for (int w = 0; w < kWarps; ++w) {
+        before += w < warp ? s_warp[w] : 0u;
+        total += s_warp[w];
+    }
+    uint32_t e = before + inc - sum;
+#pragma unroll
+    for (int j = 0; j < PER; ++j) {
+        const int s = threadIdx.x * PER + j;
+        if (s < nseg) s_pre[s] = e;
+        e += v[j];
+    }
+    if (threadIdx.x == 0) s_pre[nseg] = total;
+    __syncthreads();
+    return total;
+}
+
+// segment of unit u: the last s with s_pre[s] <= u (segments with no units are skipped)
+__device__ __forceinline__ int seg_find(const uint32_t* s_pre, int nseg, uint32_t u) {
+    int lo = 0, hi = nseg - 1;
+    while (lo < hi) {
+        const int mid = (lo + hi + 1) >> 1;
+        if (s_pre[mid] <= u) lo = mid;
+        else hi = mid - 1;
+    }
+    return lo;
+}
+
+// grow tiles of a list: kBlock * ITEMS slots, ITEMS * kWarps mask words
+template <int ITEMS>
+struct GrowShape {
+    static constexpr uint32_t kTile = kBlock * ITEMS;
+    static constexpr uint32_t kWords = ITEMS * kWarps;
+};
+constexpr uint32_t kSuper = 64;  // tiles per supertile of the two-level tile prefix
+
+// Exclusive prefix of tile `tile` of a (cnt: per-tile pairs, sup: per-supertile pairs)
+// count array, computed by one warp; every lane returns both prefixes.
+__device__ __forceinline__ void tile_prefix(const uint32_t* cnt, const uint32_t* sup, uint32_t tile, uint32_t& pa, uint32_t& pb) {
+    const int lane = threadIdx.x & 31;
+    const uint32_t s = tile / kSuper;
+    uint32_t a = 0, b = 0;
+    for (uint32_t i = lane; i < s; i += 32) { a += sup[2 * i]; b += sup[2 * i + 1]; }
+    for (uint32_t i = s * kSuper + lane; i < tile; i += 32) { a += cnt[2 * i]; b += cnt[2 * i + 1]; }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+        a += __shfl_xor_sync(0xFFFFFFFFu, a, o);
+        b += __shfl_xor_sync(0xFFFFFFFFu, b, o);
+    }
+    pa = a; pb = b;
+}
+
 // ------------------------------------------------------------------ K1 grow
-// Three launches, none of which waits on another block:
-//   k_grow_fill   streams the slots of one list in tiles of kGrowTile (one block per
-//                 tile, grid-stride), updates the fills, and writes one bit per slot
-//                 (full / INACTIVE) plus the tile's two counts;
-//   k_scan_tiles  one block per scanned array: exclusive scan of the tile counts;
-//   k_grow_lists  one warp per tile expands the bit masks into the FullRX list and
-//                 the capped recycle list, in slot order.
+// Two launches, neither of which waits on another block:
+//   k_grow_fill   streams the slots of every (domain, list) in tiles of kBlock*ITEMS
+//                 slots, updates the fills, writes one bit per slot (full / INACTIVE)
+//                 and the tile's two counts, and adds them to its supertile's counts;
+//   k_grow_lists  one warp per tile: the tile's exclusive prefix from the supertile
+//                 and tile counts, then the FullRX list and the capped recycle list in
+//                 slot order; the warp of a list's last tile stores the list totals.
 // REFRESH: recompute vel of every active slot from the P table and the current
 // physics (after T, rho or the drag changed) before growing it.
-constexpr int kGrowItems = 8;
-constexpr uint32_t kGrowTile = kBlock * kGrowItems;  // 64 mask words per tile
-
-template <bool FP32, bool REFRESH>
-__global__ void __launch_bounds__(kBlock, 4) k_grow_fill(DomainArgs a, int L) {
-    constexpr int ITEMS = kGrowItems;
-    const DFront fr = a.f[L];
-    const uint32_t n = a.st->next_never[L];
-    const uint32_t ntiles = (n + kGrowTile - 1) / kGrowTile;
-    __shared__ uint32_t s_f[kWarps], s_i[kWarps];
+// returns the thread's ACTIVE slots (the Sv share)
+template <bool FP32, bool REFRESH, int ITEMS>
+__device__ __forceinline__ uint32_t grow_tile(const DomainArgs& a, int L, uint32_t tile, uint32_t n, uint32_t* s_f, uint32_t* s_i) {
+    using S = GrowShape<ITEMS>;
+    const DFront& fr = a.f[L];
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    unsigned long long sv = 0;
-    for (uint32_t tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
-        const uint32_t base = tile * kGrowTile;
-        uint8_t d[ITEMS];
+    const uint32_t base = tile * S::kTile;
+    uint32_t sv = 0;
+    uint8_t d[ITEMS];
+#pragma unroll
+    for (int k = 0; k < ITEMS; ++k) {
+        const uint32_t slot = base + (uint32_t)(k * kBlock) + threadIdx.x;
+        d[k] = slot < n ? fr.dir[slot] : kInactive;
+    }
+    bool full[ITEMS];
+    if (!FP32) {
+        double w[ITEMS], fill[ITEMS];  // w: cached inc, or vel when the increment is stale
 #pragma unroll
         for (int k = 0; k < ITEMS; ++k) {
             const uint32_t slot = base + (uint32_t)(k * kBlock) + threadIdx.x;
-            d[k] = slot < n ? fr.dir[slot] : kInactive;
-        }
-        bool full[ITEMS];
-        if (!FP32) {
-            double w[ITEMS], fill[ITEMS];  // w: cached inc, or vel when the increment is stale
-#pragma unroll
-            for (int k = 0; k < ITEMS; ++k) {
-                const uint32_t slot = base + (uint32_t)(k * kBlock) + threadIdx.x;
-                w[k] = -1.0; fill[k] = 0.0;
-                if (d[k] != kInactive) {
-                    if (REFRESH) {
-                        const uint32_t g = fr.defg[slot];
-                        const double P = __longlong_as_double((long long)a.ptab[(unsigned long long)fr.rxg[slot] * a.ndefg + g]);
-                        w[k] = velocity_factor(a, P, g, d[k] & kCodeMask);
-                        ((double*)fr.vel)[slot] = w[k];
-                    } else if (a.dt_changed || (d[k] & kStale)) {
-                        w[k] = ((const double*)fr.vel)[slot];
-                    } else {
-                        w[k] = fr.inc[slot];
-                    }
-                    fill[k] = ((const double*)fr.fill)[slot];
+            w[k] = -1.0; fill[k] = 0.0;
+            if (d[k] != kInactive) {
+                if (REFRESH) {
+                    const uint32_t g = fr.defg[slot];
+                    const double P = __longlong_as_double((long long)a.ptab[(unsigned long long)fr.rxg[slot] * a.ndefg + g]);
+                    w[k] = velocity_factor(a, P, g, d[k] & kCodeMask);
+                    ((double*)fr.vel)[slot] = w[k];
+                } else if (a.dt_changed || (d[k] & kStale)) {
+                    w[k] = ((const double*)fr.vel)[slot];
+                } else {
+                    w[k] = fr.inc[slot];
                 }
-            }
-#pragma unroll
-            for (int k = 0; k < ITEMS; ++k) {
-                full[k] = false;
-                if (d[k] != kInactive) {
-                    ++sv;
-                    const uint32_t slot = base + (uint32_t)(k * kBlock) + threadIdx.x;
-                    double inc = w[k];
-                    if (REFRESH || a.dt_changed || (d[k] & kStale)) {
-                        if (__double_as_longlong(w[k]) >= 0) inc = __dmul_rn(__dmul_rn(w[k], a.dt), a.cinv);
-                        fr.inc[slot] = inc;
-                        if (d[k] & kStale) fr.dir[slot] = d[k] & kCodeMask;
-                    }
-                    if (__double_as_longlong(inc) >= 0) {  // sign bit clear: driving force present
-                        const double f = __dadd_rn(fill[k], inc);
-                        ((double*)fr.fill)[slot] = f;
-                        full[k] = __double_as_longlong(f) >= 0x3FF0000000000000ll;  // f >= 1.0, f never negative
-                    }
-                }
-            }
-        } else {
-            float vel[ITEMS], fill[ITEMS], comp[ITEMS];
-#pragma unroll
-            for (int k = 0; k < ITEMS; ++k) {
-                const uint32_t slot = base + (uint32_t)(k * kBlock) + threadIdx.x;
-                vel[k] = -1.0f; fill[k] = 0.0f; comp[k] = 0.0f;
-                if (d[k] != kInactive) {
-                    if (REFRESH) {
-                        const uint32_t g = fr.defg[slot];
-                        const double P = __longlong_as_double((long long)a.ptab[(unsigned long long)fr.rxg[slot] * a.ndefg + g]);
-                        vel[k] = (float)velocity_factor(a, P, g, d[k] & kCodeMask);
-                        ((float*)fr.vel)[slot] = vel[k];
-                    } else {
-                        vel[k] = ((const float*)fr.vel)[slot];
-                    }
-                    fill[k] = ((const float*)fr.fill)[slot];
-                    comp[k] = fr.comp[slot];
-                }
-            }
-#pragma unroll
-            for (int k = 0; k < ITEMS; ++k) {
-                full[k] = false;
-                if (d[k] != kInactive) {
-                    ++sv;
-                    if (vel[k] >= 0.0f) {
-                        // Kahan-compensated accumulation of the fill
-                        const float inc = vel[k] * a.dtc32;
-                        const float y = inc - comp[k];
-                        const float t = fill[k] + y;
-                        const float c = (t - fill[k]) - y;
-                        const uint32_t slot = base + (uint32_t)(k * kBlock) + threadIdx.x;
-                        ((float*)fr.fill)[slot] = t;
-                        fr.comp[slot] = c;
-                        full[k] = (t - c) >= 1.0f;
-                    }
-                }
+                fill[k] = ((const double*)fr.fill)[slot];
             }
         }
-        uint32_t cf = 0, ci = 0;
 #pragma unroll
         for (int k = 0; k < ITEMS; ++k) {
-            const uint32_t fm = __ballot_sync(0xFFFFFFFFu, full[k]);
-            const uint32_t im = __ballot_sync(0xFFFFFFFFu, d[k] == kInactive && base + (uint32_t)(k * kBlock) + threadIdx.x < n);
-            if (lane == 0) {
-                const uint32_t word = tile * (kGrowTile / 32) + (uint32_t)(k * kWarps + warp);  // slots 32 word .. 32 word + 31
-                fr.fmask[word] = fm;
-                fr.imask[word] = im;
+            full[k] = false;
+            if (d[k] != kInactive) {
+                ++sv;
+                const uint32_t slot = base + (uint32_t)(k * kBlock) + threadIdx.x;
+                double inc = w[k];
+                if (REFRESH || a.dt_changed || (d[k] & kStale)) {
+                    if (__double_as_longlong(w[k]) >= 0) inc = __dmul_rn(__dmul_rn(w[k], a.dt), a.cinv);
+                    fr.inc[slot] = inc;
+                    if (d[k] & kStale) fr.dir[slot] = d[k] & kCodeMask;
+                }
+                if (__double_as_longlong(inc) >= 0) {  // sign bit clear: driving force present
+                    const double f = __dadd_rn(fill[k], inc);
+                    ((double*)fr.fill)[slot] = f;
+                    full[k] = __double_as_longlong(f) >= 0x3FF0000000000000ll;  // f >= 1.0, f never negative
+                }
             }
-            cf += __popc(fm);
-            ci += __popc(im);
         }
-        if (lane == 0) { s_f[warp] = cf; s_i[warp] = ci; }
-        __syncthreads();
-        if (threadIdx.x == 0) {
-            uint32_t tf = 0, ti = 0;
+    } else {
+        float vel[ITEMS], fill[ITEMS], comp[ITEMS];
 #pragma unroll
-            for (int w = 0; w < kWarps; ++w) { tf += s_f[w]; ti += s_i[w]; }
-            fr.tcnt[2 * tile] = tf;
-            fr.tcnt[2 * tile + 1] = ti;
+        for (int k = 0; k < ITEMS; ++k) {
+            const uint32_t slot = base + (uint32_t)(k * kBlock) + threadIdx.x;
+            vel[k] = -1.0f; fill[k] = 0.0f; comp[k] = 0.0f;
+            if (d[k] != kInactive) {
+                if (REFRESH) {
+                    const uint32_t g = fr.defg[slot];
+                    const double P = __longlong_as_double((long long)a.ptab[(unsigned long long)fr.rxg[slot] * a.ndefg + g]);
+                    vel[k] = (float)velocity_factor(a, P, g, d[k] & kCodeMask);
+                    ((float*)fr.vel)[slot] = vel[k];
+                } else {
+                    vel[k] = ((const float*)fr.vel)[slot];
+                }
+                fill[k] = ((const float*)fr.fill)[slot];
+                comp[k] = fr.comp[slot];
+            }
         }
-        __syncthreads();
+#pragma unroll
+        for (int k = 0; k < ITEMS; ++k) {
+            full[k] = false;
+            if (d[k] != kInactive) {
+                ++sv;
+                const uint32_t slot = base + (uint32_t)(k * kBlock) + threadIdx.x;
+                if (d[k] & kStale) fr.dir[slot] = d[k] & kCodeMask;
+                if (vel[k] >= 0.0f) {
+                    // Kahan-compensated accumulation of the fill
+                    const float inc = vel[k] * a.dtc32;
+                    const float y = inc - comp[k];
+                    const float t = fill[k] + y;
+                    const float c = (t - fill[k]) - y;
+                    ((float*)fr.fill)[slot] = t;
+                    fr.comp[slot] = c;
+                    full[k] = (t - c) >= 1.0f;
+                }
+            }
+        }
     }
+    uint32_t cf = 0, ci = 0;
 #pragma unroll
-    for (int o = 16; o > 0; o >>= 1) sv += __shfl_down_sync(0xFFFFFFFFu, sv, o);
-    if (lane == 0 && sv) atomicAdd(&a.st->sv[L], sv);
+    for (int k = 0; k < ITEMS; ++k) {
+        const uint32_t fm = __ballot_sync(0xFFFFFFFFu, full[k]);
+        const uint32_t im = __ballot_sync(0xFFFFFFFFu, d[k] == kInactive && base + (uint32_t)(k * kBlock) + threadIdx.x < n);
+        if (lane == 0) {
+            const uint32_t word = tile * S::kWords + (uint32_t)(k * kWarps + warp);  // slots 32 word .. 32 word + 31
+            fr.fmask[word] = fm;
+            fr.imask[word] = im;
+        }
+        cf += __popc(fm);
+        ci += __popc(im);
+    }
+    if (lane == 0) { s_f[warp] = cf; s_i[warp] = ci; }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        uint32_t tf = 0, ti = 0;
+#pragma unroll
+        for (int w = 0; w < kWarps; ++w) { tf += s_f[w]; ti += s_i[w]; }
+        fr.tcnt[2 * tile] = tf;
+        fr.tcnt[2 * tile + 1] = ti;
+        if (tf) atomicAdd(&fr.scnt[2 * (tile / kSuper)], tf);
+        if (ti) atomicAdd(&fr.scnt[2 * (tile / kSuper) + 1], ti);
+    }
+    __syncthreads();
+    return sv;
 }
+
+// warp-summed Sv share into the domain's counter (one atomic per warp and segment)
+__device__ __forceinline__ void flush_sv(const DomainArgs& a, int L, uint32_t sv) {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) sv += __shfl_xor_sync(0xFFFFFFFFu, sv, o);
+    if ((threadIdx.x & 31) == 0 && sv) atomicAdd(&a.st->sv[L], (unsigned long long)sv);
+}
+
+// slots of list L of a domain this step ( 0 for a domain that is not stepping)
+__device__ __forceinline__ uint32_t list_slots(const DomainArgs& a, int L) { return a.active ? a.st->next_never[L] : 0u; }
+
+template <bool FP32, int ITEMS>
+__global__ void __launch_bounds__(kBlock, ITEMS >= 16 ? 2 : 4) k_grow_fill(int base, int ndom) {
+    using S = GrowShape<ITEMS>;
+    __shared__ uint32_t s_pre[kMaxSegs + 1];
+    __shared__ uint32_t s_f[kWarps], s_i[kWarps];
+    const int nseg = 2 * ndom;
+    const uint32_t total = seg_prefix(s_pre, nseg, [&](int s) {
+        return (list_slots(c_args[base + (s >> 1)], s & 1) + S::kTile - 1) / S::kTile;
+    });
+    int cur = -1;       // segment whose Sv share is being accumulated
+    uint32_t sv = 0;
+    for (uint32_t u = blockIdx.x; u < total; u += gridDim.x) {
+        const int s = seg_find(s_pre, nseg, u);
+        if (s != cur) {
+            if (cur >= 0) flush_sv(c_args[base + (cur >> 1)], cur & 1, sv);
+            cur = s;
+            sv = 0;
+        }
+        const DomainArgs& a = c_args[base + (s >> 1)];
+        const int L = s & 1;
+        const uint32_t tile = u - s_pre[s];
+        const uint32_t n = a.st->next_never[L];
+        if (a.refresh) sv += grow_tile<FP32, true, ITEMS>(a, L, tile, n, s_f, s_i);
+        else sv += grow_tile<FP32, false, ITEMS>(a, L, tile, n, s_f, s_i);
+    }
+    if (cur >= 0) flush_sv(c_args[base + (cur >> 1)], cur & 1, sv);
+}
+
+// one warp per grow tile
+template <int ITEMS>
+__global__ void __launch_bounds__(kBlock) k_grow_lists(int base, int ndom) {
+    using S = GrowShape<ITEMS>;
+    constexpr int WPL = (int)S::kWords / 32;  // mask words per lane
+    __shared__ uint32_t s_pre[kMaxSegs + 1];
+    const int nseg = 2 * ndom;
+    const uint32_t total = seg_prefix(s_pre, nseg, [&](int s) {
+        return (list_slots(c_args[base + (s >> 1)], s & 1) + S::kTile - 1) / S::kTile;
+    });
+    const int lane = threadIdx.x & 31;
+    const uint32_t lt = lanemask_lt();
+    const uint32_t nw = (gridDim.x * blockDim.x) >> 5;
+    for (uint32_t u = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; u < total; u += nw) {
+        const int s = seg_find(s_pre, nseg, u);
+        const DomainArgs& a = c_args[base + (s >> 1)];
+        const int L = s & 1;
+        const DFront& fr = a.f[L];
+        const uint32_t tile = u - s_pre[s];
+        uint32_t rf, ri;
+        tile_prefix(fr.tcnt, fr.scnt, tile, rf, ri);
+        uint32_t fw[WPL], iw[WPL];
+#pragma unroll
+        for (int h = 0; h < WPL; ++h) {
+            fw[h] = fr.fmask[tile * S::kWords + (uint32_t)(32 * h + lane)];
+            iw[h] = fr.imask[tile * S::kWords + (uint32_t)(32 * h + lane)];
+        }
+        const uint32_t reccap = fr.reccap;
+#pragma unroll
+        for (int h = 0; h < WPL; ++h) {
+            // word 32h + j covers slots base + 32 (32h + j) .. + 31; lane j of the loop below
+            // owns bit `lane` of word 32h + j
+            uint32_t cf = __popc(fw[h]), ci = __popc(iw[h]);
+            uint32_t xf = cf, xi = ci;
+#pragma unroll
+            for (int o = 1; o < 32; o <<= 1) {
+                const uint32_t p = __shfl_up_sync(0xFFFFFFFFu, xf, o), q = __shfl_up_sync(0xFFFFFFFFu, xi, o);
+                if (lane >= o) { xf += p; xi += q; }
+            }
+            const uint32_t ef = rf + xf - cf, ei = ri + xi - ci;  // exclusive rank of the word's first bit
+            for (int j = 0; j < 32; ++j) {
+                const uint32_t wf = __shfl_sync(0xFFFFFFFFu, fw[h], j), wi = __shfl_sync(0xFFFFFFFFu, iw[h], j);
+                const uint32_t bf = __shfl_sync(0xFFFFFFFFu, ef, j), bi = __shfl_sync(0xFFFFFFFFu, ei, j);
+                const uint32_t slot = tile * S::kTile + 32u * (uint32_t)(32 * h + j) + (uint32_t)lane;
+                if ((wf >> lane) & 1u) fr.full[bf + __popc(wf & lt)] = slot;
+                if ((wi >> lane) & 1u) {
+                    const uint32_t r = bi + __popc(wi & lt);
+                    if (r < reccap) fr.recyc[r] = slot;
+                }
+            }
+            rf += __shfl_sync(0xFFFFFFFFu, xf, 31);
+            ri += __shfl_sync(0xFFFFFFFFu, xi, 31);
+        }
+        if (tile + 1 == s_pre[s + 1] - s_pre[s] && lane == 0) {  // the list's last tile: totals
+            a.st->nfull[L] = rf;
+            a.st->ninactive[L] = ri;
+            a.st->nrec[L] = min(ri, reccap);
+        }
+    }
+}
+
+constexpr int kGrowItems = 8;                        // tile shape of the defragmentation passes
+constexpr uint32_t kGrowTile = kBlock * kGrowItems;
 
 // In-place exclusive scan of `ntiles` (a, b) count pairs by one block of 1024 threads;
 // returns the totals in thread 0.
@@ -363,58 +558,6 @@ __device__ __forceinline__ void scan_pairs_block(uint32_t* cnt, uint32_t ntiles,
     totB = s_carry[1];
 }
 
-// block L scans the grow tile counts of list L; blocks 2 scans the commit tiles
-template <int KIND>
-__global__ void __launch_bounds__(1024) k_scan_tiles(DomainArgs a) {
-    uint32_t tA, tB;
-    if (KIND == 0) {
-        const int L = blockIdx.x;
-        const uint32_t n = a.st->next_never[L];
-        scan_pairs_block(a.f[L].tcnt, (n + kGrowTile - 1) / kGrowTile, tA, tB);
-        if (threadIdx.x == 0) {
-            a.st->nfull[L] = tA;
-            a.st->ninactive[L] = tB;
-            a.st->nrec[L] = min(tB, a.f[L].reccap);
-        }
-    } else {
-        const uint32_t F = a.st->nfull[0] + a.st->nfull[1];
-        scan_pairs_block(a.ctcnt, (F + kBlock - 1) / kBlock, tA, tB);
-        if (threadIdx.x == 0) { a.st->nwin[0] = tA; a.st->nwin[1] = tB; }
-    }
-}
-
-// one warp per grow tile: lane l owns mask words 2l and 2l+1 of the tile
-__global__ void __launch_bounds__(kBlock) k_grow_lists(DomainArgs a) {
-    const int L = blockIdx.y;
-    const DFront fr = a.f[L];
-    const uint32_t n = a.st->next_never[L];
-    const uint32_t ntiles = (n + kGrowTile - 1) / kGrowTile;
-    const int lane = threadIdx.x & 31;
-    const uint32_t gw = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, nw = (gridDim.x * blockDim.x) >> 5;
-    const uint32_t lt = lanemask_lt();
-    for (uint32_t tile = gw; tile < ntiles; tile += nw) {
-        const uint32_t w0 = tile * (kGrowTile / 32) + 2 * lane;
-        const uint32_t f0 = fr.fmask[w0], f1 = fr.fmask[w0 + 1], i0 = fr.imask[w0], i1 = fr.imask[w0 + 1];
-        const uint32_t cf = __popc(f0) + __popc(f1), ci = __popc(i0) + __popc(i1);
-        uint32_t xf = cf, xi = ci;
-#pragma unroll
-        for (int o = 1; o < 32; o <<= 1) {
-            const uint32_t a1 = __shfl_up_sync(0xFFFFFFFFu, xf, o), b1 = __shfl_up_sync(0xFFFFFFFFu, xi, o);
-            if (lane >= o) { xf += a1; xi += b1; }
-        }
-        uint32_t rf = fr.tcnt[2 * tile] + xf - cf, ri = fr.tcnt[2 * tile + 1] + xi - ci;
-        (void)lt;
-        const uint32_t words[2][2] = {{f0, f1}, {i0, i1}};
-        for (int h = 0; h < 2; ++h) {
-            const uint32_t sbase = (w0 + h) * 32;
-            uint32_t m = words[0][h];
-            while (m) { const int b = __ffs(m) - 1; m &= m - 1; fr.full[rf++] = sbase + b; }
-            m = words[1][h];
-            while (m && ri < fr.reccap) { const int b = __ffs(m) - 1; m &= m - 1; fr.recyc[ri++] = sbase + b; }
-        }
-    }
-}
-
 // ------------------------------------------------------------------ K2 claim
 // Attempts LO..HI-1 of one full cell: the grid loads are all issued before the atomics
 // (claims are a min, so the order of the atomics does not matter).  Inside cells are
@@ -428,7 +571,7 @@ __device__ __forceinline__ uint32_t claim_plane(const DomainArgs& a, uint32_t ce
         gv[k] = 0xFFFFFFFFu;
         if (INSIDE) {
             tg[k] = cell + (uint32_t)a.noff[LO + k];
-            if (tg[k] < a.ncells) gv[k] = a.grid[tg[k]];
+            if (tg[k] < a.ncells) gv[k] = a.grid[tg[k]];  // not __ldg: stays behind the previous plane's atomics
             else atomicOr(&a.st->err, kErrBounds);
         } else {
             bool inter;
@@ -446,13 +589,26 @@ __device__ __forceinline__ uint32_t claim_plane(const DomainArgs& a, uint32_t ce
     return mask;
 }
 
-__global__ void __launch_bounds__(kBlock, 4) k_claim(DomainArgs a) {
-    const uint32_t F0 = a.st->nfull[0], F = F0 + a.st->nfull[1];
-    if (26ull * F >= 0xFFFFFFFFull) {
-        if (blockIdx.x == 0 && threadIdx.x == 0) atomicOr(&a.st->err, kErrKeyLimit);
-        return;
-    }
-    for (uint32_t f = blockIdx.x * blockDim.x + threadIdx.x; f < F; f += gridDim.x * blockDim.x) {
+// full cells of a domain this step (Inside list first); 0 when the 32-bit attempt
+// ordinal 26 f + d could overflow (flagged)
+__device__ __forceinline__ uint32_t full_cells(const DomainArgs& a) {
+    if (!a.active) return 0u;
+    const uint32_t F = a.st->nfull[0] + a.st->nfull[1];
+    return 26ull * F >= 0xFFFFFFFFull ? 0u : F;
+}
+
+__global__ void __launch_bounds__(kBlock, 4) k_claim(int base, int ndom) {
+    __shared__ uint32_t s_pre[kMaxSegs + 1];
+    const uint32_t total = seg_prefix(s_pre, ndom, [&](int s) {
+        const DomainArgs& a = c_args[base + (s)];
+        if (a.active && 26ull * (a.st->nfull[0] + a.st->nfull[1]) >= 0xFFFFFFFFull) atomicOr(&a.st->err, kErrKeyLimit);
+        return full_cells(a);
+    });
+    for (uint32_t u = blockIdx.x * blockDim.x + threadIdx.x; u < total; u += gridDim.x * blockDim.x) {
+        const int s = seg_find(s_pre, ndom, u);
+        const DomainArgs& a = c_args[base + (s)];
+        const uint32_t f = u - s_pre[s];
+        const uint32_t F0 = a.st->nfull[0];
         uint32_t mask;
         if (f < F0) {
             const uint32_t cell = a.f[0].xyz[a.f[0].full[f]];
@@ -580,29 +736,34 @@ __device__ __forceinline__ bool lookup_p(const DomainArgs& a, uint32_t rxg, uint
 }
 
 // ------------------------------------------------------------------ K3 commit (+ finalize)
-// k_resolve: one thread per full cell (tiles of kBlock full cells, grid-stride): its
-// attempts whose claim holds the own ordinal won; writes the win mask, the mask of wins
-// that go to the Border list, and the tile's two win counts.
-// k_commit (after k_scan_tiles<1>): winners are ranked per destination list in
-// full-cell then direction order and take recycled slots first, then appended slots,
-// like omp_getNextFreeSlotInRXFront*(CELLRECYCLE); the full cell then becomes
-// recrystallized (grid = ndefg + rxg, counts, slot INACTIVE).
-__global__ void __launch_bounds__(kBlock, 4) k_resolve(DomainArgs a) {
-    const uint32_t F0 = a.st->nfull[0], F = F0 + a.st->nfull[1];
-    if (26ull * F >= 0xFFFFFFFFull) return;
-    const uint32_t ntiles = (F + kBlock - 1) / kBlock;
+// k_resolve: one thread per full cell, tiles of kBlock full cells: its attempts whose
+// claim holds the own ordinal won; writes the win mask, the mask of wins that go to
+// the Border list, the tile's two win counts and adds them to its supertile.
+// k_commit: winners are ranked per destination list in full-cell then direction
+// order (tile prefix from the supertile and tile counts) and take recycled slots
+// first, then appended slots, like omp_getNextFreeSlotInRXFront*(CELLRECYCLE); the
+// full cell then becomes recrystallized (grid = ndefg + rxg, counts, slot INACTIVE).
+__device__ __forceinline__ uint32_t commit_tiles(const DomainArgs& a) { return (full_cells(a) + kBlock - 1) / kBlock; }
+
+__global__ void __launch_bounds__(kBlock, 4) k_resolve(int base, int ndom) {
+    __shared__ uint32_t s_pre[kMaxSegs + 1];
     __shared__ uint32_t s_a[kWarps], s_b[kWarps];
+    const uint32_t total = seg_prefix(s_pre, ndom, [&](int s) { return commit_tiles(c_args[base + (s)]); });
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    for (uint32_t tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
+    for (uint32_t u = blockIdx.x; u < total; u += gridDim.x) {
+        const int s = seg_find(s_pre, ndom, u);
+        const DomainArgs& a = c_args[base + (s)];
+        const uint32_t tile = u - s_pre[s];
+        const uint32_t F0 = a.st->nfull[0], F = F0 + a.st->nfull[1];
         const uint32_t f = tile * kBlock + threadIdx.x;
         uint32_t win = 0, tob = 0;
         if (f < F) {
             const uint32_t mask = a.amask[f];
             if (mask) {
                 const int L = f >= F0 ? 1 : 0;
-                const uint32_t slot = a.f[L].full[L ? f - F0 : f];
+                const uint32_t cell = a.f[L].xyz[a.f[L].full[L ? f - F0 : f]];
                 int x, y, z;
-                decode(a, a.f[L].xyz[slot], x, y, z);
+                decode(a, cell, x, y, z);
                 const bool allB = (L == 0) && !(x > 1 && x < (int)a.nx - 2 && y > 1 && y < (int)a.ny - 2 && z > 1 && z < (int)a.nz - 2);
                 uint32_t cl[26];
                 uint32_t inter_m = 0;
@@ -641,20 +802,30 @@ __global__ void __launch_bounds__(kBlock, 4) k_resolve(DomainArgs a) {
             for (int w = 0; w < kWarps; ++w) { ta += s_a[w]; tb += s_b[w]; }
             a.ctcnt[2 * tile] = ta;
             a.ctcnt[2 * tile + 1] = tb;
+            if (ta) atomicAdd(&a.csct[2 * (tile / kSuper)], ta);
+            if (tb) atomicAdd(&a.csct[2 * (tile / kSuper) + 1], tb);
         }
         __syncthreads();
     }
 }
 
 template <bool FP32>
-__global__ void __launch_bounds__(kBlock, 4) k_commit(DomainArgs a) {
-    const uint32_t F0 = a.st->nfull[0], F = F0 + a.st->nfull[1];
-    if (26ull * F >= 0xFFFFFFFFull) return;
-    const uint32_t ntiles = (F + kBlock - 1) / kBlock;
-    __shared__ uint32_t s_a[kWarps], s_b[kWarps];
+__global__ void __launch_bounds__(kBlock, 4) k_commit(int base, int ndom) {
+    __shared__ uint32_t s_pre[kMaxSegs + 1];
+    __shared__ uint32_t s_a[kWarps], s_b[kWarps], s_base[2];
+    const uint32_t total = seg_prefix(s_pre, ndom, [&](int s) { return commit_tiles(c_args[base + (s)]); });
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    for (uint32_t tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
+    for (uint32_t u = blockIdx.x; u < total; u += gridDim.x) {
+        const int s = seg_find(s_pre, ndom, u);
+        const DomainArgs& a = c_args[base + (s)];
+        const uint32_t tile = u - s_pre[s];
+        const uint32_t F0 = a.st->nfull[0], F = F0 + a.st->nfull[1];
         const uint32_t f = tile * kBlock + threadIdx.x;
+        if (warp == 0) {
+            uint32_t pa, pb;
+            tile_prefix(a.ctcnt, a.csct, tile, pa, pb);
+            if (lane == 0) { s_base[0] = pa; s_base[1] = pb; }
+        }
         const uint32_t win = f < F ? a.amask[f] : 0u, tob = f < F ? a.tobm[f] : 0u;
         const uint32_t cB = __popc(tob), cA = __popc(win) - cB;
         uint32_t iA = cA, iB = cB;
@@ -665,10 +836,17 @@ __global__ void __launch_bounds__(kBlock, 4) k_commit(DomainArgs a) {
         }
         if (lane == 31) { s_a[warp] = iA; s_b[warp] = iB; }
         __syncthreads();
-        uint32_t rA = a.ctcnt[2 * tile] + iA - cA, rB = a.ctcnt[2 * tile + 1] + iB - cB;
+        uint32_t rA = s_base[0] + iA - cA, rB = s_base[1] + iB - cB;
 #pragma unroll
         for (int w = 0; w < kWarps; ++w)
             if (w < warp) { rA += s_a[w]; rB += s_b[w]; }
+        if (threadIdx.x == 0 && tile + 1 == s_pre[s + 1] - s_pre[s]) {  // the domain's last tile: totals
+            uint32_t ta = 0, tb = 0;
+#pragma unroll
+            for (int w = 0; w < kWarps; ++w) { ta += s_a[w]; tb += s_b[w]; }
+            a.st->nwin[0] = s_base[0] + ta;
+            a.st->nwin[1] = s_base[1] + tb;
+        }
         if (f < F) {
             const int L = f >= F0 ? 1 : 0;
             const DFront& src = a.f[L];
@@ -734,10 +912,17 @@ __global__ void __launch_bounds__(kBlock, 4) k_commit(DomainArgs a) {
 // P(rxg, defg) from the table (classified on the device when exact, else requested
 // from the host: vel = -1 and the slot goes on the pending list) and the cached
 // velocity factor; the running P max over the new weights.
+__device__ __forceinline__ uint32_t new_cells(const DomainArgs& a) { return a.active ? a.st->nwin[0] + a.st->nwin[1] : 0u; }
+
 template <bool FP32>
-__global__ void __launch_bounds__(kBlock) k_new_vel(DomainArgs a) {
-    const uint32_t n0 = a.st->nwin[0], n = n0 + a.st->nwin[1];
-    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+__global__ void __launch_bounds__(kBlock, 4) k_new_vel(int base, int ndom) {
+    __shared__ uint32_t s_pre[kMaxSegs + 1];
+    const uint32_t total = seg_prefix(s_pre, ndom, [&](int s) { return new_cells(c_args[base + (s)]); });
+    for (uint32_t u = blockIdx.x * blockDim.x + threadIdx.x; u < total; u += gridDim.x * blockDim.x) {
+        const int s = seg_find(s_pre, ndom, u);
+        const DomainArgs& a = c_args[base + (s)];
+        const uint32_t i = u - s_pre[s];
+        const uint32_t n0 = a.st->nwin[0];
         const int D = i >= n0 ? 1 : 0;
         const uint32_t r = D ? i - n0 : i;
         const DFront& dst = a.f[D];
@@ -760,13 +945,13 @@ __global__ void __launch_bounds__(kBlock) k_new_vel(DomainArgs a) {
     }
 }
 
-// ------------------------------------------------------------------ K4 step end
+// ------------------------------------------------------------------ K4 step end, step start
 // Host mailbox in pinned, device-mapped memory: k_step_end writes the step's scalars,
 // the mobility-weight requests and the depleted grains straight into host memory, so
 // the host needs one stream synchronization per step and no copies; the host writes
-// the requested weights back into ans_* for k_fill_ptab.
-constexpr uint32_t kBoxMiss = 65536;
-constexpr uint32_t kBoxDep = 65536;
+// the requested weights back into ans_* for the next step's k_apply_answers.
+constexpr uint32_t kBoxMiss = 16384;
+constexpr uint32_t kBoxDep = 16384;
 struct HostBox {
     DevState snap;
     unsigned long long miss[kBoxMiss];
@@ -775,17 +960,24 @@ struct HostBox {
     double ans_val[kBoxMiss];
 };
 
-// Advances the high-water marks, posts the step to the mailbox and clears the
-// per-step fields for the next step.  One block.
-__global__ void __launch_bounds__(kBlock) k_step_end(DomainArgs a, HostBox* box) {
+// One block per domain: advances the high-water marks, posts the step to the domain's
+// mailbox, clears the supertile counters the step used and the per-step fields.
+__global__ void __launch_bounds__(kBlock) k_step_end(int base, int ndom, uint32_t grow_tile) {
+    const DomainArgs& a = c_args[base + (blockIdx.x)];
+    if (!a.active) return;
     DevState* st = a.st;
-    __shared__ uint32_t s_nm, s_nd;
+    HostBox* box = a.box;
+    __shared__ uint32_t s_nm, s_nd, s_sup[3];
     if (threadIdx.x == 0) {
+        const uint32_t F = st->nfull[0] + st->nfull[1];
+        for (int L = 0; L < 2; ++L) s_sup[L] = ((st->next_never[L] + grow_tile - 1) / grow_tile + kSuper - 1) / kSuper;
+        s_sup[2] = ((F + kBlock - 1) / kBlock + kSuper - 1) / kSuper;
         const uint32_t cap[2] = {a.f[0].cap, a.f[1].cap};
         for (int D = 0; D < 2; ++D) {
             if (st->nwin[D] > st->nrec[D]) st->next_never[D] += st->nwin[D] - st->nrec[D];
             if (st->next_never[D] > cap[D]) { st->next_never[D] = cap[D]; st->err |= kErrCapacity; }
         }
+        st->npend_prev = min(st->npending, a.pendcap);
         box->snap = *st;
         s_nm = min(min(st->nmiss, a.misscap), kBoxMiss);
         s_nd = min(min(st->ndepleted, a.ndefg), kBoxDep);
@@ -793,10 +985,49 @@ __global__ void __launch_bounds__(kBlock) k_step_end(DomainArgs a, HostBox* box)
     __syncthreads();
     for (uint32_t i = threadIdx.x; i < s_nm; i += blockDim.x) box->miss[i] = a.miss[i];
     for (uint32_t i = threadIdx.x; i < s_nd; i += blockDim.x) box->depleted[i] = a.depleted[i];
+    for (uint32_t i = threadIdx.x; i < 2 * s_sup[0]; i += blockDim.x) a.f[0].scnt[i] = 0u;
+    for (uint32_t i = threadIdx.x; i < 2 * s_sup[1]; i += blockDim.x) a.f[1].scnt[i] = 0u;
+    for (uint32_t i = threadIdx.x; i < 2 * s_sup[2]; i += blockDim.x) a.csct[i] = 0u;
     __syncthreads();
     if (threadIdx.x == 0) {
         char* p = (char*)st + kStepFieldsOffset;
         for (size_t i = 0; i < sizeof(DevState) - kStepFieldsOffset; ++i) p[i] = 0;
+    }
+}
+
+// Step start: the weights the host computed for last step's requests go into the
+// table (k_apply_answers), then the cells that waited for them get their velocity
+// factor (k_fix_pending), before any fill is updated.
+__device__ __forceinline__ uint32_t answers(const DomainArgs& a) { return a.active ? a.n_ans : 0u; }
+__device__ __forceinline__ uint32_t pending_cells(const DomainArgs& a) { return a.active ? a.st->npend_prev : 0u; }
+
+__global__ void __launch_bounds__(kBlock) k_apply_answers(int base, int ndom) {
+    __shared__ uint32_t s_pre[kMaxSegs + 1];
+    const uint32_t total = seg_prefix(s_pre, ndom, [&](int s) { return answers(c_args[base + (s)]); });
+    for (uint32_t u = blockIdx.x * blockDim.x + threadIdx.x; u < total; u += gridDim.x * blockDim.x) {
+        const int s = seg_find(s_pre, ndom, u);
+        const DomainArgs& a = c_args[base + (s)];
+        const uint32_t i = u - s_pre[s];
+        a.ptab[a.ans_idx[i]] = (unsigned long long)__double_as_longlong(a.ans_val[i]);
+    }
+}
+
+template <bool FP32>
+__global__ void __launch_bounds__(kBlock) k_fix_pending(int base, int ndom) {
+    __shared__ uint32_t s_pre[kMaxSegs + 1];
+    const uint32_t total = seg_prefix(s_pre, ndom, [&](int s) { return pending_cells(c_args[base + (s)]); });
+    for (uint32_t u = blockIdx.x * blockDim.x + threadIdx.x; u < total; u += gridDim.x * blockDim.x) {
+        const int s = seg_find(s_pre, ndom, u);
+        const DomainArgs& a = c_args[base + (s)];
+        const uint32_t e = a.pending[u - s_pre[s]];
+        const int D = (int)(e >> 31);
+        const uint32_t slot = e & 0x7FFFFFFFu;
+        const DFront& f = a.f[D];
+        const uint32_t g = f.defg[slot];
+        const double P = __longlong_as_double((long long)a.ptab[(unsigned long long)f.rxg[slot] * a.ndefg + g]);
+        const double v = velocity_factor(a, P, g, f.dir[slot] & kCodeMask);
+        if (!FP32) ((double*)f.vel)[slot] = v;
+        else ((float*)f.vel)[slot] = (float)v;
     }
 }
 

@@ -18,7 +18,7 @@ from pathlib import Path
 import numpy as np
 
 from . import _abi
-from ._abi import GenParams, Params, ScoreError, StepStats, Timing
+from ._abi import GenParams, Params, ScoreError, StepStats, Timing, Tune
 
 
 def _ptr(a: np.ndarray | None):
@@ -344,10 +344,141 @@ class GrowthMachine:
         self._check(self._lib.score_get_timing(self._ctx, C.byref(t)))
         return t
 
+    def tune(self) -> Tune:
+        t = Tune()
+        self._check(self._lib.score_get_tune(self._ctx, C.byref(t)))
+        return t
+
+    def set_tune(self, t: Tune | None = None, **kw) -> None:
+        """Launch configuration (items, *_blocks_per_sm, use_graph); results never depend on it."""
+        t = t or self.tune()
+        for k, v in kw.items():
+            setattr(t, k, v)
+        self._check(self._lib.score_set_tune(self._ctx, C.byref(t)))
+
+    def autotune(self, x_target: float = -1.0, max_steps: int = 0) -> Tune:
+        """Pick the fastest launch configuration on real steps; leaves the domain restarted
+        with its nuclei placed."""
+        t = Tune()
+        self._check(self._lib.score_autotune(self._ctx, x_target, max_steps, C.byref(t)))
+        return t
+
     def close(self) -> None:
         if self._ctx:
             self._lib.score_destroy(self._ctx)
             self._ctx = C.c_void_p()
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+# ---------------------------------------------------------------- batched ensemble
+class Batch:
+    """Many independent domains stepped together in one sequence of launches per step
+    (the reference's ensemble of solitary units, SCORE_Kernel.cpp:1640-1756)."""
+
+    def __init__(self, params: list[Params], device: int = 0):
+        self._lib = lib()
+        self._b = C.c_void_p()
+        arr = (Params * len(params))(*params)
+        s = self._lib.score_batch_create(C.byref(self._b), arr, len(params), device)
+        if s != _abi.OK:
+            raise ScoreError(s, self._lib.score_status_string(s).decode())
+        self.params = list(params)
+        self.domains: list[Domain | None] = [None] * len(params)
+        self._keep: dict[int, list] = {}
+
+    def __len__(self) -> int:
+        return len(self.params)
+
+    def _check(self, s: int) -> None:
+        if s != _abi.OK:
+            msg = self._lib.score_batch_last_error(self._b).decode() if self._b else ""
+            raise ScoreError(s, msg or self._lib.score_status_string(s).decode())
+
+    def load_domain(self, i: int, d: Domain, ptable: np.ndarray | None = None) -> None:
+        keep = [np.ascontiguousarray(x) for x in (d.grid, d.defg_quat, d.defg_rho0, d.rxg_quat, d.rxg_site, d.rxg_tincub)]
+        if ptable is not None:
+            keep.append(np.ascontiguousarray(ptable, dtype=np.float64))
+        g, dq, rho, rq, site, tinc = keep[:6]
+        self._check(self._lib.score_batch_load_domain(self._b, i, _ptr(g), _ptr(dq), _ptr(rho), d.ndefg, _ptr(rq), _ptr(site),
+                                                      _ptr(tinc), d.nrxg, _ptr(keep[6] if ptable is not None else None)))
+        self._keep[i] = keep
+        self.domains[i] = d
+
+    def restart(self) -> None:
+        self._check(self._lib.score_batch_restart(self._b))
+
+    def place_nuclei(self) -> None:
+        self._check(self._lib.score_batch_place_nuclei(self._b))
+
+    def run_until(self, x_target: float = -1.0, max_steps: int = 0) -> int:
+        n = C.c_uint32()
+        self._check(self._lib.score_batch_run_until(self._b, x_target, max_steps, C.byref(n)))
+        return n.value
+
+    def trace(self, i: int) -> list[StepStats]:
+        n = C.c_uint32()
+        self._check(self._lib.score_batch_trace(self._b, i, None, 0, C.byref(n)))
+        buf = (StepStats * max(1, n.value))()
+        self._check(self._lib.score_batch_trace(self._b, i, buf, n.value, C.byref(n)))
+        return list(buf[: n.value])
+
+    def stats(self, i: int) -> StepStats:
+        st = StepStats()
+        self._check(self._lib.score_batch_get_stats(self._b, i, C.byref(st)))
+        return st
+
+    def labels(self, i: int, out: np.ndarray | None = None) -> np.ndarray:
+        d = self.domains[i]
+        if out is None:
+            out = np.empty((d.nz, d.ny, d.nx), dtype=np.uint32)
+        self._check(self._lib.score_batch_export_labels(self._b, i, _ptr(out)))
+        return out
+
+    def grain_counts(self, i: int) -> tuple[np.ndarray, np.ndarray]:
+        d = self.domains[i]
+        r = np.empty(d.nrxg, dtype=np.uint32)
+        g = np.empty(d.ndefg, dtype=np.uint32)
+        self._check(self._lib.score_batch_grain_counts(self._b, i, _ptr(r), _ptr(g)))
+        return r, g
+
+    def timing(self) -> Timing:
+        t = Timing()
+        self._check(self._lib.score_batch_get_timing(self._b, C.byref(t)))
+        return t
+
+    def tune(self) -> Tune:
+        t = Tune()
+        self._check(self._lib.score_batch_get_tune(self._b, C.byref(t)))
+        return t
+
+    def set_tune(self, t: Tune | None = None, **kw) -> None:
+        t = t or self.tune()
+        for k, v in kw.items():
+            setattr(t, k, v)
+        self._check(self._lib.score_batch_set_tune(self._b, C.byref(t)))
+
+    def autotune(self, x_target: float = -1.0, max_steps: int = 0) -> Tune:
+        """Fastest launch configuration on real steps; leaves the batch restarted with its
+        nuclei placed."""
+        t = Tune()
+        self._check(self._lib.score_batch_autotune(self._b, x_target, max_steps, C.byref(t)))
+        return t
+
+    def close(self) -> None:
+        if self._b:
+            self._lib.score_batch_destroy(self._b)
+            self._b = C.c_void_p()
 
     def __enter__(self):
         return self
