@@ -11,11 +11,16 @@ until X > 0.99.  Inputs are synthetic and seeded (rank r uses seed r).
           timed with CUDA events on the library's stream, max over ranks.
   e2e     same metric through the C ABI from pinned host buffers: every run
           copies the domain in (score_load_domain) and the labels out.
-  roofline  grow kernel (the dominant kernel): algorithmic bytes (29 B per FP64
-          front-cell update) / its event-timed duration, against the measured
-          HBM copy bandwidth.
+  roofline  k_grow_fill (the dominant kernel): algorithmic bytes (25 B per FP64
+          front-cell update: infector byte, cached increment, fill read and write;
+          17 B FP32+Kahan) / its event-timed duration, against the measured HBM
+          copy bandwidth.
   cpu_baseline  the C oracle (single thread) on a bounded 256^3 sample of the
           same workload (same grain and nucleus densities), run to X > 0.99.
+
+`--workload batch` times the batched ensemble instead (64 domains, edges uniform in
+[64, 256] per axis), `--precision 1` the FP32+Kahan fill (with its error against the
+FP64 path), `--autotune` picks the launch configuration first.
 
 `--impl reference` times the reference's CPU path instead: the oracle port (the
 SCORE reference cannot be compiled on this host) as independent same-density
@@ -222,14 +227,196 @@ def run_reference_arm(args) -> None:
     print(json.dumps(line), flush=True)
 
 
+class PlainWorkload:
+    """One cubic domain through GrowthMachine (the headline workload at --edge 512)."""
+
+    def __init__(self, sg, args, rank, local):
+        n = args.edge
+        f = (n / N_EDGE) ** 3
+        self.n, self.ngr, self.nnuc = n, max(1, round(N_GRAINS * f)), max(1, round(N_NUCLEI * f))
+        self.d = sg.generate_domain(n, n, n, self.ngr, self.nnuc, seed=rank)
+        self.p = read_params(n, args.precision)
+        self.sg = sg
+        self.gm = sg.GrowthMachine(self.p, device=local)
+        self.gm.load_domain(self.d)
+        self.tuned = self.gm.autotune(X_TARGET) if args.autotune else None
+        self.misses = None
+
+    def run(self):
+        gm = self.gm
+        gm.restart()
+        gm.place_nuclei()
+        tr = gm.run_until(X_TARGET)
+        self.misses = sum(s.p_misses for s in tr)
+        self.last_trace = tr
+        return sum(s.Sv for s in tr), len(tr), gm.timing()
+
+    def launches(self):
+        return self.gm.timing().kernel_launches
+
+    def e2e(self, runs):
+        sg, d, n = self.sg, self.d, self.n
+        pin = [pinned_copy(x) for x in (d.grid, d.defg_quat, d.defg_rho0, d.rxg_quat, d.rxg_site, d.rxg_tincub)]
+        pd = sg.Domain(n, n, n, *pin)
+        lab = pinned_copy(np.empty((n, n, n), dtype=np.uint32))
+        gm = self.gm
+
+        def once():
+            gm.load_domain(pd)
+            gm.place_nuclei()
+            tr = gm.run_until(X_TARGET)
+            gm.labels(lab)
+            return sum(s.Sv for s in tr)
+        once()
+        t0 = time.perf_counter()
+        sv = sum(once() for _ in range(runs))
+        return sv, time.perf_counter() - t0, sum(x.nbytes for x in pin), lab.nbytes
+
+    def fp32_error(self):
+        """FP32+Kahan against the FP64 path (bit-exact with the reference) on the same domain."""
+        lab32 = self.gm.labels()
+        x32 = np.array([s.X for s in self.last_trace])
+        p64 = self.sg.Params.from_buffer_copy(self.p)
+        p64.precision = 0
+        with self.sg.GrowthMachine(p64) as g64:
+            g64.load_domain(self.d)
+            g64.place_nuclei()
+            tr64 = g64.run_until(X_TARGET)
+            lab64 = g64.labels()
+        x64 = np.array([s.X for s in tr64])
+        m = min(len(x32), len(x64))
+        return label_error(lab32, lab64, x32[:m], x64[:m], self.d.ndefg)
+
+    def config(self):
+        return {"workload": WORKLOAD if self.n == N_EDGE else f"{self.n}^3 at the 512^3 workload's densities",
+                "cells": self.n ** 3, "grains": self.ngr, "nuclei": self.nnuc,
+                "l2": "inputs larger than L2 (grid alone 512 MiB)" if self.n >= 320 else "grid smaller than L2"}
+
+    def close(self):
+        self.gm.close()
+
+
+def batch_shapes(ndom: int):
+    """Batched-ensemble shapes: edges uniform in [64, 256] per axis, 100-5000 grains and
+    50-2000 nuclei per domain; domain i draws from seed i."""
+    out = []
+    for i in range(ndom):
+        r = np.random.default_rng(i)
+        nx, ny, nz = (int(v) for v in r.integers(64, 257, size=3))
+        out.append((nx, ny, nz, int(r.integers(100, 5001)), int(r.integers(50, 2001)), i))
+    return out
+
+
+class BatchWorkload:
+    """64 independent domains of uneven sizes stepped together (score_batch_*)."""
+
+    def __init__(self, sg, args, rank, local):
+        self.sg = sg
+        self.shapes = batch_shapes(args.domains)
+        self.doms, params = [], []
+        with tempfile.TemporaryDirectory() as td:
+            for k, (nx, ny, nz, ng, nn, seed) in enumerate(self.shapes):
+                params.append(sg.read_uds(sg.UdsSpec(nx=nx, ny=ny, nz=nz, precision=args.precision).write(Path(td) / f"{k}.uds")))
+                self.doms.append(sg.generate_domain(nx, ny, nz, ng, nn, seed=seed + 1000 * rank))
+        self.params = params
+        self.b = sg.Batch(params, device=local)
+        for k, d in enumerate(self.doms):
+            self.b.load_domain(k, d)
+        self.tuned = self.b.autotune(X_TARGET) if args.autotune else None
+        self.misses = None
+
+    def run(self):
+        b = self.b
+        b.restart()
+        b.place_nuclei()
+        steps = b.run_until(X_TARGET)
+        traces = [b.trace(k) for k in range(len(self.doms))]
+        self.last_traces = traces
+        self.misses = sum(s.p_misses for t in traces for s in t)
+        return sum(s.Sv for t in traces for s in t), steps, b.timing()
+
+    def launches(self):
+        return self.b.timing().kernel_launches
+
+    def e2e(self, runs):
+        sg, b = self.sg, self.b
+        pins, labs = [], []
+        for d in self.doms:
+            pin = [pinned_copy(x) for x in (d.grid, d.defg_quat, d.defg_rho0, d.rxg_quat, d.rxg_site, d.rxg_tincub)]
+            pins.append(sg.Domain(d.nx, d.ny, d.nz, *pin))
+            labs.append(pinned_copy(np.empty((d.nz, d.ny, d.nx), dtype=np.uint32)))
+
+        def once():
+            for k, pd in enumerate(pins):
+                b.load_domain(k, pd)
+            b.place_nuclei()
+            b.run_until(X_TARGET)
+            for k, lab in enumerate(labs):
+                b.labels(k, lab)
+            return sum(s.Sv for k in range(len(pins)) for s in b.trace(k))
+        once()
+        t0 = time.perf_counter()
+        sv = sum(once() for _ in range(runs))
+        h2d = sum(x.nbytes for pd in pins for x in (pd.grid, pd.defg_quat, pd.defg_rho0, pd.rxg_quat, pd.rxg_site, pd.rxg_tincub))
+        return sv, time.perf_counter() - t0, h2d, sum(lab.nbytes for lab in labs)
+
+    def fp32_error(self):
+        lab32 = [self.b.labels(k) for k in range(len(self.doms))]
+        self.b.close()  # the FP64 batch needs the device's argument slots
+        p64 = []
+        for p in self.params:
+            q = self.sg.Params.from_buffer_copy(p)
+            q.precision = 0
+            p64.append(q)
+        errs = []
+        with self.sg.Batch(p64) as b64:
+            for k, d in enumerate(self.doms):
+                b64.load_domain(k, d)
+            b64.place_nuclei()
+            b64.run_until(X_TARGET)
+            for k, d in enumerate(self.doms):
+                x32 = np.array([s.X for s in self.last_traces[k]])
+                x64 = np.array([s.X for s in b64.trace(k)])
+                m = min(len(x32), len(x64))
+                errs.append(label_error(lab32[k], b64.labels(k), x32[:m], x64[:m], d.ndefg))
+        return {"label_mismatch": max(e["label_mismatch"] for e in errs), "max_abs_dX": max(e["max_abs_dX"] for e in errs),
+                "mean_grain_size_rel_err": max(e["mean_grain_size_rel_err"] for e in errs), "aggregate": "max over domains"}
+
+    def config(self):
+        cells = sum(a * b * c for a, b, c, *_ in self.shapes)
+        return {"workload": f"batched ensemble: {len(self.shapes)} domains, edges uniform in [64,256] per axis, "
+                            f"100-5000 grains, 50-2000 nuclei, one launch sequence per step (CUDA graph)",
+                "domains": len(self.shapes), "cells": cells, "grains": sum(s[3] for s in self.shapes),
+                "nuclei": sum(s[4] for s in self.shapes), "l2": "inputs larger than L2"}
+
+    def close(self):
+        self.b.close()
+
+
+def label_error(lab32, lab64, x32, x64, ndefg):
+    """fraction of cells with a different final label, max |dX(t)|, relative error of the
+    mean recrystallized grain size (cells per recrystallized grain)."""
+    lab32, lab64 = lab32.ravel(), lab64.ravel()
+    def mean_size(lab):
+        rx = lab[lab >= ndefg]
+        return rx.size / max(1, np.unique(rx).size)
+    m64 = mean_size(lab64)
+    return {"label_mismatch": float(np.mean(lab32 != lab64)), "max_abs_dX": float(np.max(np.abs(x32 - x64))) if len(x32) else 0.0,
+            "mean_grain_size_rel_err": abs(mean_size(lab32) - m64) / m64 if m64 else 0.0}
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
     ap.add_argument("--steps", type=int, default=5)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--workload", default="plain", choices=["plain", "batch"],
+                    help="plain: one 512^3 domain (headline); batch: ensemble of uneven domains")
     ap.add_argument("--edge", type=int, default=N_EDGE)
+    ap.add_argument("--domains", type=int, default=64, help="batch workload: number of domains")
     ap.add_argument("--precision", type=int, default=0, help="0 FP64 (bit-exact), 1 FP32+Kahan")
+    ap.add_argument("--autotune", action="store_true", help="pick the launch configuration before timing")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true", help="skip the end-to-end runs (profiling captures)")
     args = ap.parse_args()
@@ -240,32 +427,18 @@ def main():
     dist = init_dist(world)
     import score_gb300 as sg
     sg.build()
-    n = args.edge
-    f = (n / N_EDGE) ** 3
-    ngr, nnuc = max(1, round(N_GRAINS * f)), max(1, round(N_NUCLEI * f))
-    d = sg.generate_domain(n, n, n, ngr, nnuc, seed=rank)
-    p = read_params(n, args.precision)
-    gm = sg.GrowthMachine(p, device=local)
-    gm.load_domain(d)
-
-    def one_run():
-        gm.restart()
-        gm.place_nuclei()
-        tr = gm.run_until(X_TARGET)
-        tm = gm.timing()
-        one_run.misses = sum(s.p_misses for s in tr)
-        return sum(s.Sv for s in tr), len(tr), tm
+    wl = (BatchWorkload if args.workload == "batch" else PlainWorkload)(sg, args, rank, local)
 
     for _ in range(args.warmup):
-        one_run()
+        wl.run()
     barrier(dist)
-    launches0 = gm.timing().kernel_launches
+    launches0 = wl.launches()
     tot_sv, tot_steps, run_ms, grow_bytes, grow_launches = 0, 0, 0.0, 0.0, 0
     phase = {"grow_ms": 0.0, "fill_ms": 0.0, "claim_ms": 0.0, "commit_ms": 0.0, "host_ms": 0.0, "wait_ms": 0.0,
-             "weights_ms": 0.0}
+             "weights_ms": 0.0, "pre_ms": 0.0, "post_ms": 0.0}
     with ClockSampler(local) as clk:
         for _ in range(args.steps):
-            sv, ns, tm = one_run()
+            sv, ns, tm = wl.run()
             tot_sv += sv
             tot_steps += ns
             run_ms += tm.run_ms
@@ -274,7 +447,7 @@ def main():
             for k in phase:
                 phase[k] += getattr(tm, k)
     fill_ms = phase["fill_ms"]
-    launches = gm.timing().kernel_launches - launches0
+    launches = wl.launches() - launches0
     barrier(dist)
     t_max = reduce_max(dist, run_ms / 1e3)
     sv_all = reduce_sum(dist, float(tot_sv))
@@ -283,29 +456,14 @@ def main():
     # end to end through the C ABI: pinned host inputs in, labels out, every run
     e_value, h2d, d2h = None, 0, 0
     if not args.no_e2e:
-        pin = [pinned_copy(x) for x in (d.grid, d.defg_quat, d.defg_rho0, d.rxg_quat, d.rxg_site, d.rxg_tincub)]
-        pd = sg.Domain(n, n, n, *pin)
-        lab = pinned_copy(np.empty((n, n, n), dtype=np.uint32))
-        h2d = sum(x.nbytes for x in pin)
-        d2h = lab.nbytes
-        e2e_runs = max(1, min(args.steps, 3))
-        gm.load_domain(pd)
-        gm.place_nuclei()
-        gm.run_until(X_TARGET)
-        gm.labels(lab)
+        runs = max(1, min(args.steps, 3))
         barrier(dist)
-        e_sv, t0 = 0, time.perf_counter()
-        for _ in range(e2e_runs):
-            gm.load_domain(pd)
-            gm.place_nuclei()
-            tr = gm.run_until(X_TARGET)
-            gm.labels(lab)
-            e_sv += sum(s.Sv for s in tr)
-        e_s = time.perf_counter() - t0
+        e_sv, e_s, h2d, d2h = wl.e2e(runs)
         barrier(dist)
         e_s = reduce_max(dist, e_s)
         e_value = reduce_sum(dist, float(e_sv)) / e_s
-    gm.close()
+    fp32_err = wl.fp32_error() if args.precision == 1 else None
+    wl.close()
 
     if rank == 0:
         peak, peak_kind = measured_peak_gbs()
@@ -313,22 +471,28 @@ def main():
         achieved = grow_bytes / (fill_ms / 1e3) / 1e9 if fill_ms > 0 else 0.0
         traffic = None
         tf = ROOT / "profiles" / "grow_traffic.json"
-        if tf.exists():
+        if tf.exists() and args.workload == "plain" and args.precision == 0:
             try:
                 tj = json.loads(tf.read_text())
                 traffic = tj["dram_bytes_per_update"] * (tot_sv / max(1, grow_launches))
             except Exception:
                 traffic = None
+        cfg = wl.config()
+        cfg.update({"growth_steps_per_run": tot_steps // args.steps, "updates_per_run": tot_sv // args.steps,
+                    "time_to_X099_ms": run_ms / args.steps, "parallelism": f"{world} independent ranks",
+                    "phase_ms_per_run": {k: v / args.steps for k, v in phase.items()},
+                    "host_weight_misses_per_run": wl.misses})
+        if wl.tuned is not None:
+            t = wl.tuned
+            cfg["autotuned"] = {"items": t.items, "fill_blocks_per_sm": t.fill_blocks_per_sm,
+                                "claim_blocks_per_sm": t.claim_blocks_per_sm, "commit_blocks_per_sm": t.commit_blocks_per_sm}
+        if fp32_err is not None:
+            cfg["fp32_error_vs_fp64"] = fp32_err
         line = {
             "metric": METRIC, "value": value, "unit": "updates/s", "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": run_ms / args.steps, "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "f64" if args.precision == 0 else "f32+kahan", "data": "synthetic",
-            "config": {"workload": WORKLOAD if n == N_EDGE else f"{n}^3 at the 512^3 workload's densities",
-                       "cells": n ** 3, "grains": ngr, "nuclei": nnuc, "growth_steps_per_run": tot_steps // args.steps,
-                       "updates_per_run": tot_sv // args.steps, "time_to_X099_ms": run_ms / args.steps,
-                       "l2": "inputs larger than L2 (grid alone 512 MiB)", "parallelism": f"{world} independent domains",
-                       "phase_ms_per_run": {k: v / args.steps for k, v in phase.items()},
-                       "host_weight_misses_per_run": getattr(one_run, "misses", None)},
+            "config": cfg,
             "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                          "frac": achieved / peak if peak else None, "traffic": traffic,
                          "kernel": "k_grow_fill", "bytes_per_update": bpu, "peak_source": f"{peak_kind} (MEASURED_PEAKS.json hbm_gbs)"},

@@ -199,6 +199,8 @@ typedef struct score_timing {
     double fill_ms;         /* the fill-update kernels alone (part of grow_ms) */
     double wait_ms;         /* host time blocked on the step's stream synchronization */
     double weights_ms;      /* host time computing requested mobility weights (libm FP64) */
+    double pre_ms;          /* host time before the launch (nucleation, arguments) */
+    double post_ms;         /* host wall time after the wait (mailboxes, weights, physics) */
 } score_timing;
 int  score_get_timing(score_ctx* ctx, score_timing* out);
 

@@ -72,7 +72,7 @@ class Timing(C.Structure):
     _fields_ = [
         ("total_ms", _d), ("grow_ms", _d), ("claim_ms", _d), ("commit_ms", _d), ("host_ms", _d),
         ("grow_launches", C.c_uint64), ("grow_bytes", _d), ("step_bytes", _d), ("kernel_launches", C.c_uint64),
-        ("run_ms", _d), ("fill_ms", _d), ("wait_ms", _d), ("weights_ms", _d),
+        ("run_ms", _d), ("fill_ms", _d), ("wait_ms", _d), ("weights_ms", _d), ("pre_ms", _d), ("post_ms", _d),
     ]
 
 

@@ -12,8 +12,10 @@ constexpr uint8_t kInactive = 0xFF;         // dir byte of an INACTIVE slot
 constexpr uint8_t kStale = 0x40;            // dir bit: cached fill increment not computed yet
 constexpr uint8_t kCodeMask = 0x3F;         // dir bits holding the infector code 0..26
 constexpr uint32_t kClaimFree = 0xFFFFFFFFu;
+constexpr uint8_t kPend = 0x80;             // dir bit: vel holds an answer tag, P comes from the host
 constexpr unsigned long long kPtabEmpty = 0xFFFFFFFFFFFFFFFFull;    // NaN bit pattern, never a weight
-constexpr unsigned long long kPtabPending = 0xFFFFFFFFFFFFFFFEull;  // requested from the host this step
+constexpr unsigned long long kPtabTag = 0xFFFE000000000000ull;      // | m: requested from the host as miss m
+constexpr unsigned long long kMissVoid = 0xFFFFFFFFFFFFFFFFull;     // miss slot lost a race: no request
 
 // error flags (DevState::err)
 constexpr uint32_t kErrTimeout = 1u << 0;    // kept for the status code; no kernel waits on another
@@ -29,15 +31,14 @@ struct DevState {
     uint32_t next_never[2];     // slots ever used per list (Inside, Border)
     uint32_t err;               // sticky error flags
     uint32_t err_info;
-    uint32_t npend_prev;        // pending cells of the last step (fixed at the start of the next)
-    uint32_t reserved[3];
+    uint32_t reserved[4];
     // ---- per step ----
     uint32_t nfull[2];          // FullRX list lengths
     uint32_t ninactive[2];      // INACTIVE slots seen by the scan (uncapped)
     uint32_t nrec[2];           // recycle list lengths = min(ninactive, cap)
     uint32_t nwin[2];           // newly infected cells per destination list
     uint32_t nmiss;             // (rxg,defg) pairs whose P the host must compute
-    uint32_t npending;          // new cells whose P waits for the host
+    uint32_t ntagged;           // new cells whose P waits for the host (tagged)
     uint32_t ndepleted;         // deformed grains whose last cell recrystallized
     uint32_t pad;
     unsigned long long sv[2];   // ACTIVE slots updated

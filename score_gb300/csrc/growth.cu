@@ -19,6 +19,10 @@
 #include <cstddef>
 #include <cstdio>
 #include <cstring>
+#include <atomic>
+#include <condition_variable>
+#include <functional>
+#include <memory>
 #include <mutex>
 #include <string>
 #include <thread>
@@ -211,6 +215,8 @@ struct score_ctx {
     double dt_cached = -1.0;             // dt the front's cached fill increments were computed with
     double pf_sig[2] = {0, 0};           // Gb^2/2 and drag the driving-force table was computed with
     uint64_t rho_version = 0, pf_rho_version = ~0ull, rhomax_version = ~0ull;
+    std::vector<uint32_t> rho_order;   // deformed grains by descending rho0 (rho max while rho == rho0)
+    size_t rho_cursor = 0;             // rho_order[0, cursor) have no cells left
 
     DomainArgs a{};
     DevState* d_state = nullptr;
@@ -237,6 +243,9 @@ struct score_ctx {
     Engine* eng = nullptr;             // launches this domain's steps (its own, or a batch's)
     bool own_eng = false;
     bool running = false;              // steps in the next batched step
+    double weights_ms = 0.0;           // host time in requested weights (summed into the engine's timing)
+    std::vector<unsigned long long> ans_idx;  // weights computed for the last step's requests
+    std::vector<double> ans_val;
     uint64_t launches = 0;             // kernels launched outside the step sequence
     std::vector<score_step_stats> trace;  // per-step stats of the last batched run
 
@@ -262,7 +271,7 @@ void score_ctx::release_domain() {
     if (device >= 0) cudaSetDevice(device);
     void* ptrs[] = {a.f[0].inc, a.f[1].inc, scratch.inc, a.f[0].fill, a.f[0].comp, a.f[0].vel, a.f[0].defg, a.f[0].rxg, a.f[0].xyz, a.f[0].dir, a.f[0].full, a.f[0].recyc,
                     a.f[1].fill, a.f[1].comp, a.f[1].vel, a.f[1].defg, a.f[1].rxg, a.f[1].xyz, a.f[1].dir, a.f[1].full, a.f[1].recyc,
-                    a.grid, a.claim, a.amask, a.ptab, a.defg_cnt, a.rxg_cnt, a.depleted, a.miss, a.pending, a.tobm, a.ctcnt,
+                    a.grid, a.claim, a.amask, a.ptab, a.defg_cnt, a.rxg_cnt, a.depleted, a.miss, a.tobm, a.ctcnt,
                     a.f[0].fmask, a.f[0].imask, a.f[0].tcnt, a.f[1].fmask, a.f[1].imask, a.f[1].tcnt,
                     a.f[0].scnt, a.f[1].scnt, a.csct,
                     d_state, d_pforce, d_u32tmp, d_stage, d_grid_init, d_defg_cnt_init, d_rxq, d_dfq,
@@ -328,6 +337,71 @@ void free_slots(int device, int base, int n) {
     g_slots_used[device] &= ~((n == 64 ? ~0ull : ((1ull << n) - 1)) << base);
 }
 
+// Persistent worker threads for the per-domain host work of a batched step.
+class WorkerPool {
+public:
+    explicit WorkerPool(unsigned n) {
+        for (unsigned i = 0; i < n; ++i) th_.emplace_back([this] { loop(); });
+    }
+    ~WorkerPool() {
+        {
+            std::lock_guard<std::mutex> l(mu_);
+            stop_ = true;
+        }
+        cv_.notify_all();
+        for (auto& t : th_) t.join();
+    }
+    // run f(0..n-1) on the workers and the calling thread; returns when all are done
+    void run(int n, const std::function<void(int)>& f) {
+        {
+            std::lock_guard<std::mutex> l(mu_);
+            job_ = &f;
+            njobs_ = n;
+            next_.store(0);
+            pending_ = n;
+            ++gen_;
+        }
+        cv_.notify_all();
+        work();
+        std::unique_lock<std::mutex> l(mu_);
+        done_.wait(l, [this] { return pending_ == 0; });
+        job_ = nullptr;
+    }
+
+private:
+    void work() {
+        for (;;) {
+            const int i = next_.fetch_add(1);
+            if (i >= njobs_.load()) return;
+            (*job_.load())(i);
+            std::lock_guard<std::mutex> l(mu_);
+            if (--pending_ == 0) done_.notify_all();
+        }
+    }
+    void loop() {
+        uint64_t seen = 0;
+        for (;;) {
+            {
+                std::unique_lock<std::mutex> l(mu_);
+                cv_.wait(l, [&] { return stop_ || gen_ != seen; });
+                if (stop_) return;
+                seen = gen_;
+                if (!job_.load()) continue;
+            }
+            work();
+        }
+    }
+    std::vector<std::thread> th_;
+    std::mutex mu_;
+    std::condition_variable cv_, done_;
+    std::atomic<const std::function<void(int)>*> job_{nullptr};
+    std::atomic<int> njobs_{0};
+    int pending_ = 0;
+    std::atomic<int> next_{0};
+    uint64_t gen_ = 0;
+    bool stop_ = false;
+};
+
 struct Engine {
     int device = 0, sms = 1;
     cudaStream_t stream = nullptr;
@@ -348,6 +422,18 @@ struct Engine {
     score_timing tm{};
     uint64_t launches = 0;
     std::string err;
+    std::unique_ptr<WorkerPool> pool;  // batches of several domains
+    // the host's weights for all domains' requests, copied to the device in one piece
+    unsigned long long* h_ans_i = nullptr; double* h_ans_v = nullptr;
+    unsigned long long* d_ans_i = nullptr; double* d_ans_v = nullptr;
+    size_t ans_cap = 0, ans_total = 0;
+    int stage_answers();
+    cudaError_t upload_answers() {
+        if (!ans_total) return cudaSuccess;
+        cudaError_t e = cudaMemcpyAsync(d_ans_i, h_ans_i, ans_total * 8, cudaMemcpyHostToDevice, stream);
+        if (e == cudaSuccess) e = cudaMemcpyAsync(d_ans_v, h_ans_v, ans_total * 8, cudaMemcpyHostToDevice, stream);
+        return e;
+    }
 
     ~Engine() { release(); }
     int init(int dev, int ndom) {
@@ -373,6 +459,12 @@ struct Engine {
     void release() {
         cudaSetDevice(device);
         drop_graph();
+        if (h_ans_i) cudaFreeHost(h_ans_i);
+        if (h_ans_v) cudaFreeHost(h_ans_v);
+        if (d_ans_i) cudaFree(d_ans_i);
+        if (d_ans_v) cudaFree(d_ans_v);
+        h_ans_i = nullptr; h_ans_v = nullptr; d_ans_i = nullptr; d_ans_v = nullptr;
+        ans_cap = ans_total = 0;
         if (h_args) cudaFreeHost(h_args);
         d_args = nullptr; h_args = nullptr;
         free_slots(device, base, nslots);
@@ -435,7 +527,8 @@ double weight_of(score_ctx* c, uint32_t r, uint32_t g) {
 void resolve_weights(score_ctx* c, const std::vector<unsigned long long>& idx, std::vector<double>& val) {
     val.resize(idx.size());
     auto work = [&](size_t lo, size_t hi) {
-        for (size_t i = lo; i < hi; ++i) val[i] = weight_of(c, (uint32_t)(idx[i] / c->ndefg), (uint32_t)(idx[i] % c->ndefg));
+        for (size_t i = lo; i < hi; ++i)  // a void slot (lost race) keeps 0, which no cell reads
+            val[i] = idx[i] == kMissVoid ? 0.0 : weight_of(c, (uint32_t)(idx[i] / c->ndefg), (uint32_t)(idx[i] % c->ndefg));
     };
     size_t n = idx.size();
     unsigned nth = std::max(1u, std::min(32u, std::thread::hardware_concurrency()));
@@ -451,7 +544,7 @@ int check_device_errors(score_ctx* c, uint32_t flags) {
     if (flags & kErrKeyLimit) return c->fail(SCORE_ERR_KEYLIMIT, "more than 2^32-1 infection attempts in one step");
     if (flags & kErrBorderRef) return c->fail(SCORE_ERR_BORDER_CAPACITY, "Border list exceeded 2(xy+xz+yz) slots (the reference writes out of bounds here)");
     if (flags & kErrCapacity) return c->fail(SCORE_ERR_CAPACITY, "front list capacity exceeded");
-    if (flags & kErrMissCap) return c->fail(SCORE_ERR_CAPACITY, "pending mobility-weight list capacity exceeded");
+    if (flags & kErrMissCap) return c->fail(SCORE_ERR_CAPACITY, "mobility-weight request list capacity exceeded");
     return c->fail(SCORE_ERR_STATE, "device bounds check failed (corrupt domain?)");
 }
 
@@ -616,6 +709,8 @@ int reset_state(score_ctx* c) {
     if (e == cudaSuccess) e = cudaMemsetAsync(a.csct, 0, c->csct_words * 4, st);
     if (e != cudaSuccess) return c->cuda_fail(e, "reset domain");
     a.n_ans = 0;
+    c->ans_idx.clear();
+    c->ans_val.clear();
     memset(&c->h_box->snap, 0, sizeof(DevState));
     c->running = false;
     c->trace.clear();
@@ -627,6 +722,7 @@ int reset_state(score_ctx* c) {
     ph.init(&c->prm);
     ph.rhomax = rhomax_of(c->rho, c->defg_cnt_host);
     c->rho_version = 0; c->rhomax_version = 0; c->pf_rho_version = ~0ull;
+    c->rho_cursor = 0;
     ph.update_temperature();
     ph.update_atomistic();
     ph.update_mobilities();
@@ -655,31 +751,6 @@ int reset_state(score_ctx* c) {
 // ------------------------------------------------------------------ step of one domain, host side
 namespace {
 
-// The weights answered after the last step and the cells that waited for them are
-// normally applied by the first kernels of the next step; a defragmentation moves
-// slots, so before one they are applied at once, for this domain alone.
-int flush_pending(score_ctx* c) {
-    if (c->a.n_ans == 0 && c->h_box->snap.npend_prev == 0) return SCORE_OK;
-    Engine& E = *c->eng;
-    size_t i = 0;
-    while (i < E.dom.size() && E.dom[i] != c) ++i;
-    DomainArgs a = c->a;
-    a.active = 1;
-    E.h_args[i] = a;
-    cudaError_t e = cudaMemcpyAsync(E.d_args + i, E.h_args + i, sizeof(DomainArgs), cudaMemcpyHostToDevice, c->stream);
-    if (e != cudaSuccess) return c->cuda_fail(e, "apply weights");
-    k_apply_answers<<<(uint32_t)c->sms * 2, kBlock, 0, c->stream>>>(E.base + (int)i, 1);
-    if (c->fp32) k_fix_pending<true><<<(uint32_t)c->sms * 2, kBlock, 0, c->stream>>>(E.base + (int)i, 1);
-    else k_fix_pending<false><<<(uint32_t)c->sms * 2, kBlock, 0, c->stream>>>(E.base + (int)i, 1);
-    c->launches += 2;
-    e = cudaMemsetAsync((char*)c->d_state + offsetof(DevState, npend_prev), 0, 4, c->stream);
-    if (e == cudaSuccess) e = cudaStreamSynchronize(c->stream);
-    if (e != cudaSuccess) return c->cuda_fail(e, "apply weights");
-    c->a.n_ans = 0;
-    c->h_box->snap.npend_prev = 0;
-    return SCORE_OK;
-}
-
 // Before the launch: time-dependent nucleation, defragmentation at X logpoints and the
 // argument block of this step.
 int pre_step(score_ctx* c, uint32_t* newnuc) {
@@ -688,8 +759,6 @@ int pre_step(score_ctx* c, uint32_t* newnuc) {
     if (s != SCORE_OK) return s;
     // on-the-fly defragmentation at user X logpoints (SCORE_Kernel.cpp:6625-6630, thresholds in cells)
     if (c->prm.defragmentation && c->defrag_cnt < c->prm.n_defrag && c->Xcells >= c->prm.defrag_x[c->defrag_cnt] * (double)c->N) {
-        s = flush_pending(c);
-        if (s != SCORE_OK) return s;
         for (int L = 0; L < 2; ++L) { s = defragment(c, L); if (s != SCORE_OK) return s; }
         c->defrag_cnt++;
     }
@@ -718,6 +787,9 @@ int post_step(score_ctx* c, uint32_t newnuc, score_step_stats* out) {
     double pmax_new = 0.0;
     if (hs.pmax_bits) memcpy(&pmax_new, &hs.pmax_bits, 8);
     a.n_ans = 0;
+    c->ans_idx.clear();
+    c->ans_val.clear();
+    uint32_t nreq = 0;  // distinct weights requested (void race slots excluded)
     if (hs.nmiss > 0) {
         std::vector<unsigned long long> idx(hs.nmiss);
         std::vector<double> val;
@@ -731,25 +803,12 @@ int post_step(score_ctx* c, uint32_t newnuc, score_step_stats* out) {
         }
         const auto w_t0 = std::chrono::steady_clock::now();
         resolve_weights(c, idx, val);
-        c->eng->tm.weights_ms += std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - w_t0).count();
+        c->weights_ms += std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - w_t0).count();
         for (double v : val) if (v > pmax_new) pmax_new = v;
-        if (hs.nmiss <= kBoxMiss) {
-            // read by the next step's k_apply_answers; the previous one finished before this step ended
-            memcpy(c->h_box->ans_idx, idx.data(), (size_t)hs.nmiss * 8);
-            memcpy(c->h_box->ans_val, val.data(), (size_t)hs.nmiss * 8);
-            a.ans_idx = c->d_box->ans_idx;
-            a.ans_val = c->d_box->ans_val;
-        } else {
-            if (!c->stage((size_t)hs.nmiss * 16)) return c->fail(SCORE_ERR_NOMEM, "staging buffer");
-            unsigned long long* si = (unsigned long long*)c->d_stage;
-            double* sv = (double*)(si + hs.nmiss);
-            e = cudaMemcpyAsync(si, idx.data(), (size_t)hs.nmiss * 8, cudaMemcpyHostToDevice, st);
-            if (e == cudaSuccess) e = cudaMemcpyAsync(sv, val.data(), (size_t)hs.nmiss * 8, cudaMemcpyHostToDevice, st);
-            if (e == cudaSuccess) e = cudaStreamSynchronize(st);  // pageable sources go out of scope
-            if (e != cudaSuccess) return c->cuda_fail(e, "upload weights");
-            a.ans_idx = si;
-            a.ans_val = sv;
-        }
+        for (unsigned long long x : idx) nreq += x != kMissVoid;
+        // staged by the engine into one host-to-device copy before the next step
+        c->ans_idx.swap(idx);
+        c->ans_val.swap(val);
         a.n_ans = hs.nmiss;
     }
     // deformed grains that ran out of cells this step (synchronize_mydefpool_counts)
@@ -777,7 +836,14 @@ int post_step(score_ctx* c, uint32_t newnuc, score_step_stats* out) {
     c->Xcells = c->Xcells + (double)nfull;
     const double X = (c->Xcells / (double)c->N);
     if (c->rhomax_version != c->rho_version) {  // rho max only moves when rho or the grain set changes
-        ph.rhomax = rhomax_of(c->rho, c->defg_cnt_host);
+        if (c->rho_version == 0) {
+            // rho is still rho0: the first grain in descending-rho0 order that has cells
+            while (c->rho_cursor < c->rho_order.size() && c->defg_cnt_host[c->rho_order[c->rho_cursor]] == 0) ++c->rho_cursor;
+            const double best = c->rho_cursor < c->rho_order.size() ? c->rho[c->rho_order[c->rho_cursor]] : -1.0;
+            ph.rhomax = (best >= kRhomaxWellAnnealed) ? best : kRhomaxWellAnnealed;
+        } else {
+            ph.rhomax = rhomax_of(c->rho, c->defg_cnt_host);
+        }
         c->rhomax_version = c->rho_version;
     }
     const double rhomax_step = ph.rhomax;
@@ -802,7 +868,7 @@ int post_step(score_ctx* c, uint32_t newnuc, score_step_stats* out) {
     o.Pmax = ph.Pmax; o.rhomax = rhomax_step; o.dXstep = 0.0;
     o.next_never[0] = c->next_never[0]; o.next_never[1] = c->next_never[1];
     o.n_recycled[0] = hs.nrec[0]; o.n_recycled[1] = hs.nrec[1];
-    o.p_misses = hs.nmiss;
+    o.p_misses = nreq;
     if (out) *out = o;
     return SCORE_OK;
 }
@@ -831,8 +897,6 @@ void launch_sequence_t(const Engine& E, int n) {
     cudaStream_t st = E.stream;
     const int d = E.base;
     const uint32_t S = (uint32_t)E.sms;
-    k_apply_answers<<<S * 2, kBlock, 0, st>>>(d, n);
-    k_fix_pending<FP32><<<S * 2, kBlock, 0, st>>>(d, n);
     record(E, 0);
     if (E.cfg.items == 4) launch_grow<FP32, 4>(E, n);
     else if (E.cfg.items == 16) launch_grow<FP32, 16>(E, n);
@@ -847,7 +911,7 @@ void launch_sequence_t(const Engine& E, int n) {
     record(E, 4);
 }
 
-constexpr int kStepKernels = 10;
+constexpr int kStepKernels = 8;
 
 }  // namespace
 
@@ -858,7 +922,8 @@ void Engine::launch_sequence(int n) {
 
 // the argument copy and the kernels of one step, as a graph replay or direct launches
 cudaError_t Engine::enqueue_step(int n) {
-    cudaError_t e = cudaMemcpyAsync(d_args, h_args, (size_t)n * sizeof(DomainArgs), cudaMemcpyHostToDevice, stream);
+    cudaError_t e = upload_answers();
+    if (e == cudaSuccess) e = cudaMemcpyAsync(d_args, h_args, (size_t)n * sizeof(DomainArgs), cudaMemcpyHostToDevice, stream);
     if (e != cudaSuccess) return e;
     if (!use_graph) {
         launch_sequence(n);
@@ -883,6 +948,43 @@ cudaError_t Engine::enqueue_step(int n) {
     return cudaGraphLaunch(gexec, stream);
 }
 
+// Pack every domain's answered weights into the pinned staging buffer and point the
+// domains' argument blocks at their part of the device copy (made by upload_answers
+// before the next step's kernels).
+int Engine::stage_answers() {
+    size_t total = 0;
+    for (score_ctx* c : dom) total += c->ans_idx.size();
+    ans_total = 0;
+    if (total == 0) return SCORE_OK;
+    if (total > ans_cap) {
+        const size_t cap = std::max<size_t>(total, 2 * ans_cap);
+        if (h_ans_i) cudaFreeHost(h_ans_i);
+        if (h_ans_v) cudaFreeHost(h_ans_v);
+        if (d_ans_i) cudaFree(d_ans_i);
+        if (d_ans_v) cudaFree(d_ans_v);
+        h_ans_i = nullptr; h_ans_v = nullptr; d_ans_i = nullptr; d_ans_v = nullptr;
+        ans_cap = 0;
+        cudaError_t e = cudaMallocHost((void**)&h_ans_i, cap * 8);
+        if (e == cudaSuccess) e = cudaMallocHost((void**)&h_ans_v, cap * 8);
+        if (e == cudaSuccess) e = cudaMalloc((void**)&d_ans_i, cap * 8);
+        if (e == cudaSuccess) e = cudaMalloc((void**)&d_ans_v, cap * 8);
+        if (e != cudaSuccess) return fail(SCORE_ERR_NOMEM, "weight staging buffers");
+        ans_cap = cap;
+    }
+    size_t off = 0;
+    for (score_ctx* c : dom) {
+        const size_t k = c->ans_idx.size();
+        if (!k) continue;
+        memcpy(h_ans_i + off, c->ans_idx.data(), k * 8);
+        memcpy(h_ans_v + off, c->ans_val.data(), k * 8);
+        c->a.ans_idx = d_ans_i + off;
+        c->a.ans_val = d_ans_v + off;
+        off += k;
+    }
+    ans_total = total;
+    return SCORE_OK;
+}
+
 // One step of every running domain.
 int Engine::step(bool timed) {
     cudaSetDevice(device);
@@ -902,10 +1004,13 @@ int Engine::step(bool timed) {
         h_args[i] = c->a;
     }
     if (nrun == 0) return SCORE_OK;
+    const auto pre_t1 = std::chrono::steady_clock::now();
+    tm.pre_ms += std::chrono::duration<double, std::milli>(pre_t1 - host_t0).count();
     cudaError_t e = enqueue_step(n);
     const auto wait_t0 = std::chrono::steady_clock::now();
     if (e == cudaSuccess) e = cudaStreamSynchronize(stream);  // the one wait of the step: the mailboxes are filled
-    tm.wait_ms += std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - wait_t0).count();
+    const auto wait_t1 = std::chrono::steady_clock::now();
+    tm.wait_ms += std::chrono::duration<double, std::milli>(wait_t1 - wait_t0).count();
     if (e != cudaSuccess) {
         for (score_ctx* c : dom) c->failed = true;
         return fail(SCORE_ERR_CUDA, std::string("growth step: ") + cudaGetErrorString(e));
@@ -922,15 +1027,33 @@ int Engine::step(bool timed) {
     }
     tm.grow_launches += 1;
     const double bpu = fp32 ? 17.0 : 25.0;  // algorithmic bytes per front-cell update of k_grow_fill
+    // the master-block work of each domain (weights, physics, dt) is independent
+    std::vector<int> status(n, SCORE_OK);
+    auto post = [&](int i) {
+        score_ctx* c = dom[i];
+        if (!c->running) return;
+        cudaSetDevice(device);  // the calling thread may be a worker
+        status[i] = post_step(c, newnuc[i], nullptr);
+    };
+    if (n >= 4) {
+        if (!pool) pool.reset(new WorkerPool(std::max(1u, std::min(15u, std::thread::hardware_concurrency() - 1))));
+        pool->run(n, post);
+    } else {
+        for (int i = 0; i < n; ++i) post(i);
+    }
     for (int i = 0; i < n; ++i) {
         score_ctx* c = dom[i];
         if (!c->running) continue;
-        score_step_stats st;
-        const int s = post_step(c, newnuc[i], &st);
-        if (s != SCORE_OK) return fail(s, c->err);
+        if (status[i] != SCORE_OK) return fail(status[i], c->err);
+        const score_step_stats& st = c->last;
         tm.grow_bytes += bpu * (double)st.Sv;
         tm.step_bytes += bpu * (double)st.Sv + 120.0 * (double)st.n_full + 37.0 * (double)st.n_new;
+        tm.weights_ms += c->weights_ms;
+        c->weights_ms = 0.0;
     }
+    const int sa = stage_answers();
+    if (sa != SCORE_OK) return sa;
+    tm.post_ms += std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - wait_t1).count();
     tm.host_ms += std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - host_t0).count();
     return SCORE_OK;
 }
@@ -974,7 +1097,7 @@ namespace {
 int check_params(const score_params* p, int device) {
     if (p->nx < 3 || p->ny < 3 || p->nz < 3) return SCORE_ERR_ARG;
     const uint64_t N = (uint64_t)p->nx * p->ny * p->nz;
-    if (N >= 0x7FFFFFFFull) return SCORE_ERR_ARG;  // pending-list entries keep the list id in bit 31 of a slot index
+    if (N >= 0x7FFFFFFFull) return SCORE_ERR_ARG;  // slot counters and ranks are 32-bit with headroom
     if (p->n_schedule < 1) return SCORE_ERR_ARG;
     int ndev = 0;
     if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) { cudaGetLastError(); return SCORE_ERR_NOT_BUILT; }
@@ -1176,6 +1299,9 @@ int score_load_domain(score_ctx* c, const uint32_t* grid, const double* defg_qua
     c->site.assign(rxg_site, rxg_site + nrxg);
     c->tincub.assign(nrxg, 0.0);
     if (rxg_tincub) c->tincub.assign(rxg_tincub, rxg_tincub + nrxg);
+    c->rho_order.resize(ndefg);
+    for (uint32_t g = 0; g < ndefg; ++g) c->rho_order[g] = g;
+    std::stable_sort(c->rho_order.begin(), c->rho_order.end(), [&](uint32_t x, uint32_t y) { return c->rho0[x] > c->rho0[y]; });
     c->nuc_order.resize(nrxg);
     for (uint32_t r = 0; r < nrxg; ++r) c->nuc_order[r] = r;
     std::stable_sort(c->nuc_order.begin(), c->nuc_order.end(), [&](uint32_t x, uint32_t y) { return c->tincub[x] < c->tincub[y]; });
@@ -1226,7 +1352,7 @@ int score_load_domain(score_ctx* c, const uint32_t* grid, const double* defg_qua
             if (e == cudaSuccess) e = dalloc(&f.scnt, c->scnt_words[L]);
         }
         c->csct_words = 2 * ((N / kBlock + 2) / kSuper + 2);
-        a.misscap = a.pendcap = (uint32_t)std::min<uint64_t>(N, 1ull << 25);
+        a.misscap = (uint32_t)std::min<uint64_t>(N, 1ull << 25);
         if (e == cudaSuccess) e = dalloc(&a.grid, N);
         if (e == cudaSuccess) e = dalloc(&c->d_grid_init, N);
         if (e == cudaSuccess) e = dalloc(&a.claim, N);
@@ -1240,7 +1366,6 @@ int score_load_domain(score_ctx* c, const uint32_t* grid, const double* defg_qua
         if (e == cudaSuccess) e = dalloc(&a.rxg_cnt, nrxg);
         if (e == cudaSuccess) e = dalloc(&a.depleted, ndefg);
         if (e == cudaSuccess) e = dalloc(&a.miss, a.misscap);
-        if (e == cudaSuccess) e = dalloc(&a.pending, a.pendcap);
         if (e == cudaSuccess) e = dalloc(&c->d_state, 1);
         if (e == cudaSuccess) e = dalloc(&c->d_pforce, ndefg);
         if (e == cudaSuccess) e = dalloc(&c->d_u32tmp, 64);

@@ -93,8 +93,7 @@ struct DomainArgs {
     uint32_t* rxg_cnt;
     uint32_t* depleted;
     unsigned long long* miss;   // table indices the host must fill
-    uint32_t* pending;          // (list << 31) | slot of new cells waiting for P
-    uint32_t misscap, pendcap;
+    uint32_t misscap;
     uint32_t nx, ny, nz, nxy;
     uint32_t ncells;
     int32_t noff[26];           // linear offset of neighbour d of an interior cell
@@ -105,8 +104,8 @@ struct DomainArgs {
     int32_t dt_changed;         // dt differs from the dt the cached increments were made with
     int32_t refresh;            // recompute every vel this step (T, rho or the drag changed)
     int32_t active;             // the domain steps in this launch
-    uint32_t n_ans;             // weights the host computed for the last step's requests
-    const unsigned long long* ans_idx;  // their table indices (device view of the mailbox)
+    uint32_t n_ans;             // weights the host computed for the last step's requests (miss slot order)
+    const unsigned long long* ans_idx;  // their table indices (device copy; kMissVoid = none)
     const double* ans_val;
     HostBox* box;               // device view of the domain's mailbox
     double mLAGB, mHAGB, mGS, mRH, dt, cinv;
@@ -249,6 +248,11 @@ __device__ __forceinline__ int seg_find(const uint32_t* s_pre, int nseg, uint32_
     return lo;
 }
 
+// Thread-per-item kernels pad each segment to whole warps, so that the 32 items of a
+// warp belong to one domain and its argument reads stay uniform (one constant-cache
+// access per field); padding items are skipped.
+__device__ __forceinline__ uint32_t warp_pad(uint32_t n) { return (n + 31u) & ~31u; }
+
 // grow tiles of a list: kBlock * ITEMS slots, ITEMS * kWarps mask words
 template <int ITEMS>
 struct GrowShape {
@@ -283,6 +287,16 @@ __device__ __forceinline__ void tile_prefix(const uint32_t* cnt, const uint32_t*
 //                 slot order; the warp of a list's last tile stores the list totals.
 // REFRESH: recompute vel of every active slot from the P table and the current
 // physics (after T, rho or the drag changed) before growing it.
+// A cell created last step whose weight the host computed: P = answer `tag`; the table
+// entry (tagged until now) gets the value for later lookups.
+__device__ __forceinline__ double answered_velocity(const DomainArgs& a, const DFront& fr, uint32_t slot, uint8_t dir,
+                                                    unsigned long long tag) {
+    const uint32_t m = (uint32_t)tag;
+    const double P = a.ans_val[m];
+    a.ptab[a.ans_idx[m]] = (unsigned long long)__double_as_longlong(P);
+    return velocity_factor(a, P, fr.defg[slot], dir & kCodeMask);
+}
+
 // returns the thread's ACTIVE slots (the Sv share)
 template <bool FP32, bool REFRESH, int ITEMS>
 __device__ __forceinline__ uint32_t grow_tile(const DomainArgs& a, int L, uint32_t tile, uint32_t n, uint32_t* s_f, uint32_t* s_i) {
@@ -305,7 +319,10 @@ __device__ __forceinline__ uint32_t grow_tile(const DomainArgs& a, int L, uint32
             const uint32_t slot = base + (uint32_t)(k * kBlock) + threadIdx.x;
             w[k] = -1.0; fill[k] = 0.0;
             if (d[k] != kInactive) {
-                if (REFRESH) {
+                if (d[k] & kPend) {
+                    w[k] = answered_velocity(a, fr, slot, d[k], ((const unsigned long long*)fr.vel)[slot]);
+                    ((double*)fr.vel)[slot] = w[k];
+                } else if (REFRESH) {
                     const uint32_t g = fr.defg[slot];
                     const double P = __longlong_as_double((long long)a.ptab[(unsigned long long)fr.rxg[slot] * a.ndefg + g]);
                     w[k] = velocity_factor(a, P, g, d[k] & kCodeMask);
@@ -344,7 +361,10 @@ __device__ __forceinline__ uint32_t grow_tile(const DomainArgs& a, int L, uint32
             const uint32_t slot = base + (uint32_t)(k * kBlock) + threadIdx.x;
             vel[k] = -1.0f; fill[k] = 0.0f; comp[k] = 0.0f;
             if (d[k] != kInactive) {
-                if (REFRESH) {
+                if (d[k] & kPend) {
+                    vel[k] = (float)answered_velocity(a, fr, slot, d[k], ((const uint32_t*)fr.vel)[slot]);
+                    ((float*)fr.vel)[slot] = vel[k];
+                } else if (REFRESH) {
                     const uint32_t g = fr.defg[slot];
                     const double P = __longlong_as_double((long long)a.ptab[(unsigned long long)fr.rxg[slot] * a.ndefg + g]);
                     vel[k] = (float)velocity_factor(a, P, g, d[k] & kCodeMask);
@@ -598,16 +618,18 @@ __device__ __forceinline__ uint32_t full_cells(const DomainArgs& a) {
 }
 
 __global__ void __launch_bounds__(kBlock, 4) k_claim(int base, int ndom) {
-    __shared__ uint32_t s_pre[kMaxSegs + 1];
+    __shared__ uint32_t s_pre[kMaxSegs + 1], s_cnt[kMaxSegs];
     const uint32_t total = seg_prefix(s_pre, ndom, [&](int s) {
         const DomainArgs& a = c_args[base + (s)];
         if (a.active && 26ull * (a.st->nfull[0] + a.st->nfull[1]) >= 0xFFFFFFFFull) atomicOr(&a.st->err, kErrKeyLimit);
-        return full_cells(a);
+        s_cnt[s] = full_cells(a);
+        return warp_pad(s_cnt[s]);
     });
     for (uint32_t u = blockIdx.x * blockDim.x + threadIdx.x; u < total; u += gridDim.x * blockDim.x) {
         const int s = seg_find(s_pre, ndom, u);
         const DomainArgs& a = c_args[base + (s)];
         const uint32_t f = u - s_pre[s];
+        if (f >= s_cnt[s]) continue;
         const uint32_t F0 = a.st->nfull[0];
         uint32_t mask;
         if (f < F0) {
@@ -705,10 +727,15 @@ __device__ __noinline__ bool device_weight(const DomainArgs& A, uint32_t rxg, ui
     return false;
 }
 
-// P of a new cell from the table; unknown entries are classified on the device when
-// exact, otherwise requested from the host
-__device__ __forceinline__ bool lookup_p(const DomainArgs& a, uint32_t rxg, uint32_t defg, double& P) {
-    unsigned long long* e = &a.ptab[(unsigned long long)rxg * a.ndefg + defg];
+// P of a new cell from the table.  An unknown entry is classified on the device when
+// its value is exact; otherwise it is requested from the host: the first requester
+// takes miss slot m (atomicAdd) and tags the entry kPtabTag | m; every cell of the pair
+// carries m and gets P from the host's answer m in the next step's k_grow_fill.  A
+// requester that loses the race to tag the entry voids its slot.  Returns true with P,
+// or false with the tag.
+__device__ __forceinline__ bool lookup_p(const DomainArgs& a, uint32_t rxg, uint32_t defg, double& P, uint32_t& tag) {
+    const unsigned long long idx = (unsigned long long)rxg * a.ndefg + defg;
+    unsigned long long* e = &a.ptab[idx];
     unsigned long long bits = *(volatile unsigned long long*)e;
     if (bits == kPtabEmpty) {
         double v;
@@ -717,20 +744,20 @@ __device__ __forceinline__ bool lookup_p(const DomainArgs& a, uint32_t rxg, uint
             const unsigned long long old = atomicCAS(e, kPtabEmpty, vb);
             if (old == kPtabEmpty || old == vb) { P = v; return true; }
             bits = old;
-            if (bits == kPtabPending) return false;
-            P = __longlong_as_double((long long)bits);
-            return true;
-        }
-        unsigned long long old = atomicCAS(e, kPtabEmpty, kPtabPending);
-        if (old == kPtabEmpty) {
+        } else {
             const uint32_t m = atomicAdd(&a.st->nmiss, 1u);
-            if (m < a.misscap) a.miss[m] = (unsigned long long)rxg * a.ndefg + defg;
-            else atomicOr(&a.st->err, kErrMissCap);
-            return false;
+            if (m >= a.misscap) { atomicOr(&a.st->err, kErrMissCap); tag = 0; return false; }
+            const unsigned long long old = atomicCAS(e, kPtabEmpty, kPtabTag | m);
+            if (old == kPtabEmpty) {
+                a.miss[m] = idx;
+                tag = m;
+                return false;
+            }
+            a.miss[m] = kMissVoid;
+            bits = old;
         }
-        bits = old;
     }
-    if (bits == kPtabPending) return false;
+    if ((bits >> 48) == (kPtabTag >> 48)) { tag = (uint32_t)bits; return false; }
     P = __longlong_as_double((long long)bits);
     return true;
 }
@@ -894,15 +921,33 @@ __global__ void __launch_bounds__(kBlock, 4) k_commit(int base, int ndom) {
             }
             // the full cell is now recrystallized
             a.grid[cell] = a.ndefg + rsrc;
-            atomicAdd(&a.rxg_cnt[rsrc], 1u);
-            const uint32_t old = atomicSub(&a.defg_cnt[gsrc], 1u);
-            if (old == 1u) {
-                const uint32_t q = atomicAdd(&a.st->ndepleted, 1u);
-                if (q < a.ndefg) a.depleted[q] = gsrc;
-            }
             src.dir[slot] = kInactive;
             if (!FP32) ((double*)src.fill)[slot] = 0.0;
             else { ((float*)src.fill)[slot] = 0.0f; src.comp[slot] = 0.0f; }
+        }
+        // per-grain cell counts: one atomic per grain and warp (full cells of one grain
+        // tend to finish together)
+        {
+            const bool has = f < F;
+            const uint32_t act = __ballot_sync(0xFFFFFFFFu, has);
+            uint32_t rsrc = 0, gsrc = 0;
+            if (has) {
+                const int L = f >= F0 ? 1 : 0;
+                const uint32_t slot = a.f[L].full[L ? f - F0 : f];
+                rsrc = a.f[L].rxg[slot];
+                gsrc = a.f[L].defg[slot];
+            }
+            const uint32_t mr = __match_any_sync(0xFFFFFFFFu, has ? rsrc : 0xFFFFFFFFu) & act;
+            const uint32_t mg = __match_any_sync(0xFFFFFFFFu, has ? gsrc : 0xFFFFFFFFu) & act;
+            if (has && (__ffs(mr) - 1) == lane) atomicAdd(&a.rxg_cnt[rsrc], (uint32_t)__popc(mr));
+            if (has && (__ffs(mg) - 1) == lane) {
+                const uint32_t k = (uint32_t)__popc(mg);
+                const uint32_t old = atomicSub(&a.defg_cnt[gsrc], k);
+                if (old == k) {
+                    const uint32_t q = atomicAdd(&a.st->ndepleted, 1u);
+                    if (q < a.ndefg) a.depleted[q] = gsrc;
+                }
+            }
         }
         __syncthreads();
     }
@@ -916,12 +961,16 @@ __device__ __forceinline__ uint32_t new_cells(const DomainArgs& a) { return a.ac
 
 template <bool FP32>
 __global__ void __launch_bounds__(kBlock, 4) k_new_vel(int base, int ndom) {
-    __shared__ uint32_t s_pre[kMaxSegs + 1];
-    const uint32_t total = seg_prefix(s_pre, ndom, [&](int s) { return new_cells(c_args[base + (s)]); });
+    __shared__ uint32_t s_pre[kMaxSegs + 1], s_cnt[kMaxSegs];
+    const uint32_t total = seg_prefix(s_pre, ndom, [&](int s) {
+        s_cnt[s] = new_cells(c_args[base + (s)]);
+        return warp_pad(s_cnt[s]);
+    });
     for (uint32_t u = blockIdx.x * blockDim.x + threadIdx.x; u < total; u += gridDim.x * blockDim.x) {
         const int s = seg_find(s_pre, ndom, u);
         const DomainArgs& a = c_args[base + (s)];
         const uint32_t i = u - s_pre[s];
+        if (i >= s_cnt[s]) continue;
         const uint32_t n0 = a.st->nwin[0];
         const int D = i >= n0 ? 1 : 0;
         const uint32_t r = D ? i - n0 : i;
@@ -930,34 +979,47 @@ __global__ void __launch_bounds__(kBlock, 4) k_new_vel(int base, int ndom) {
         const uint32_t ns = r < nrec ? dst.recyc[r] : a.st->next_never[D] + (r - nrec);
         if (ns >= dst.cap) continue;  // k_commit flagged the overflow
         const uint32_t gt = dst.defg[ns];
-        const int code = dst.dir[ns] & kCodeMask;
+        const uint8_t dir = dst.dir[ns];
         double P = 0.0;
-        const bool known = lookup_p(a, dst.rxg[ns], gt, P);
-        if (!FP32) ((double*)dst.vel)[ns] = known ? velocity_factor(a, P, gt, code) : -1.0;
-        else ((float*)dst.vel)[ns] = known ? (float)velocity_factor(a, P, gt, code) : -1.0f;
+        uint32_t tag = 0;
+        const bool known = lookup_p(a, dst.rxg[ns], gt, P, tag);
+        if (known) {
+            if (!FP32) ((double*)dst.vel)[ns] = velocity_factor(a, P, gt, dir & kCodeMask);
+            else ((float*)dst.vel)[ns] = (float)velocity_factor(a, P, gt, dir & kCodeMask);
+        } else {
+            // vel holds the answer tag until the next k_grow_fill
+            if (!FP32) ((unsigned long long*)dst.vel)[ns] = tag;
+            else ((uint32_t*)dst.vel)[ns] = tag;
+            dst.dir[ns] = dir | kPend;
+        }
         if (!known) {
-            const uint32_t q = atomicAdd(&a.st->npending, 1u);
-            if (q < a.pendcap) a.pending[q] = ((uint32_t)D << 31) | ns;
-            else atomicOr(&a.st->err, kErrMissCap);
+            atomicAdd(&a.st->ntagged, 1u);
         } else if (P > 0.0) {
-            atomicMax(&a.st->pmax_bits, (unsigned long long)__double_as_longlong(P));
+            // running max of the new weights: one atomic per distinct value in the warp
+            const unsigned long long bits = (unsigned long long)__double_as_longlong(P);
+            const uint32_t act = __activemask();
+            unsigned long long m = bits;
+            for (int o = 16; o > 0; o >>= 1) {
+                const unsigned long long x = __shfl_xor_sync(act, m, o);
+                const bool src_on = (act >> ((threadIdx.x & 31) ^ o)) & 1u;
+                if (src_on && x > m) m = x;
+            }
+            if (m == bits && (__ffs(__match_any_sync(act, bits)) - 1) == (int)(threadIdx.x & 31))
+                atomicMax(&a.st->pmax_bits, bits);
         }
     }
 }
 
-// ------------------------------------------------------------------ K4 step end, step start
+// ------------------------------------------------------------------ K4 step end
 // Host mailbox in pinned, device-mapped memory: k_step_end writes the step's scalars,
 // the mobility-weight requests and the depleted grains straight into host memory, so
-// the host needs one stream synchronization per step and no copies; the host writes
-// the requested weights back into ans_* for the next step's k_apply_answers.
+// the host needs one stream synchronization per step and no copies.
 constexpr uint32_t kBoxMiss = 16384;
 constexpr uint32_t kBoxDep = 16384;
 struct HostBox {
     DevState snap;
     unsigned long long miss[kBoxMiss];
     uint32_t depleted[kBoxDep];
-    unsigned long long ans_idx[kBoxMiss];
-    double ans_val[kBoxMiss];
 };
 
 // One block per domain: advances the high-water marks, posts the step to the domain's
@@ -977,7 +1039,6 @@ __global__ void __launch_bounds__(kBlock) k_step_end(int base, int ndom, uint32_
             if (st->nwin[D] > st->nrec[D]) st->next_never[D] += st->nwin[D] - st->nrec[D];
             if (st->next_never[D] > cap[D]) { st->next_never[D] = cap[D]; st->err |= kErrCapacity; }
         }
-        st->npend_prev = min(st->npending, a.pendcap);
         box->snap = *st;
         s_nm = min(min(st->nmiss, a.misscap), kBoxMiss);
         s_nd = min(min(st->ndepleted, a.ndefg), kBoxDep);
@@ -992,42 +1053,6 @@ __global__ void __launch_bounds__(kBlock) k_step_end(int base, int ndom, uint32_
     if (threadIdx.x == 0) {
         char* p = (char*)st + kStepFieldsOffset;
         for (size_t i = 0; i < sizeof(DevState) - kStepFieldsOffset; ++i) p[i] = 0;
-    }
-}
-
-// Step start: the weights the host computed for last step's requests go into the
-// table (k_apply_answers), then the cells that waited for them get their velocity
-// factor (k_fix_pending), before any fill is updated.
-__device__ __forceinline__ uint32_t answers(const DomainArgs& a) { return a.active ? a.n_ans : 0u; }
-__device__ __forceinline__ uint32_t pending_cells(const DomainArgs& a) { return a.active ? a.st->npend_prev : 0u; }
-
-__global__ void __launch_bounds__(kBlock) k_apply_answers(int base, int ndom) {
-    __shared__ uint32_t s_pre[kMaxSegs + 1];
-    const uint32_t total = seg_prefix(s_pre, ndom, [&](int s) { return answers(c_args[base + (s)]); });
-    for (uint32_t u = blockIdx.x * blockDim.x + threadIdx.x; u < total; u += gridDim.x * blockDim.x) {
-        const int s = seg_find(s_pre, ndom, u);
-        const DomainArgs& a = c_args[base + (s)];
-        const uint32_t i = u - s_pre[s];
-        a.ptab[a.ans_idx[i]] = (unsigned long long)__double_as_longlong(a.ans_val[i]);
-    }
-}
-
-template <bool FP32>
-__global__ void __launch_bounds__(kBlock) k_fix_pending(int base, int ndom) {
-    __shared__ uint32_t s_pre[kMaxSegs + 1];
-    const uint32_t total = seg_prefix(s_pre, ndom, [&](int s) { return pending_cells(c_args[base + (s)]); });
-    for (uint32_t u = blockIdx.x * blockDim.x + threadIdx.x; u < total; u += gridDim.x * blockDim.x) {
-        const int s = seg_find(s_pre, ndom, u);
-        const DomainArgs& a = c_args[base + (s)];
-        const uint32_t e = a.pending[u - s_pre[s]];
-        const int D = (int)(e >> 31);
-        const uint32_t slot = e & 0x7FFFFFFFu;
-        const DFront& f = a.f[D];
-        const uint32_t g = f.defg[slot];
-        const double P = __longlong_as_double((long long)a.ptab[(unsigned long long)f.rxg[slot] * a.ndefg + g]);
-        const double v = velocity_factor(a, P, g, f.dir[slot] & kCodeMask);
-        if (!FP32) ((double*)f.vel)[slot] = v;
-        else ((float*)f.vel)[slot] = (float)v;
     }
 }
 
