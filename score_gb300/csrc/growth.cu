@@ -906,12 +906,11 @@ void launch_sequence_t(const Engine& E, int n) {
     record(E, 3);
     k_resolve<<<S * (uint32_t)E.cfg.commit_bpsm, kBlock, 0, st>>>(d, n);
     k_commit<FP32><<<S * (uint32_t)E.cfg.commit_bpsm, kBlock, 0, st>>>(d, n);
-    k_new_vel<FP32><<<S * 8, kBlock, 0, st>>>(d, n);
     k_step_end<<<(uint32_t)n, kBlock, 0, st>>>(d, n, (uint32_t)(kBlock * E.cfg.items));
     record(E, 4);
 }
 
-constexpr int kStepKernels = 8;
+constexpr int kStepKernels = 7;
 
 }  // namespace
 
@@ -1138,7 +1137,7 @@ int make_ctx(const score_params* p, Engine* eng, bool own, score_ctx** out) {
 // keeps slot order and claims are decided by ordinal) while cycling candidate
 // configurations step by step, and keeps per kernel group the candidate with the least
 // time per unit of work: k_grow_fill + k_grow_lists per front slot, k_claim per full
-// cell, k_resolve + k_commit + k_new_vel per full cell.  Direct launches while tuning.
+// cell, k_resolve + k_commit per full cell.  Direct launches while tuning.
 int Engine::autotune(double x_target, uint32_t max_steps, score_tune* out) {
     static const int kItems[3] = {4, 8, 16};
     static const int kFill[4] = {4, 8, 16, 32};

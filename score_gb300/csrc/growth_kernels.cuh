@@ -29,8 +29,10 @@
 //             order and take recycled slots first, then appended slots, like
 //             omp_getNextFreeSlotInRXFront*(CELLRECYCLE).  The full cell then becomes
 //             recrystallized (grid = ndefg + rxg, counts, slot INACTIVE) — the tail of
-//             updateFullRX{Inside,Border}, SCORE_Kernel.cpp:4559-4774.
-//   k_new_vel one thread per new cell: mobility weight P and cached velocity factor.
+//             updateFullRX{Inside,Border}, SCORE_Kernel.cpp:4559-4774.  The wins of a
+//             tile are spread over all its threads; each new cell gets its mobility
+//             weight P (table, device classification, or a tag for the host) and
+//             cached velocity factor.
 //   k_step_end  slot high-water marks, stats snapshot, reset of the per-step fields.
 #pragma once
 #include <cstdint>
@@ -836,14 +838,39 @@ __global__ void __launch_bounds__(kBlock, 4) k_resolve(int base, int ndom) {
     }
 }
 
+// warp-reduced running P max (ordered bits of a positive double) and tagged-cell count
+__device__ __forceinline__ void flush_new(const DomainArgs& a, double pmax, uint32_t ntag) {
+    unsigned long long b = (unsigned long long)__double_as_longlong(pmax);
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+        const unsigned long long x = __shfl_xor_sync(0xFFFFFFFFu, b, o);
+        if (x > b) b = x;
+        ntag += __shfl_xor_sync(0xFFFFFFFFu, ntag, o);
+    }
+    if ((threadIdx.x & 31) == 0) {
+        if (b) atomicMax(&a.st->pmax_bits, b);
+        if (ntag) atomicAdd(&a.st->ntagged, ntag);
+    }
+}
+
 template <bool FP32>
-__global__ void __launch_bounds__(kBlock, 4) k_commit(int base, int ndom) {
+__global__ void __launch_bounds__(kBlock, 3) k_commit(int base, int ndom) {
     __shared__ uint32_t s_pre[kMaxSegs + 1];
-    __shared__ uint32_t s_a[kWarps], s_b[kWarps], s_base[2];
+    __shared__ uint32_t s_a[kWarps], s_b[kWarps], s_w[kWarps], s_base[2];
+    // per full cell of the tile: win masks, first ranks, cell (| Border list << 31), grain, overshoot
+    __shared__ uint32_t s_off[kBlock + 1], s_win[kBlock], s_tob[kBlock], s_rA[kBlock], s_rB[kBlock], s_cell[kBlock], s_rsrc[kBlock];
+    __shared__ double s_over[kBlock];
     const uint32_t total = seg_prefix(s_pre, ndom, [&](int s) { return commit_tiles(c_args[base + (s)]); });
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    int cur = -1;           // domain whose P max and tag count are being accumulated
+    double pmax = 0.0;      // max of the new positive weights
+    uint32_t ntag = 0;      // new cells waiting for the host
     for (uint32_t u = blockIdx.x; u < total; u += gridDim.x) {
         const int s = seg_find(s_pre, ndom, u);
+        if (s != cur) {
+            if (cur >= 0) flush_new(c_args[base + cur], pmax, ntag);
+            cur = s; pmax = 0.0; ntag = 0;
+        }
         const DomainArgs& a = c_args[base + (s)];
         const uint32_t tile = u - s_pre[s];
         const uint32_t F0 = a.st->nfull[0], F = F0 + a.st->nfull[1];
@@ -854,19 +881,29 @@ __global__ void __launch_bounds__(kBlock, 4) k_commit(int base, int ndom) {
             if (lane == 0) { s_base[0] = pa; s_base[1] = pb; }
         }
         const uint32_t win = f < F ? a.amask[f] : 0u, tob = f < F ? a.tobm[f] : 0u;
-        const uint32_t cB = __popc(tob), cA = __popc(win) - cB;
-        uint32_t iA = cA, iB = cB;
+        const uint32_t cB = __popc(tob), cA = __popc(win) - cB, cW = cA + cB;
+        uint32_t iA = cA, iB = cB, iW = cW;
 #pragma unroll
         for (int o = 1; o < 32; o <<= 1) {
             const uint32_t xa = __shfl_up_sync(0xFFFFFFFFu, iA, o), xb = __shfl_up_sync(0xFFFFFFFFu, iB, o);
-            if (lane >= o) { iA += xa; iB += xb; }
+            const uint32_t xw = __shfl_up_sync(0xFFFFFFFFu, iW, o);
+            if (lane >= o) { iA += xa; iB += xb; iW += xw; }
         }
-        if (lane == 31) { s_a[warp] = iA; s_b[warp] = iB; }
+        if (lane == 31) { s_a[warp] = iA; s_b[warp] = iB; s_w[warp] = iW; }
+        // the full cell's own data, loaded while the scans complete
+        const int L = f >= F0 ? 1 : 0;
+        uint32_t slot = 0, cell = 0, rsrc = 0, gsrc = 0;
+        if (f < F) {
+            slot = a.f[L].full[L ? f - F0 : f];
+            cell = a.f[L].xyz[slot];
+            rsrc = a.f[L].rxg[slot];
+            gsrc = a.f[L].defg[slot];
+        }
         __syncthreads();
-        uint32_t rA = s_base[0] + iA - cA, rB = s_base[1] + iB - cB;
+        uint32_t rA = s_base[0] + iA - cA, rB = s_base[1] + iB - cB, oW = iW - cW;
 #pragma unroll
         for (int w = 0; w < kWarps; ++w)
-            if (w < warp) { rA += s_a[w]; rB += s_b[w]; }
+            if (w < warp) { rA += s_a[w]; rB += s_b[w]; oW += s_w[w]; }
         if (threadIdx.x == 0 && tile + 1 == s_pre[s + 1] - s_pre[s]) {  // the domain's last tile: totals
             uint32_t ta = 0, tb = 0;
 #pragma unroll
@@ -874,52 +911,83 @@ __global__ void __launch_bounds__(kBlock, 4) k_commit(int base, int ndom) {
             a.st->nwin[0] = s_base[0] + ta;
             a.st->nwin[1] = s_base[1] + tb;
         }
-        if (f < F) {
-            const int L = f >= F0 ? 1 : 0;
-            const DFront& src = a.f[L];
-            const uint32_t slot = src.full[L ? f - F0 : f];
-            const uint32_t cell = src.xyz[slot];
-            const uint32_t rsrc = src.rxg[slot], gsrc = src.defg[slot];
-            if (win) {
-                int x, y, z;
-                decode(a, cell, x, y, z);
-                double over = 0.0;
-                float over32 = 0.0f;
-                if (!FP32) over = __dsub_rn(((const double*)src.fill)[slot], 1.0);
-                else over32 = (((const float*)src.fill)[slot] - 1.0f) - src.comp[slot];
-                uint32_t m = win;
-                while (m) {
-                    const int d = __ffs(m) - 1;
-                    m &= m - 1;
-                    uint32_t t;
-                    bool inter;
-                    target_of(a, L, x, y, z, d, t, inter);
-                    const int D = (tob >> d) & 1u;
-                    const uint32_t r = D ? rB++ : rA++;
-                    const DFront& dst = a.f[D];
-                    const uint32_t nrec = a.st->nrec[D];
-                    const uint32_t ns = r < nrec ? dst.recyc[r] : a.st->next_never[D] + (r - nrec);
-                    if (ns >= dst.cap) { atomicOr(&a.st->err, kErrCapacity); continue; }
-                    if (D == 1 && a.border_policy == 0 && r >= nrec && ns >= a.border_ref_cap) atomicOr(&a.st->err, kErrBorderRef);
-                    const uint32_t gt = a.grid[t];
-                    const int cls = c_cls[d];
-                    if (!FP32) {
-                        const double fac = cls == 1 ? 0.0682 : (cls == 2 ? 0.0542 : 0.0484);
-                        ((double*)dst.fill)[ns] = __dmul_rn(over, fac);
-                    } else {
-                        const float fac = cls == 1 ? 0.0682f : (cls == 2 ? 0.0542f : 0.0484f);
-                        ((float*)dst.fill)[ns] = over32 * fac;
-                        dst.comp[ns] = 0.0f;
-                    }
-                    dst.dir[ns] = c_code[d] | kStale;  // vel follows in k_new_vel
-                    dst.defg[ns] = gt;
-                    dst.rxg[ns] = rsrc;
-                    dst.xyz[ns] = t;
-                    a.grid[t] = 4096002000u;  // CURRENTLY_INFECTED
-                    a.claim[t] = kClaimFree;
-                }
+        s_off[threadIdx.x] = oW;
+        if (threadIdx.x == kBlock - 1) s_off[kBlock] = oW + cW;
+        s_win[threadIdx.x] = win;
+        s_tob[threadIdx.x] = tob;
+        s_rA[threadIdx.x] = rA;
+        s_rB[threadIdx.x] = rB;
+        s_cell[threadIdx.x] = cell | ((uint32_t)L << 31);
+        s_rsrc[threadIdx.x] = rsrc;
+        if (win) {
+            if (!FP32) s_over[threadIdx.x] = __dsub_rn(((const double*)a.f[L].fill)[slot], 1.0);
+            else s_over[threadIdx.x] = (double)((((const float*)a.f[L].fill)[slot] - 1.0f) - a.f[L].comp[slot]);
+        }
+        __syncthreads();
+        // every win of the tile by all threads: win k belongs to the full cell t with
+        // s_off[t] <= k < s_off[t + 1]; its direction is the (k - s_off[t])-th set bit and
+        // its rank in the destination list counts the cell's earlier wins there
+        const uint32_t W = s_off[kBlock];
+        for (uint32_t k = threadIdx.x; k < W; k += kBlock) {
+            int lo = 0, hi = kBlock - 1;
+            while (lo < hi) {
+                const int mid = (lo + hi + 1) >> 1;
+                if (s_off[mid] <= k) lo = mid;
+                else hi = mid - 1;
             }
+            const int t = lo;
+            const uint32_t m = s_win[t], tb = s_tob[t];
+            const int d = (int)__fns(m, 0u, (int)(k - s_off[t]) + 1);
+            const int D = (tb >> d) & 1u;
+            const uint32_t below = m & ((1u << d) - 1u);
+            const uint32_t r = D ? s_rB[t] + __popc(below & tb) : s_rA[t] + __popc(below & ~tb);
+            const uint32_t sc = s_cell[t];
+            const int Ls = (int)(sc >> 31);
+            int x, y, z;
+            decode(a, sc & 0x7FFFFFFFu, x, y, z);
+            uint32_t tgt;
+            bool inter;
+            target_of(a, Ls, x, y, z, d, tgt, inter);
+            const DFront& dst = a.f[D];
+            const uint32_t nrec = a.st->nrec[D];
+            const uint32_t ns = r < nrec ? dst.recyc[r] : a.st->next_never[D] + (r - nrec);
+            if (ns >= dst.cap) { atomicOr(&a.st->err, kErrCapacity); continue; }
+            if (D == 1 && a.border_policy == 0 && r >= nrec && ns >= a.border_ref_cap) atomicOr(&a.st->err, kErrBorderRef);
+            const uint32_t gt = a.grid[tgt];
+            const int cls = c_cls[d];
+            if (!FP32) {
+                const double fac = cls == 1 ? 0.0682 : (cls == 2 ? 0.0542 : 0.0484);
+                ((double*)dst.fill)[ns] = __dmul_rn(s_over[t], fac);
+            } else {
+                const float fac = cls == 1 ? 0.0682f : (cls == 2 ? 0.0542f : 0.0484f);
+                ((float*)dst.fill)[ns] = (float)s_over[t] * fac;
+                dst.comp[ns] = 0.0f;
+            }
+            const uint32_t rs = s_rsrc[t];
+            dst.defg[ns] = gt;
+            dst.rxg[ns] = rs;
+            dst.xyz[ns] = tgt;
+            a.grid[tgt] = 4096002000u;  // CURRENTLY_INFECTED
+            a.claim[tgt] = kClaimFree;
+            // mobility weight and cached velocity factor of the new cell
+            double P = 0.0;
+            uint32_t tag = 0;
+            if (lookup_p(a, rs, gt, P, tag)) {
+                if (!FP32) ((double*)dst.vel)[ns] = velocity_factor(a, P, gt, c_code[d]);
+                else ((float*)dst.vel)[ns] = (float)velocity_factor(a, P, gt, c_code[d]);
+                dst.dir[ns] = c_code[d] | kStale;
+                if (P > pmax) pmax = P;
+            } else {
+                // vel holds the answer tag until the next k_grow_fill
+                if (!FP32) ((unsigned long long*)dst.vel)[ns] = tag;
+                else ((uint32_t*)dst.vel)[ns] = tag;
+                dst.dir[ns] = c_code[d] | kStale | kPend;
+                ++ntag;
+            }
+        }
+        if (f < F) {
             // the full cell is now recrystallized
+            const DFront& src = a.f[L];
             a.grid[cell] = a.ndefg + rsrc;
             src.dir[slot] = kInactive;
             if (!FP32) ((double*)src.fill)[slot] = 0.0;
@@ -930,13 +998,6 @@ __global__ void __launch_bounds__(kBlock, 4) k_commit(int base, int ndom) {
         {
             const bool has = f < F;
             const uint32_t act = __ballot_sync(0xFFFFFFFFu, has);
-            uint32_t rsrc = 0, gsrc = 0;
-            if (has) {
-                const int L = f >= F0 ? 1 : 0;
-                const uint32_t slot = a.f[L].full[L ? f - F0 : f];
-                rsrc = a.f[L].rxg[slot];
-                gsrc = a.f[L].defg[slot];
-            }
             const uint32_t mr = __match_any_sync(0xFFFFFFFFu, has ? rsrc : 0xFFFFFFFFu) & act;
             const uint32_t mg = __match_any_sync(0xFFFFFFFFu, has ? gsrc : 0xFFFFFFFFu) & act;
             if (has && (__ffs(mr) - 1) == lane) atomicAdd(&a.rxg_cnt[rsrc], (uint32_t)__popc(mr));
@@ -951,63 +1012,7 @@ __global__ void __launch_bounds__(kBlock, 4) k_commit(int base, int ndom) {
         }
         __syncthreads();
     }
-}
-
-// k_new_vel: one thread per cell infected this step (both lists, in rank order):
-// P(rxg, defg) from the table (classified on the device when exact, else requested
-// from the host: vel = -1 and the slot goes on the pending list) and the cached
-// velocity factor; the running P max over the new weights.
-__device__ __forceinline__ uint32_t new_cells(const DomainArgs& a) { return a.active ? a.st->nwin[0] + a.st->nwin[1] : 0u; }
-
-template <bool FP32>
-__global__ void __launch_bounds__(kBlock, 4) k_new_vel(int base, int ndom) {
-    __shared__ uint32_t s_pre[kMaxSegs + 1], s_cnt[kMaxSegs];
-    const uint32_t total = seg_prefix(s_pre, ndom, [&](int s) {
-        s_cnt[s] = new_cells(c_args[base + (s)]);
-        return warp_pad(s_cnt[s]);
-    });
-    for (uint32_t u = blockIdx.x * blockDim.x + threadIdx.x; u < total; u += gridDim.x * blockDim.x) {
-        const int s = seg_find(s_pre, ndom, u);
-        const DomainArgs& a = c_args[base + (s)];
-        const uint32_t i = u - s_pre[s];
-        if (i >= s_cnt[s]) continue;
-        const uint32_t n0 = a.st->nwin[0];
-        const int D = i >= n0 ? 1 : 0;
-        const uint32_t r = D ? i - n0 : i;
-        const DFront& dst = a.f[D];
-        const uint32_t nrec = a.st->nrec[D];
-        const uint32_t ns = r < nrec ? dst.recyc[r] : a.st->next_never[D] + (r - nrec);
-        if (ns >= dst.cap) continue;  // k_commit flagged the overflow
-        const uint32_t gt = dst.defg[ns];
-        const uint8_t dir = dst.dir[ns];
-        double P = 0.0;
-        uint32_t tag = 0;
-        const bool known = lookup_p(a, dst.rxg[ns], gt, P, tag);
-        if (known) {
-            if (!FP32) ((double*)dst.vel)[ns] = velocity_factor(a, P, gt, dir & kCodeMask);
-            else ((float*)dst.vel)[ns] = (float)velocity_factor(a, P, gt, dir & kCodeMask);
-        } else {
-            // vel holds the answer tag until the next k_grow_fill
-            if (!FP32) ((unsigned long long*)dst.vel)[ns] = tag;
-            else ((uint32_t*)dst.vel)[ns] = tag;
-            dst.dir[ns] = dir | kPend;
-        }
-        if (!known) {
-            atomicAdd(&a.st->ntagged, 1u);
-        } else if (P > 0.0) {
-            // running max of the new weights: one atomic per distinct value in the warp
-            const unsigned long long bits = (unsigned long long)__double_as_longlong(P);
-            const uint32_t act = __activemask();
-            unsigned long long m = bits;
-            for (int o = 16; o > 0; o >>= 1) {
-                const unsigned long long x = __shfl_xor_sync(act, m, o);
-                const bool src_on = (act >> ((threadIdx.x & 31) ^ o)) & 1u;
-                if (src_on && x > m) m = x;
-            }
-            if (m == bits && (__ffs(__match_any_sync(act, bits)) - 1) == (int)(threadIdx.x & 31))
-                atomicMax(&a.st->pmax_bits, bits);
-        }
-    }
+    if (cur >= 0) flush_new(c_args[base + cur], pmax, ntag);
 }
 
 // ------------------------------------------------------------------ K4 step end
