@@ -13,7 +13,7 @@ until X > 0.99.  Inputs are synthetic and seeded (rank r uses seed r).
           copies the domain in (score_load_domain) and the labels out.
   roofline  k_grow_fill (the dominant kernel): algorithmic bytes (25 B per FP64
           front-cell update: infector byte, cached increment, fill read and write;
-          17 B FP32+Kahan) / its event-timed duration, against the measured HBM
+          21 B FP32+Kahan: byte, velocity factor, fill and compensation read and write) / its event-timed duration, against the measured HBM
           copy bandwidth.
   cpu_baseline  the C oracle (single thread) on a bounded 256^3 sample of the
           same workload (same grain and nucleus densities), run to X > 0.99.
@@ -52,7 +52,8 @@ X_TARGET = 0.99
 # algorithmic bytes of one front-cell update in k_grow_fill: FP64 reads the infector byte,
 # the cached increment and the fill and writes the fill (1 + 8 + 8 + 8); FP32+Kahan
 # reads byte, velocity factor, fill and compensation and writes fill and compensation
-BYTES_PER_UPDATE = {0: 25.0, 1: 17.0}
+# (1 + 4 + 4 + 4 + 4 + 4)
+BYTES_PER_UPDATE = {0: 25.0, 1: 21.0}
 METRIC = "front-cell updates/s (RX growth step to X=0.99)"
 WORKLOAD = "512^3 Voronoi domain, 20000 deformed grains, 50000 site-saturated nuclei, FP64, T=1000K, until X>0.99"
 

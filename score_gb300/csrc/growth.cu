@@ -1025,7 +1025,7 @@ int Engine::step(bool timed) {
         tm.total_ms += g + cl + cm;
     }
     tm.grow_launches += 1;
-    const double bpu = fp32 ? 17.0 : 25.0;  // algorithmic bytes per front-cell update of k_grow_fill
+    const double bpu = fp32 ? 21.0 : 25.0;  // algorithmic bytes per front-cell update of k_grow_fill
     // the master-block work of each domain (weights, physics, dt) is independent
     std::vector<int> status(n, SCORE_OK);
     auto post = [&](int i) {
