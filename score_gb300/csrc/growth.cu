@@ -305,8 +305,8 @@ void score_ctx::release_stream() {
 struct TuneCfg {
     int items = 8;          // grow tile = kBlock * items slots
     int fill_bpsm = 16;     // k_grow_fill blocks per SM
-    int claim_bpsm = 4;     // k_claim blocks per SM
-    int commit_bpsm = 4;    // k_resolve / k_commit blocks per SM
+    int claim_bpsm = 2;     // k_claim blocks per SM (autotuner's choice on the 512^3 workload)
+    int commit_bpsm = 8;    // k_resolve / k_commit blocks per SM (same)
     bool operator==(const TuneCfg& o) const {
         return items == o.items && fill_bpsm == o.fill_bpsm && claim_bpsm == o.claim_bpsm && commit_bpsm == o.commit_bpsm;
     }
@@ -887,7 +887,8 @@ inline void record(const Engine& E, int k) {
 
 template <bool FP32, int ITEMS>
 void launch_grow(const Engine& E, int n) {
-    k_grow_fill<FP32, ITEMS><<<(uint32_t)(E.sms * E.cfg.fill_bpsm), kBlock, 0, E.stream>>>(E.base, n);
+    if (n == 1) k_grow_fill<FP32, ITEMS, true><<<(uint32_t)(E.sms * E.cfg.fill_bpsm), kBlock, 0, E.stream>>>(E.base, n);
+    else k_grow_fill<FP32, ITEMS, false><<<(uint32_t)(E.sms * E.cfg.fill_bpsm), kBlock, 0, E.stream>>>(E.base, n);
     record(E, 1);
     k_grow_lists<ITEMS><<<(uint32_t)E.sms * 8, kBlock, 0, E.stream>>>(E.base, n);
 }
@@ -902,10 +903,16 @@ void launch_sequence_t(const Engine& E, int n) {
     else if (E.cfg.items == 16) launch_grow<FP32, 16>(E, n);
     else launch_grow<FP32, 8>(E, n);
     record(E, 2);
-    k_claim<<<S * (uint32_t)E.cfg.claim_bpsm, kBlock, 0, st>>>(d, n);
+    if (n == 1) k_claim<true><<<S * (uint32_t)E.cfg.claim_bpsm, kBlock, 0, st>>>(d, n);
+    else k_claim<false><<<S * (uint32_t)E.cfg.claim_bpsm, kBlock, 0, st>>>(d, n);
     record(E, 3);
-    k_resolve<<<S * (uint32_t)E.cfg.commit_bpsm, kBlock, 0, st>>>(d, n);
-    k_commit<FP32><<<S * (uint32_t)E.cfg.commit_bpsm, kBlock, 0, st>>>(d, n);
+    if (n == 1) {
+        k_resolve<true><<<S * (uint32_t)E.cfg.commit_bpsm, kBlock, 0, st>>>(d, n);
+        k_commit<FP32, true><<<S * (uint32_t)E.cfg.commit_bpsm, kBlock, 0, st>>>(d, n);
+    } else {
+        k_resolve<false><<<S * (uint32_t)E.cfg.commit_bpsm, kBlock, 0, st>>>(d, n);
+        k_commit<FP32, false><<<S * (uint32_t)E.cfg.commit_bpsm, kBlock, 0, st>>>(d, n);
+    }
     k_step_end<<<(uint32_t)n, kBlock, 0, st>>>(d, n, (uint32_t)(kBlock * E.cfg.items));
     record(E, 4);
 }

@@ -436,11 +436,30 @@ __device__ __forceinline__ void flush_sv(const DomainArgs& a, int L, uint32_t sv
 // slots of list L of a domain this step ( 0 for a domain that is not stepping)
 __device__ __forceinline__ uint32_t list_slots(const DomainArgs& a, int L) { return a.active ? a.st->next_never[L] : 0u; }
 
-template <bool FP32, int ITEMS>
+// ONE: a single domain (the plain path): its argument block sits at a launch-uniform
+// slot and the two lists are walked in turn, so every argument read is uniform.
+template <bool FP32, int ITEMS, bool ONE>
 __global__ void __launch_bounds__(kBlock, ITEMS >= 16 ? 2 : 4) k_grow_fill(int base, int ndom) {
     using S = GrowShape<ITEMS>;
     __shared__ uint32_t s_pre[kMaxSegs + 1];
     __shared__ uint32_t s_f[kWarps], s_i[kWarps];
+    if (ONE) {
+        const DomainArgs& a = c_args[base];
+        if (!a.active) return;
+#pragma unroll
+        for (int L = 0; L < 2; ++L) {
+            const uint32_t n = a.st->next_never[L];
+            const uint32_t ntiles = (n + S::kTile - 1) / S::kTile;
+            uint32_t sv = 0;
+            if (a.refresh) {
+                for (uint32_t tile = blockIdx.x; tile < ntiles; tile += gridDim.x) sv += grow_tile<FP32, true, ITEMS>(a, L, tile, n, s_f, s_i);
+            } else {
+                for (uint32_t tile = blockIdx.x; tile < ntiles; tile += gridDim.x) sv += grow_tile<FP32, false, ITEMS>(a, L, tile, n, s_f, s_i);
+            }
+            flush_sv(a, L, sv);
+        }
+        return;
+    }
     const int nseg = 2 * ndom;
     const uint32_t total = seg_prefix(s_pre, nseg, [&](int s) {
         return (list_slots(c_args[base + (s >> 1)], s & 1) + S::kTile - 1) / S::kTile;
@@ -619,19 +638,28 @@ __device__ __forceinline__ uint32_t full_cells(const DomainArgs& a) {
     return 26ull * F >= 0xFFFFFFFFull ? 0u : F;
 }
 
+template <bool ONE>
 __global__ void __launch_bounds__(kBlock, 4) k_claim(int base, int ndom) {
     __shared__ uint32_t s_pre[kMaxSegs + 1], s_cnt[kMaxSegs];
-    const uint32_t total = seg_prefix(s_pre, ndom, [&](int s) {
+    auto count = [&](int s) {
         const DomainArgs& a = c_args[base + (s)];
         if (a.active && 26ull * (a.st->nfull[0] + a.st->nfull[1]) >= 0xFFFFFFFFull) atomicOr(&a.st->err, kErrKeyLimit);
-        s_cnt[s] = full_cells(a);
-        return warp_pad(s_cnt[s]);
-    });
+        return full_cells(a);
+    };
+    uint32_t total;
+    if (ONE) {
+        total = count(0);
+    } else {
+        total = seg_prefix(s_pre, ndom, [&](int s) {
+            s_cnt[s] = count(s);
+            return warp_pad(s_cnt[s]);
+        });
+    }
     for (uint32_t u = blockIdx.x * blockDim.x + threadIdx.x; u < total; u += gridDim.x * blockDim.x) {
-        const int s = seg_find(s_pre, ndom, u);
+        const int s = ONE ? 0 : seg_find(s_pre, ndom, u);
         const DomainArgs& a = c_args[base + (s)];
-        const uint32_t f = u - s_pre[s];
-        if (f >= s_cnt[s]) continue;
+        const uint32_t f = ONE ? u : u - s_pre[s];
+        if (!ONE && f >= s_cnt[s]) continue;
         const uint32_t F0 = a.st->nfull[0];
         uint32_t mask;
         if (f < F0) {
@@ -774,15 +802,17 @@ __device__ __forceinline__ bool lookup_p(const DomainArgs& a, uint32_t rxg, uint
 // full cell then becomes recrystallized (grid = ndefg + rxg, counts, slot INACTIVE).
 __device__ __forceinline__ uint32_t commit_tiles(const DomainArgs& a) { return (full_cells(a) + kBlock - 1) / kBlock; }
 
+template <bool ONE>
 __global__ void __launch_bounds__(kBlock, 4) k_resolve(int base, int ndom) {
     __shared__ uint32_t s_pre[kMaxSegs + 1];
     __shared__ uint32_t s_a[kWarps], s_b[kWarps];
-    const uint32_t total = seg_prefix(s_pre, ndom, [&](int s) { return commit_tiles(c_args[base + (s)]); });
+    const uint32_t total = ONE ? commit_tiles(c_args[base])
+                               : seg_prefix(s_pre, ndom, [&](int s) { return commit_tiles(c_args[base + (s)]); });
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     for (uint32_t u = blockIdx.x; u < total; u += gridDim.x) {
-        const int s = seg_find(s_pre, ndom, u);
+        const int s = ONE ? 0 : seg_find(s_pre, ndom, u);
         const DomainArgs& a = c_args[base + (s)];
-        const uint32_t tile = u - s_pre[s];
+        const uint32_t tile = ONE ? u : u - s_pre[s];
         const uint32_t F0 = a.st->nfull[0], F = F0 + a.st->nfull[1];
         const uint32_t f = tile * kBlock + threadIdx.x;
         uint32_t win = 0, tob = 0;
@@ -853,26 +883,27 @@ __device__ __forceinline__ void flush_new(const DomainArgs& a, double pmax, uint
     }
 }
 
-template <bool FP32>
+template <bool FP32, bool ONE>
 __global__ void __launch_bounds__(kBlock, 3) k_commit(int base, int ndom) {
     __shared__ uint32_t s_pre[kMaxSegs + 1];
     __shared__ uint32_t s_a[kWarps], s_b[kWarps], s_w[kWarps], s_base[2];
     // per full cell of the tile: win masks, first ranks, cell (| Border list << 31), grain, overshoot
     __shared__ uint32_t s_off[kBlock + 1], s_win[kBlock], s_tob[kBlock], s_rA[kBlock], s_rB[kBlock], s_cell[kBlock], s_rsrc[kBlock];
     __shared__ double s_over[kBlock];
-    const uint32_t total = seg_prefix(s_pre, ndom, [&](int s) { return commit_tiles(c_args[base + (s)]); });
+    const uint32_t total = ONE ? commit_tiles(c_args[base])
+                               : seg_prefix(s_pre, ndom, [&](int s) { return commit_tiles(c_args[base + (s)]); });
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     int cur = -1;           // domain whose P max and tag count are being accumulated
     double pmax = 0.0;      // max of the new positive weights
     uint32_t ntag = 0;      // new cells waiting for the host
     for (uint32_t u = blockIdx.x; u < total; u += gridDim.x) {
-        const int s = seg_find(s_pre, ndom, u);
+        const int s = ONE ? 0 : seg_find(s_pre, ndom, u);
         if (s != cur) {
             if (cur >= 0) flush_new(c_args[base + cur], pmax, ntag);
             cur = s; pmax = 0.0; ntag = 0;
         }
         const DomainArgs& a = c_args[base + (s)];
-        const uint32_t tile = u - s_pre[s];
+        const uint32_t tile = ONE ? u : u - s_pre[s];
         const uint32_t F0 = a.st->nfull[0], F = F0 + a.st->nfull[1];
         const uint32_t f = tile * kBlock + threadIdx.x;
         if (warp == 0) {
@@ -904,7 +935,7 @@ __global__ void __launch_bounds__(kBlock, 3) k_commit(int base, int ndom) {
 #pragma unroll
         for (int w = 0; w < kWarps; ++w)
             if (w < warp) { rA += s_a[w]; rB += s_b[w]; oW += s_w[w]; }
-        if (threadIdx.x == 0 && tile + 1 == s_pre[s + 1] - s_pre[s]) {  // the domain's last tile: totals
+        if (threadIdx.x == 0 && tile + 1 == (ONE ? total : s_pre[s + 1] - s_pre[s])) {  // the domain's last tile: totals
             uint32_t ta = 0, tb = 0;
 #pragma unroll
             for (int w = 0; w < kWarps; ++w) { ta += s_a[w]; tb += s_b[w]; }
