@@ -1354,7 +1354,7 @@ int score_load_domain(score_ctx* c, const uint32_t* grid, const double* defg_qua
             c->scnt_words[L] = 2 * (tiles / kSuper + 2);
             if (e == cudaSuccess) e = dalloc(&f.fmask, words);
             if (e == cudaSuccess) e = dalloc(&f.imask, words);
-            if (e == cudaSuccess) e = dalloc(&f.tcnt, 2 * tiles);
+            if (e == cudaSuccess) e = dalloc(&f.tcnt, 2 * tiles * kWarps);
             if (e == cudaSuccess) e = dalloc(&f.scnt, c->scnt_words[L]);
         }
         c->csct_words = 2 * ((N / kBlock + 2) / kSuper + 2);

@@ -53,7 +53,7 @@ struct DFront {
     uint32_t* recyc;     // recycle list (slot indices, slot order, capped)
     uint32_t* fmask;     // per 32 slots: full slots of this step (bit = slot % 32)
     uint32_t* imask;     // per 32 slots: INACTIVE slots of this step
-    uint32_t* tcnt;      // per grow tile: (full, INACTIVE) counts
+    uint32_t* tcnt;      // per warp of a grow tile: (full, INACTIVE) counts
     uint32_t* scnt;      // per supertile of kSuper grow tiles: the same counts (zero between steps)
     uint32_t cap;        // device capacity of the slot arrays
     uint32_t reccap;     // ntotalRecyclingList of the reference
@@ -263,14 +263,15 @@ struct GrowShape {
 };
 constexpr uint32_t kSuper = 64;  // tiles per supertile of the two-level tile prefix
 
-// Exclusive prefix of tile `tile` of a (cnt: per-tile pairs, sup: per-supertile pairs)
-// count array, computed by one warp; every lane returns both prefixes.
-__device__ __forceinline__ void tile_prefix(const uint32_t* cnt, const uint32_t* sup, uint32_t tile, uint32_t& pa, uint32_t& pb) {
+// Exclusive prefix of tile `tile` of a (cnt: count pairs, `per` entries per tile;
+// sup: per-supertile pairs) count array, computed by one warp; every lane returns both.
+__device__ __forceinline__ void tile_prefix(const uint32_t* cnt, const uint32_t* sup, uint32_t tile, uint32_t& pa, uint32_t& pb,
+                                            uint32_t per = 1) {
     const int lane = threadIdx.x & 31;
     const uint32_t s = tile / kSuper;
     uint32_t a = 0, b = 0;
     for (uint32_t i = lane; i < s; i += 32) { a += sup[2 * i]; b += sup[2 * i + 1]; }
-    for (uint32_t i = s * kSuper + lane; i < tile; i += 32) { a += cnt[2 * i]; b += cnt[2 * i + 1]; }
+    for (uint32_t i = s * kSuper * per + lane; i < tile * per; i += 32) { a += cnt[2 * i]; b += cnt[2 * i + 1]; }
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) {
         a += __shfl_xor_sync(0xFFFFFFFFu, a, o);
@@ -301,16 +302,17 @@ __device__ __forceinline__ double answered_velocity(const DomainArgs& a, const D
 
 // returns the thread's ACTIVE slots (the Sv share)
 template <bool FP32, bool REFRESH, int ITEMS>
-__device__ __forceinline__ uint32_t grow_tile(const DomainArgs& a, int L, uint32_t tile, uint32_t n, uint32_t* s_f, uint32_t* s_i) {
+__device__ __forceinline__ uint32_t grow_tile(const DomainArgs& a, int L, uint32_t tile, uint32_t n) {
     using S = GrowShape<ITEMS>;
     const DFront& fr = a.f[L];
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    const uint32_t base = tile * S::kTile;
+    // each warp owns 32 * ITEMS consecutive slots of the tile: no block barrier, warps run apart
+    const uint32_t base = tile * S::kTile + (uint32_t)warp * 32u * ITEMS + (uint32_t)lane;
     uint32_t sv = 0;
     uint8_t d[ITEMS];
 #pragma unroll
     for (int k = 0; k < ITEMS; ++k) {
-        const uint32_t slot = base + (uint32_t)(k * kBlock) + threadIdx.x;
+        const uint32_t slot = base + (uint32_t)(k * 32);
         d[k] = slot < n ? fr.dir[slot] : kInactive;
     }
     bool full[ITEMS];
@@ -318,7 +320,7 @@ __device__ __forceinline__ uint32_t grow_tile(const DomainArgs& a, int L, uint32
         double w[ITEMS], fill[ITEMS];  // w: cached inc, or vel when the increment is stale
 #pragma unroll
         for (int k = 0; k < ITEMS; ++k) {
-            const uint32_t slot = base + (uint32_t)(k * kBlock) + threadIdx.x;
+            const uint32_t slot = base + (uint32_t)(k * 32);
             w[k] = -1.0; fill[k] = 0.0;
             if (d[k] != kInactive) {
                 if (d[k] & kPend) {
@@ -342,7 +344,7 @@ __device__ __forceinline__ uint32_t grow_tile(const DomainArgs& a, int L, uint32
             full[k] = false;
             if (d[k] != kInactive) {
                 ++sv;
-                const uint32_t slot = base + (uint32_t)(k * kBlock) + threadIdx.x;
+                const uint32_t slot = base + (uint32_t)(k * 32);
                 double inc = w[k];
                 if (REFRESH || a.dt_changed || (d[k] & kStale)) {
                     if (__double_as_longlong(w[k]) >= 0) inc = __dmul_rn(__dmul_rn(w[k], a.dt), a.cinv);
@@ -360,7 +362,7 @@ __device__ __forceinline__ uint32_t grow_tile(const DomainArgs& a, int L, uint32
         float vel[ITEMS], fill[ITEMS], comp[ITEMS];
 #pragma unroll
         for (int k = 0; k < ITEMS; ++k) {
-            const uint32_t slot = base + (uint32_t)(k * kBlock) + threadIdx.x;
+            const uint32_t slot = base + (uint32_t)(k * 32);
             vel[k] = -1.0f; fill[k] = 0.0f; comp[k] = 0.0f;
             if (d[k] != kInactive) {
                 if (d[k] & kPend) {
@@ -383,7 +385,7 @@ __device__ __forceinline__ uint32_t grow_tile(const DomainArgs& a, int L, uint32
             full[k] = false;
             if (d[k] != kInactive) {
                 ++sv;
-                const uint32_t slot = base + (uint32_t)(k * kBlock) + threadIdx.x;
+                const uint32_t slot = base + (uint32_t)(k * 32);
                 if (d[k] & kStale) fr.dir[slot] = d[k] & kCodeMask;
                 if (vel[k] >= 0.0f) {
                     // Kahan-compensated accumulation of the fill
@@ -402,27 +404,22 @@ __device__ __forceinline__ uint32_t grow_tile(const DomainArgs& a, int L, uint32
 #pragma unroll
     for (int k = 0; k < ITEMS; ++k) {
         const uint32_t fm = __ballot_sync(0xFFFFFFFFu, full[k]);
-        const uint32_t im = __ballot_sync(0xFFFFFFFFu, d[k] == kInactive && base + (uint32_t)(k * kBlock) + threadIdx.x < n);
+        const uint32_t im = __ballot_sync(0xFFFFFFFFu, d[k] == kInactive && base + (uint32_t)(k * 32) < n);
         if (lane == 0) {
-            const uint32_t word = tile * S::kWords + (uint32_t)(k * kWarps + warp);  // slots 32 word .. 32 word + 31
+            const uint32_t word = tile * S::kWords + (uint32_t)(warp * ITEMS + k);  // slots 32 word .. 32 word + 31
             fr.fmask[word] = fm;
             fr.imask[word] = im;
         }
         cf += __popc(fm);
         ci += __popc(im);
     }
-    if (lane == 0) { s_f[warp] = cf; s_i[warp] = ci; }
-    __syncthreads();
-    if (threadIdx.x == 0) {
-        uint32_t tf = 0, ti = 0;
-#pragma unroll
-        for (int w = 0; w < kWarps; ++w) { tf += s_f[w]; ti += s_i[w]; }
-        fr.tcnt[2 * tile] = tf;
-        fr.tcnt[2 * tile + 1] = ti;
-        if (tf) atomicAdd(&fr.scnt[2 * (tile / kSuper)], tf);
-        if (ti) atomicAdd(&fr.scnt[2 * (tile / kSuper) + 1], ti);
+    if (lane == 0) {  // the warp's counts, and its share of the supertile's
+        const uint32_t wt = tile * kWarps + (uint32_t)warp;
+        fr.tcnt[2 * wt] = cf;
+        fr.tcnt[2 * wt + 1] = ci;
+        if (cf) atomicAdd(&fr.scnt[2 * (tile / kSuper)], cf);
+        if (ci) atomicAdd(&fr.scnt[2 * (tile / kSuper) + 1], ci);
     }
-    __syncthreads();
     return sv;
 }
 
@@ -442,7 +439,6 @@ template <bool FP32, int ITEMS, bool ONE>
 __global__ void __launch_bounds__(kBlock, ITEMS >= 16 ? 2 : 4) k_grow_fill(int base, int ndom) {
     using S = GrowShape<ITEMS>;
     __shared__ uint32_t s_pre[kMaxSegs + 1];
-    __shared__ uint32_t s_f[kWarps], s_i[kWarps];
     if (ONE) {
         const DomainArgs& a = c_args[base];
         if (!a.active) return;
@@ -452,9 +448,9 @@ __global__ void __launch_bounds__(kBlock, ITEMS >= 16 ? 2 : 4) k_grow_fill(int b
             const uint32_t ntiles = (n + S::kTile - 1) / S::kTile;
             uint32_t sv = 0;
             if (a.refresh) {
-                for (uint32_t tile = blockIdx.x; tile < ntiles; tile += gridDim.x) sv += grow_tile<FP32, true, ITEMS>(a, L, tile, n, s_f, s_i);
+                for (uint32_t tile = blockIdx.x; tile < ntiles; tile += gridDim.x) sv += grow_tile<FP32, true, ITEMS>(a, L, tile, n);
             } else {
-                for (uint32_t tile = blockIdx.x; tile < ntiles; tile += gridDim.x) sv += grow_tile<FP32, false, ITEMS>(a, L, tile, n, s_f, s_i);
+                for (uint32_t tile = blockIdx.x; tile < ntiles; tile += gridDim.x) sv += grow_tile<FP32, false, ITEMS>(a, L, tile, n);
             }
             flush_sv(a, L, sv);
         }
@@ -477,8 +473,8 @@ __global__ void __launch_bounds__(kBlock, ITEMS >= 16 ? 2 : 4) k_grow_fill(int b
         const int L = s & 1;
         const uint32_t tile = u - s_pre[s];
         const uint32_t n = a.st->next_never[L];
-        if (a.refresh) sv += grow_tile<FP32, true, ITEMS>(a, L, tile, n, s_f, s_i);
-        else sv += grow_tile<FP32, false, ITEMS>(a, L, tile, n, s_f, s_i);
+        if (a.refresh) sv += grow_tile<FP32, true, ITEMS>(a, L, tile, n);
+        else sv += grow_tile<FP32, false, ITEMS>(a, L, tile, n);
     }
     if (cur >= 0) flush_sv(c_args[base + (cur >> 1)], cur & 1, sv);
 }
@@ -503,7 +499,7 @@ __global__ void __launch_bounds__(kBlock) k_grow_lists(int base, int ndom) {
         const DFront& fr = a.f[L];
         const uint32_t tile = u - s_pre[s];
         uint32_t rf, ri;
-        tile_prefix(fr.tcnt, fr.scnt, tile, rf, ri);
+        tile_prefix(fr.tcnt, fr.scnt, tile, rf, ri, kWarps);  // the fill wrote one count pair per warp
         uint32_t fw[WPL], iw[WPL];
 #pragma unroll
         for (int h = 0; h < WPL; ++h) {
