@@ -100,15 +100,21 @@ def reduce_sum(dist, x: float) -> float:
     return float(t.item())
 
 
-def spec_for(n: int, precision: int = 0):
+def spec_for(n: int, precision: int = 0, **kw):
     import score_gb300 as sg
-    return sg.UdsSpec(nx=n, ny=n, nz=n, precision=precision)
+    return sg.UdsSpec(nx=n, ny=n, nz=n, precision=precision, **kw)
 
 
-def read_params(n: int, precision: int = 0):
+def read_params(n: int, precision: int = 0, **kw):
     import score_gb300 as sg
     with tempfile.TemporaryDirectory() as td:
-        return sg.read_uds(spec_for(n, precision).write(Path(td) / "bench.uds"))
+        return sg.read_uds(spec_for(n, precision, **kw).write(Path(td) / "bench.uds"))
+
+
+# config of the recovery workload: rho(t) = rho0 / (1 + k t), k = 0.01 1/s, and Poisson
+# incubation times at 1e3 nuclei/s
+RECOVERY_K = "0.01"
+NUCLEATION_RATE = 1000.0
 
 
 def measured_peak_gbs():
@@ -235,8 +241,13 @@ class PlainWorkload:
         n = args.edge
         f = (n / N_EDGE) ** 3
         self.n, self.ngr, self.nnuc = n, max(1, round(N_GRAINS * f)), max(1, round(N_NUCLEI * f))
-        self.d = sg.generate_domain(n, n, n, self.ngr, self.nnuc, seed=rank)
-        self.p = read_params(n, args.precision)
+        self.recovery = args.workload == "recovery"
+        if self.recovery:
+            self.d = sg.generate_domain(n, n, n, self.ngr, self.nnuc, seed=rank, nucleation_rate=NUCLEATION_RATE)
+            self.p = read_params(n, args.precision, recovery=10, recovery_k=RECOVERY_K)
+        else:
+            self.d = sg.generate_domain(n, n, n, self.ngr, self.nnuc, seed=rank)
+            self.p = read_params(n, args.precision)
         self.sg = sg
         self.gm = sg.GrowthMachine(self.p, device=local)
         self.gm.load_domain(self.d)
@@ -289,6 +300,10 @@ class PlainWorkload:
         return label_error(lab32, lab64, x32[:m], x64[:m], self.d.ndefg)
 
     def config(self):
+        if self.recovery:
+            return {"workload": f"{self.n}^3, {self.ngr} grains, {self.nnuc} nuclei with Poisson incubation times "
+                                f"({NUCLEATION_RATE:g}/s), recovery rho0/(1+{RECOVERY_K} t), until X>0.99",
+                    "cells": self.n ** 3, "grains": self.ngr, "nuclei": self.nnuc, "l2": "inputs larger than L2"}
         return {"workload": WORKLOAD if self.n == N_EDGE else f"{self.n}^3 at the 512^3 workload's densities",
                 "cells": self.n ** 3, "grains": self.ngr, "nuclei": self.nnuc,
                 "l2": "inputs larger than L2 (grid alone 512 MiB)" if self.n >= 320 else "grid smaller than L2"}
@@ -412,8 +427,9 @@ def main():
     ap.add_argument("--steps", type=int, default=5)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
-    ap.add_argument("--workload", default="plain", choices=["plain", "batch"],
-                    help="plain: one 512^3 domain (headline); batch: ensemble of uneven domains")
+    ap.add_argument("--workload", default="plain", choices=["plain", "batch", "recovery"],
+                    help="plain: one 512^3 domain (headline); batch: ensemble of uneven domains; "
+                         "recovery: 512^3 with hyperbolic recovery and Poisson nucleation")
     ap.add_argument("--edge", type=int, default=N_EDGE)
     ap.add_argument("--domains", type=int, default=64, help="batch workload: number of domains")
     ap.add_argument("--precision", type=int, default=0, help="0 FP64 (bit-exact), 1 FP32+Kahan")
