@@ -115,6 +115,12 @@ def read_params(n: int, precision: int = 0, **kw):
 # incubation times at 1e3 nuclei/s
 RECOVERY_K = "0.01"
 NUCLEATION_RATE = 1000.0
+# config of the pancake workload: 1024^3, 8,000 grains flattened 1:4:8, orientations around
+# 3 texture components with 10 degree scatter, rho 1e14 / 5e15 (50/50), 200,000 nuclei
+# preferentially on grain boundaries
+PANCAKE = dict(edge=1024, grains=8000, nuclei=200000,
+               gen=dict(aspect=(1.0, 4.0, 8.0), ori_mode=1, ncomp=3, scatter_deg=10.0, rho_mode=1, rho_lo=1e14,
+                        rho_hi=5e15, site_mode=1, gb_fraction=0.8))
 
 
 def measured_peak_gbs():
@@ -242,7 +248,13 @@ class PlainWorkload:
         f = (n / N_EDGE) ** 3
         self.n, self.ngr, self.nnuc = n, max(1, round(N_GRAINS * f)), max(1, round(N_NUCLEI * f))
         self.recovery = args.workload == "recovery"
-        if self.recovery:
+        self.pancake = args.workload == "pancake"
+        if self.pancake:
+            n = PANCAKE["edge"]
+            self.n, self.ngr, self.nnuc = n, PANCAKE["grains"], PANCAKE["nuclei"]
+            self.d = sg.generate_domain(n, n, n, self.ngr, self.nnuc, seed=rank, **PANCAKE["gen"])
+            self.p = read_params(n, args.precision)
+        elif self.recovery:
             self.d = sg.generate_domain(n, n, n, self.ngr, self.nnuc, seed=rank, nucleation_rate=NUCLEATION_RATE)
             self.p = read_params(n, args.precision, recovery=10, recovery_k=RECOVERY_K)
         else:
@@ -300,6 +312,10 @@ class PlainWorkload:
         return label_error(lab32, lab64, x32[:m], x64[:m], self.d.ndefg)
 
     def config(self):
+        if self.pancake:
+            return {"workload": f"{self.n}^3 pancake grains 1:4:8, {self.ngr} grains, 3 texture components 10 deg scatter, "
+                                f"rho 1e14/5e15, {self.nnuc} grain-boundary nuclei, until X>0.99",
+                    "cells": self.n ** 3, "grains": self.ngr, "nuclei": self.nnuc, "l2": "inputs larger than L2"}
         if self.recovery:
             return {"workload": f"{self.n}^3, {self.ngr} grains, {self.nnuc} nuclei with Poisson incubation times "
                                 f"({NUCLEATION_RATE:g}/s), recovery rho0/(1+{RECOVERY_K} t), until X>0.99",
@@ -427,9 +443,9 @@ def main():
     ap.add_argument("--steps", type=int, default=5)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
-    ap.add_argument("--workload", default="plain", choices=["plain", "batch", "recovery"],
+    ap.add_argument("--workload", default="plain", choices=["plain", "batch", "recovery", "pancake"],
                     help="plain: one 512^3 domain (headline); batch: ensemble of uneven domains; "
-                         "recovery: 512^3 with hyperbolic recovery and Poisson nucleation")
+                         "recovery: 512^3 with hyperbolic recovery and Poisson nucleation; pancake: 1024^3 rolled structure")
     ap.add_argument("--edge", type=int, default=N_EDGE)
     ap.add_argument("--domains", type=int, default=64, help="batch workload: number of domains")
     ap.add_argument("--precision", type=int, default=0, help="0 FP64 (bit-exact), 1 FP32+Kahan")
