@@ -190,7 +190,11 @@ int  score_grain_counts(score_ctx* ctx, uint32_t* rxg_counts, uint32_t* defg_cou
  * launches, the algorithmic bytes those launches moved, and run_ms = event time
  * from the start of the restart/reset to the end of the last score_run_until */
 typedef struct score_timing {
-    double total_ms, grow_ms, claim_ms, commit_ms, host_ms;
+    double total_ms;        /* device time of the step kernels */
+    double grow_ms;         /* the fill update (k_grow_fill) */
+    double claim_ms;        /* FullRX / recycle lists and the infection attempts (k_grow_lists) */
+    double commit_ms;       /* resolve, commit (new cells, weights) and step end */
+    double host_ms;         /* host wall time inside the step calls, the wait included */
     uint64_t grow_launches;
     double grow_bytes;      /* algorithmic bytes of all grow launches */
     double step_bytes;      /* algorithmic bytes of all kernels */

@@ -13,11 +13,11 @@
 // reference skips it (calcGrowthStepInside, SCORE_Kernel.cpp:4046-4130).
 //
 // Every ordered compaction (FullRX list, recycle list, slot ranks of new cells) is a
-// count pass, a one-block scan of the per-tile counts, and a write pass: no block
+// count pass that also adds its counts into supertile sums, and a write pass that
+// takes each tile's exclusive prefix from the supertile and tile counts: no block
 // ever waits on another one.
 //   k_grow_fill   per list: fill update of every ACTIVE slot in [0, next_never);
-//                 1-bit masks of full and INACTIVE slots, per-tile counts; Sv count.
-//   k_scan_tiles  exclusive scan of the tile counts; list lengths into DevState.
+//                 1-bit masks of full and INACTIVE slots, per-warp counts; Sv count.
 //   k_grow_lists  FullRX list and capped recycle list, in slot order.
 //   k_claim   one thread per full cell: the 26 infection attempts in the reference's
 //             order; a still-deformed target gets atomicMin(claim, attempt ordinal),
