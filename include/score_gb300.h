@@ -191,8 +191,8 @@ int  score_grain_counts(score_ctx* ctx, uint32_t* rxg_counts, uint32_t* defg_cou
  * from the start of the restart/reset to the end of the last score_run_until */
 typedef struct score_timing {
     double total_ms;        /* device time of the step kernels */
-    double grow_ms;         /* the fill update (k_grow_fill) */
-    double claim_ms;        /* FullRX / recycle lists and the infection attempts (k_grow_lists) */
+    double grow_ms;         /* the fill update and the FullRX / recycle lists (k_grow_fill, k_grow_lists) */
+    double claim_ms;        /* the infection attempts (k_claim) */
     double commit_ms;       /* resolve, commit (new cells, weights) and step end */
     double host_ms;         /* host wall time inside the step calls, the wait included */
     uint64_t grow_launches;
