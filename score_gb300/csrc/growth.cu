@@ -53,10 +53,6 @@ __global__ void k_gather_u32(const uint32_t* src, const uint32_t* idx, uint32_t 
     for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) out[i] = src[idx[i]];
 }
 
-__global__ void k_zero_u64(unsigned long long* p, size_t n) {
-    for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x) p[i] = 0ull;
-}
-
 struct NucRec { uint32_t list, slot, site, rxg, defg, pad; double P; };
 
 // nucleus: fill 1.0 (ALMOST_FULLY_INFECTED), infector 26 (f_geo 1.0)
@@ -285,16 +281,6 @@ void score_ctx::release_domain() {
     loaded = false;
 }
 
-void score_ctx::release_stream() {
-    if (device >= 0) cudaSetDevice(device);
-    if (h_state) cudaFreeHost(h_state);
-    h_state = nullptr;
-    if (h_box) cudaFreeHost(h_box);
-    h_box = nullptr; d_box = nullptr;
-    if (own_eng) delete eng;
-    eng = nullptr;
-    stream = nullptr;  // owned by the engine
-}
 
 // ------------------------------------------------------------------ step engine
 // Launches one growth step of every running domain of a set (one domain, or a batch of
@@ -484,6 +470,19 @@ struct Engine {
     void mark_run_start() { cudaEventRecord(ev[5], stream); }
     int mark_run_end();
 };
+
+// (after Engine is complete: deleting it runs its destructor, which returns its
+// argument slots, stream, events and pinned buffers)
+void score_ctx::release_stream() {
+    if (device >= 0) cudaSetDevice(device);
+    if (h_state) cudaFreeHost(h_state);
+    h_state = nullptr;
+    if (h_box) cudaFreeHost(h_box);
+    h_box = nullptr; d_box = nullptr;
+    if (own_eng) delete eng;
+    eng = nullptr;
+    stream = nullptr;  // owned by the engine
+}
 
 // ------------------------------------------------------------------ helpers
 namespace {
