@@ -409,17 +409,12 @@ struct Engine {
     uint64_t launches = 0;
     std::string err;
     std::unique_ptr<WorkerPool> pool;  // batches of several domains
-    // the host's weights for all domains' requests, copied to the device in one piece
+    // the host's weights for all domains' requests, in pinned device-mapped memory: the
+    // few cells that wait for them read them directly (no copy before the step)
     unsigned long long* h_ans_i = nullptr; double* h_ans_v = nullptr;
     unsigned long long* d_ans_i = nullptr; double* d_ans_v = nullptr;
     size_t ans_cap = 0, ans_total = 0;
     int stage_answers();
-    cudaError_t upload_answers() {
-        if (!ans_total) return cudaSuccess;
-        cudaError_t e = cudaMemcpyAsync(d_ans_i, h_ans_i, ans_total * 8, cudaMemcpyHostToDevice, stream);
-        if (e == cudaSuccess) e = cudaMemcpyAsync(d_ans_v, h_ans_v, ans_total * 8, cudaMemcpyHostToDevice, stream);
-        return e;
-    }
 
     ~Engine() { release(); }
     int init(int dev, int ndom) {
@@ -447,8 +442,6 @@ struct Engine {
         drop_graph();
         if (h_ans_i) cudaFreeHost(h_ans_i);
         if (h_ans_v) cudaFreeHost(h_ans_v);
-        if (d_ans_i) cudaFree(d_ans_i);
-        if (d_ans_v) cudaFree(d_ans_v);
         h_ans_i = nullptr; h_ans_v = nullptr; d_ans_i = nullptr; d_ans_v = nullptr;
         ans_cap = ans_total = 0;
         if (h_args) cudaFreeHost(h_args);
@@ -927,8 +920,7 @@ void Engine::launch_sequence(int n) {
 
 // the argument copy and the kernels of one step, as a graph replay or direct launches
 cudaError_t Engine::enqueue_step(int n) {
-    cudaError_t e = upload_answers();
-    if (e == cudaSuccess) e = cudaMemcpyAsync(d_args, h_args, (size_t)n * sizeof(DomainArgs), cudaMemcpyHostToDevice, stream);
+    cudaError_t e = cudaMemcpyAsync(d_args, h_args, (size_t)n * sizeof(DomainArgs), cudaMemcpyHostToDevice, stream);
     if (e != cudaSuccess) return e;
     if (!use_graph) {
         launch_sequence(n);
@@ -953,9 +945,8 @@ cudaError_t Engine::enqueue_step(int n) {
     return cudaGraphLaunch(gexec, stream);
 }
 
-// Pack every domain's answered weights into the pinned staging buffer and point the
-// domains' argument blocks at their part of the device copy (made by upload_answers
-// before the next step's kernels).
+// Pack every domain's answered weights into the pinned, device-mapped staging buffer
+// and point the domains' argument blocks at their part of it.
 int Engine::stage_answers() {
     size_t total = 0;
     for (score_ctx* c : dom) total += c->ans_idx.size();
@@ -965,14 +956,12 @@ int Engine::stage_answers() {
         const size_t cap = std::max<size_t>(total, 2 * ans_cap);
         if (h_ans_i) cudaFreeHost(h_ans_i);
         if (h_ans_v) cudaFreeHost(h_ans_v);
-        if (d_ans_i) cudaFree(d_ans_i);
-        if (d_ans_v) cudaFree(d_ans_v);
         h_ans_i = nullptr; h_ans_v = nullptr; d_ans_i = nullptr; d_ans_v = nullptr;
         ans_cap = 0;
-        cudaError_t e = cudaMallocHost((void**)&h_ans_i, cap * 8);
-        if (e == cudaSuccess) e = cudaMallocHost((void**)&h_ans_v, cap * 8);
-        if (e == cudaSuccess) e = cudaMalloc((void**)&d_ans_i, cap * 8);
-        if (e == cudaSuccess) e = cudaMalloc((void**)&d_ans_v, cap * 8);
+        cudaError_t e = cudaHostAlloc((void**)&h_ans_i, cap * 8, cudaHostAllocMapped);
+        if (e == cudaSuccess) e = cudaHostAlloc((void**)&h_ans_v, cap * 8, cudaHostAllocMapped);
+        if (e == cudaSuccess) e = cudaHostGetDevicePointer((void**)&d_ans_i, h_ans_i, 0);
+        if (e == cudaSuccess) e = cudaHostGetDevicePointer((void**)&d_ans_v, h_ans_v, 0);
         if (e != cudaSuccess) return fail(SCORE_ERR_NOMEM, "weight staging buffers");
         ans_cap = cap;
     }
