@@ -396,6 +396,8 @@ struct Engine {
     int base = -1, nslots = 0;         // this engine's slots of c_args
     DomainArgs* d_args = nullptr;      // device address of c_args[base]
     DomainArgs* h_args = nullptr;      // pinned staging of the argument blocks
+    std::vector<DomainArgs> h_args_dev;  // what the device's slots hold
+    bool args_dirty = true;
     TuneCfg cfg;
     bool use_graph = true;
     bool capturing = false;
@@ -430,6 +432,8 @@ struct Engine {
         if (e == cudaSuccess) e = cudaGetSymbolAddress(&sym, c_args);
         if (e == cudaSuccess) d_args = (DomainArgs*)sym + base;
         if (e == cudaSuccess) e = cudaMallocHost((void**)&h_args, (size_t)ndom * sizeof(DomainArgs));
+        h_args_dev.assign((size_t)ndom, DomainArgs{});
+        args_dirty = true;
         return e == cudaSuccess ? SCORE_OK : SCORE_ERR_CUDA;
     }
     void drop_graph() {
@@ -700,7 +704,6 @@ int reset_state(score_ctx* c) {
     for (int L = 0; L < 2 && e == cudaSuccess; ++L) e = cudaMemsetAsync(a.f[L].scnt, 0, c->scnt_words[L] * 4, st);
     if (e == cudaSuccess) e = cudaMemsetAsync(a.csct, 0, c->csct_words * 4, st);
     if (e != cudaSuccess) return c->cuda_fail(e, "reset domain");
-    a.n_ans = 0;
     c->ans_idx.clear();
     c->ans_val.clear();
     memset(&c->h_box->snap, 0, sizeof(DevState));
@@ -778,7 +781,6 @@ int post_step(score_ctx* c, uint32_t newnuc, score_step_stats* out) {
     // mobility weights requested this step: computed on the host (FP64, libm)
     double pmax_new = 0.0;
     if (hs.pmax_bits) memcpy(&pmax_new, &hs.pmax_bits, 8);
-    a.n_ans = 0;
     c->ans_idx.clear();
     c->ans_val.clear();
     uint32_t nreq = 0;  // distinct weights requested (void race slots excluded)
@@ -801,7 +803,6 @@ int post_step(score_ctx* c, uint32_t newnuc, score_step_stats* out) {
         // staged by the engine into one host-to-device copy before the next step
         c->ans_idx.swap(idx);
         c->ans_val.swap(val);
-        a.n_ans = hs.nmiss;
     }
     // deformed grains that ran out of cells this step (synchronize_mydefpool_counts)
     if (hs.ndepleted > 0) {
@@ -920,7 +921,13 @@ void Engine::launch_sequence(int n) {
 
 // the argument copy and the kernels of one step, as a graph replay or direct launches
 cudaError_t Engine::enqueue_step(int n) {
-    cudaError_t e = cudaMemcpyAsync(d_args, h_args, (size_t)n * sizeof(DomainArgs), cudaMemcpyHostToDevice, stream);
+    // the argument blocks only change when dt, the physics or a domain's state changes
+    cudaError_t e = cudaSuccess;
+    if (args_dirty || memcmp(h_args, h_args_dev.data(), (size_t)n * sizeof(DomainArgs)) != 0) {
+        e = cudaMemcpyAsync(d_args, h_args, (size_t)n * sizeof(DomainArgs), cudaMemcpyHostToDevice, stream);
+        memcpy(h_args_dev.data(), h_args, (size_t)n * sizeof(DomainArgs));
+        args_dirty = false;
+    }
     if (e != cudaSuccess) return e;
     if (!use_graph) {
         launch_sequence(n);

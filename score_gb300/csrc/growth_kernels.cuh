@@ -106,8 +106,8 @@ struct DomainArgs {
     int32_t dt_changed;         // dt differs from the dt the cached increments were made with
     int32_t refresh;            // recompute every vel this step (T, rho or the drag changed)
     int32_t active;             // the domain steps in this launch
-    uint32_t n_ans;             // weights the host computed for the last step's requests (miss slot order)
-    const unsigned long long* ans_idx;  // their table indices (device copy; kMissVoid = none)
+    const unsigned long long* ans_idx;  // weights the host computed for the last step's requests, in miss-slot
+                                        // order: table indices (kMissVoid = none), device view of pinned memory
     const double* ans_val;
     HostBox* box;               // device view of the domain's mailbox
     double mLAGB, mHAGB, mGS, mRH, dt, cinv;
