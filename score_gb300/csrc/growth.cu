@@ -61,7 +61,9 @@ __global__ void k_place_nuclei(DomainArgs a, const NucRec* rec, uint32_t n) {
     for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
         const NucRec r = rec[i];
         const DFront& f = a.f[r.list];
-        const double v = velocity_factor(a, r.P, r.defg, 26);
+        const double mo = mobility(a, r.P);
+        const double v = velocity_from_mobility(a, mo, r.defg, 26);
+        f.mob[r.slot] = mo;
         if (!FP32) { ((double*)f.fill)[r.slot] = 1.0; ((double*)f.vel)[r.slot] = v; }
         else { ((float*)f.fill)[r.slot] = 1.0f; f.comp[r.slot] = 0.0f; ((float*)f.vel)[r.slot] = (float)v; }
         f.dir[r.slot] = 26 | kStale;
@@ -153,10 +155,12 @@ __global__ void __launch_bounds__(kBlock) k_defrag_compact(DomainArgs a, int L, 
                 ((double*)scratch.fill)[r] = ((const double*)fr.fill)[s];
                 ((double*)scratch.vel)[r] = ((const double*)fr.vel)[s];
                 scratch.inc[r] = fr.inc[s];
+                scratch.mob[r] = fr.mob[s];
             } else {
                 ((float*)scratch.fill)[r] = ((const float*)fr.fill)[s];
                 scratch.comp[r] = fr.comp[s];
                 ((float*)scratch.vel)[r] = ((const float*)fr.vel)[s];
+                scratch.mob[r] = fr.mob[s];
             }
             scratch.defg[r] = fr.defg[s]; scratch.rxg[r] = fr.rxg[s]; scratch.xyz[r] = fr.xyz[s]; scratch.dir[r] = fr.dir[s];
         }
@@ -198,7 +202,8 @@ struct score_ctx {
     uint32_t nx = 0, ny = 0, nz = 0;
     uint64_t N = 0;
     uint32_t ndefg = 0, nrxg = 0;
-    bool loaded = false, fp32 = false, failed = false, refresh = false;
+    bool loaded = false, fp32 = false, failed = false;
+    int refresh = 0;                   // next step: 1 full refresh from P, 2 from cached mobilities
     std::vector<double> defg_q, rxg_q, rho0, rho, tincub;
     std::vector<uint32_t> site;
     std::vector<uint8_t> placed;
@@ -220,6 +225,7 @@ struct score_ctx {
     HostBox* h_box = nullptr;          // pinned, device-mapped step mailbox
     HostBox* d_box = nullptr;          // its device address
     double* d_pforce = nullptr;
+    double* h_pforce = nullptr;            // pinned staging of the driving forces
     uint32_t* d_grid_init = nullptr;       // the loaded deformed grid (restart source)
     double* d_rxq = nullptr;               // orientation quaternions on the device
     double* d_dfq = nullptr;
@@ -265,7 +271,7 @@ struct score_ctx {
 
 void score_ctx::release_domain() {
     if (device >= 0) cudaSetDevice(device);
-    void* ptrs[] = {a.f[0].inc, a.f[1].inc, scratch.inc, a.f[0].fill, a.f[0].comp, a.f[0].vel, a.f[0].defg, a.f[0].rxg, a.f[0].xyz, a.f[0].dir, a.f[0].full, a.f[0].recyc,
+    void* ptrs[] = {a.f[0].inc, a.f[1].inc, scratch.inc, a.f[0].mob, a.f[1].mob, scratch.mob, a.f[0].fill, a.f[0].comp, a.f[0].vel, a.f[0].defg, a.f[0].rxg, a.f[0].xyz, a.f[0].dir, a.f[0].full, a.f[0].recyc,
                     a.f[1].fill, a.f[1].comp, a.f[1].vel, a.f[1].defg, a.f[1].rxg, a.f[1].xyz, a.f[1].dir, a.f[1].full, a.f[1].recyc,
                     a.grid, a.claim, a.amask, a.ptab, a.defg_cnt, a.rxg_cnt, a.depleted, a.miss, a.tobm, a.ctcnt,
                     a.f[0].fmask, a.f[0].imask, a.f[0].tcnt, a.f[1].fmask, a.f[1].imask, a.f[1].tcnt,
@@ -273,6 +279,8 @@ void score_ctx::release_domain() {
                     d_state, d_pforce, d_u32tmp, d_stage, d_grid_init, d_defg_cnt_init, d_rxq, d_dfq,
                     scratch.fill, scratch.comp, scratch.vel, scratch.defg, scratch.rxg, scratch.xyz, scratch.dir};
     for (void* p : ptrs) if (p) cudaFree(p);
+    if (h_pforce) cudaFreeHost(h_pforce);
+    h_pforce = nullptr;
     a = DomainArgs{};
     scratch = DFront{};
     d_state = nullptr; d_pforce = nullptr; d_u32tmp = nullptr; d_stage = nullptr;
@@ -498,12 +506,14 @@ int upload_physics(score_ctx* c) {
     std::vector<double> pf(c->ndefg);
     for (uint32_t g = 0; g < c->ndefg; ++g) pf[g] = c->ph.driving_force(c->rho[g]);
     if (pf == c->pforce_host && mob_same) return SCORE_OK;
-    c->refresh = true;
+    c->refresh = (c->refresh == 1 || !mob_same) ? 1 : 2;  // new mobilities need P again
     memcpy(c->mob_host, mob, sizeof mob);
     if (pf == c->pforce_host) return SCORE_OK;
     c->pforce_host = pf;
-    cudaError_t e = cudaMemcpyAsync(c->d_pforce, c->pforce_host.data(), pf.size() * 8, cudaMemcpyHostToDevice, c->stream);
-    if (e == cudaSuccess) e = cudaStreamSynchronize(c->stream);
+    // pinned staging, stream-ordered before the next step's kernels; it is rewritten only
+    // after a later step's synchronisation
+    memcpy(c->h_pforce, pf.data(), pf.size() * 8);
+    const cudaError_t e = cudaMemcpyAsync(c->d_pforce, c->h_pforce, pf.size() * 8, cudaMemcpyHostToDevice, c->stream);
     if (e != cudaSuccess) return c->cuda_fail(e, "upload driving force");
     return SCORE_OK;
 }
@@ -626,7 +636,7 @@ int defragment(score_ctx* c, int L) {
     if (n == 0) return SCORE_OK;
     DFront& fr = c->a.f[L];
     if (c->scratch_cap < n) {
-        void* ptrs[] = {c->scratch.inc, c->scratch.fill, c->scratch.comp, c->scratch.vel, c->scratch.defg, c->scratch.rxg, c->scratch.xyz, c->scratch.dir};
+        void* ptrs[] = {c->scratch.inc, c->scratch.mob, c->scratch.fill, c->scratch.comp, c->scratch.vel, c->scratch.defg, c->scratch.rxg, c->scratch.xyz, c->scratch.dir};
         for (void* p : ptrs) if (p) cudaFree(p);
         c->scratch = DFront{};
         const size_t fb = c->fp32 ? 4 : 8;
@@ -634,6 +644,7 @@ int defragment(score_ctx* c, int L) {
         if (e == cudaSuccess && c->fp32) e = cudaMalloc((void**)&c->scratch.comp, (size_t)n * 4);
         if (e == cudaSuccess) e = cudaMalloc(&c->scratch.vel, (size_t)n * fb);
         if (e == cudaSuccess && !c->fp32) e = dalloc(&c->scratch.inc, n);
+        if (e == cudaSuccess) e = dalloc(&c->scratch.mob, n);
         if (e == cudaSuccess) e = dalloc(&c->scratch.defg, n);
         if (e == cudaSuccess) e = dalloc(&c->scratch.rxg, n);
         if (e == cudaSuccess) e = dalloc(&c->scratch.xyz, n);
@@ -672,6 +683,7 @@ int defragment(score_ctx* c, int L) {
         if (e == cudaSuccess && c->fp32) e = cudaMemcpyAsync(fr.comp, c->scratch.comp, (size_t)active * 4, cudaMemcpyDeviceToDevice, c->stream);
         if (e == cudaSuccess) e = cudaMemcpyAsync(fr.vel, c->scratch.vel, (size_t)active * fb, cudaMemcpyDeviceToDevice, c->stream);
         if (e == cudaSuccess && !c->fp32) e = cudaMemcpyAsync(fr.inc, c->scratch.inc, (size_t)active * 8, cudaMemcpyDeviceToDevice, c->stream);
+        if (e == cudaSuccess) e = cudaMemcpyAsync(fr.mob, c->scratch.mob, (size_t)active * 8, cudaMemcpyDeviceToDevice, c->stream);
         if (e == cudaSuccess) e = cudaMemcpyAsync(fr.defg, c->scratch.defg, (size_t)active * 4, cudaMemcpyDeviceToDevice, c->stream);
         if (e == cudaSuccess) e = cudaMemcpyAsync(fr.rxg, c->scratch.rxg, (size_t)active * 4, cudaMemcpyDeviceToDevice, c->stream);
         if (e == cudaSuccess) e = cudaMemcpyAsync(fr.xyz, c->scratch.xyz, (size_t)active * 4, cudaMemcpyDeviceToDevice, c->stream);
@@ -726,7 +738,7 @@ int reset_state(score_ctx* c) {
     memset(c->mob_host, 0, sizeof c->mob_host);
     int s = upload_physics(c);
     if (s != SCORE_OK) return s;
-    c->refresh = false;  // the front is empty; new cells get their factors when they are created
+    c->refresh = 0;  // the front is empty; new cells get their factors when they are created
     c->dt_cached = -1.0;
     c->Xcells = 0.0; c->step = 0; c->defrag_cnt = 0; c->n_nuclei = 0;
     c->next_never[0] = c->next_never[1] = 0;
@@ -760,10 +772,10 @@ int pre_step(score_ctx* c, uint32_t* newnuc) {
     set_step_args(c);
     DomainArgs& a = c->a;
     a.dt_changed = (ph.dt != c->dt_cached) ? 1 : 0;
-    a.refresh = c->refresh ? 1 : 0;
+    a.refresh = c->refresh;
     a.active = 1;
     c->dt_cached = ph.dt;
-    c->refresh = false;
+    c->refresh = 0;
     return SCORE_OK;
 }
 
@@ -829,8 +841,9 @@ int post_step(score_ctx* c, uint32_t newnuc, score_step_stats* out) {
     c->Xcells = c->Xcells + (double)nfull;
     const double X = (c->Xcells / (double)c->N);
     if (c->rhomax_version != c->rho_version) {  // rho max only moves when rho or the grain set changes
-        if (c->rho_version == 0) {
-            // rho is still rho0: the first grain in descending-rho0 order that has cells
+        if (c->rho_version == 0 || c->prm.recovery_model == SCORE_RECOVERY_HYPERBOLIC) {
+            // rho is rho0, or rho0 / (1 + k t) (same order): the first grain in descending-rho0
+            // order that has cells
             while (c->rho_cursor < c->rho_order.size() && c->defg_cnt_host[c->rho_order[c->rho_cursor]] == 0) ++c->rho_cursor;
             const double best = c->rho_cursor < c->rho_order.size() ? c->rho[c->rho_order[c->rho_cursor]] : -1.0;
             ph.rhomax = (best >= kRhomaxWellAnnealed) ? best : kRhomaxWellAnnealed;
@@ -1337,6 +1350,7 @@ int score_load_domain(score_ctx* c, const uint32_t* grid, const double* defg_qua
             if (e == cudaSuccess && c->fp32) e = cudaMalloc((void**)&f.comp, (size_t)caps[L] * 4);
             if (e == cudaSuccess) e = cudaMalloc(&f.vel, (size_t)caps[L] * fb);
             if (e == cudaSuccess && !c->fp32) e = dalloc(&f.inc, caps[L]);
+            if (e == cudaSuccess) e = dalloc(&f.mob, caps[L]);
             if (e == cudaSuccess) e = dalloc(&f.defg, caps[L]);
             if (e == cudaSuccess) e = dalloc(&f.rxg, caps[L]);
             if (e == cudaSuccess) e = dalloc(&f.xyz, caps[L]);
@@ -1369,6 +1383,7 @@ int score_load_domain(score_ctx* c, const uint32_t* grid, const double* defg_qua
         if (e == cudaSuccess) e = dalloc(&a.miss, a.misscap);
         if (e == cudaSuccess) e = dalloc(&c->d_state, 1);
         if (e == cudaSuccess) e = dalloc(&c->d_pforce, ndefg);
+        if (e == cudaSuccess) e = cudaMallocHost((void**)&c->h_pforce, std::max<size_t>(ndefg, 1) * 8);
         if (e == cudaSuccess) e = dalloc(&c->d_u32tmp, 64);
         if (e == cudaSuccess) e = dalloc(&c->d_rxq, 4 * (size_t)nrxg);
         if (e == cudaSuccess) e = dalloc(&c->d_dfq, 4 * (size_t)ndefg);

@@ -45,6 +45,7 @@ struct DFront {
     float* comp;         // Kahan compensation (FP32 only)
     void* vel;           // double (FP64) or float (FP32): (m p) f_geo, or -1 = no driving force
     double* inc;         // FP64 only: cached (vel dt) / cellsize for the current dt
+    double* mob;         // cached mobility m(P) of the cell's boundary (a refresh when only p changed)
     uint32_t* defg;
     uint32_t* rxg;
     uint32_t* xyz;       // linear cell index x + y nx + z nx ny
@@ -104,7 +105,8 @@ struct DomainArgs {
     uint32_t border_ref_cap;
     int32_t border_policy, boundary, mobility_model;
     int32_t dt_changed;         // dt differs from the dt the cached increments were made with
-    int32_t refresh;            // recompute every vel this step (T, rho or the drag changed)
+    int32_t refresh;            // recompute every vel this step: 1 from P (mobilities changed), 2 from the
+                                // cached mobility (only the driving force changed), 0 no
     int32_t active;             // the domain steps in this launch
     const unsigned long long* ans_idx;  // weights the host computed for the last step's requests, in miss-slot
                                         // order: table indices (kMissVoid = none), device view of pinned memory
@@ -162,10 +164,13 @@ __device__ __forceinline__ double mobility(const DomainArgs& a, double P) {
     return __dadd_rn(__dmul_rn(P, a.mGS), __dmul_rn(__dsub_rn(1.0, P), a.mHAGB));
 }
 // velocity factor (m p) f_geo, or -1 when the driving force is not above 5e-16
-__device__ __forceinline__ double velocity_factor(const DomainArgs& a, double P, uint32_t defg, int code) {
+__device__ __forceinline__ double velocity_from_mobility(const DomainArgs& a, double m, uint32_t defg, int code) {
     const double p = a.pforce[defg];
     if (!(p > 5.0e-16)) return -1.0;
-    return __dmul_rn(__dmul_rn(mobility(a, P), p), c_sf[code]);
+    return __dmul_rn(__dmul_rn(m, p), c_sf[code]);
+}
+__device__ __forceinline__ double velocity_factor(const DomainArgs& a, double P, uint32_t defg, int code) {
+    return velocity_from_mobility(a, mobility(a, P), defg, code);
 }
 
 // warp-0 exclusive scan of 2x64 block-local counters laid out [item][warp]; totals in every lane
@@ -288,8 +293,9 @@ __device__ __forceinline__ void tile_prefix(const uint32_t* cnt, const uint32_t*
 //   k_grow_lists  one warp per tile: the tile's exclusive prefix from the supertile
 //                 and tile counts, then the FullRX list and the capped recycle list in
 //                 slot order; the warp of a list's last tile stores the list totals.
-// REFRESH: recompute vel of every active slot from the P table and the current
-// physics (after T, rho or the drag changed) before growing it.
+// REFRESH 1: recompute vel of every active slot from the P table and the current
+// physics (after T changed the mobilities); REFRESH 2: from the cell's cached mobility
+// (only rho or the drag changed the driving force), no table gather.
 // A cell created last step whose weight the host computed: P = answer `tag`; the table
 // entry (tagged until now) gets the value for later lookups.
 __device__ __forceinline__ double answered_velocity(const DomainArgs& a, const DFront& fr, uint32_t slot, uint8_t dir,
@@ -297,11 +303,13 @@ __device__ __forceinline__ double answered_velocity(const DomainArgs& a, const D
     const uint32_t m = (uint32_t)tag;
     const double P = a.ans_val[m];
     a.ptab[a.ans_idx[m]] = (unsigned long long)__double_as_longlong(P);
-    return velocity_factor(a, P, fr.defg[slot], dir & kCodeMask);
+    const double mo = mobility(a, P);
+    fr.mob[slot] = mo;
+    return velocity_from_mobility(a, mo, fr.defg[slot], dir & kCodeMask);
 }
 
 // returns the thread's ACTIVE slots (the Sv share)
-template <bool FP32, bool REFRESH, int ITEMS>
+template <bool FP32, int REFRESH, int ITEMS>
 __device__ __forceinline__ uint32_t grow_tile(const DomainArgs& a, int L, uint32_t tile, uint32_t n) {
     using S = GrowShape<ITEMS>;
     const DFront& fr = a.f[L];
@@ -326,10 +334,15 @@ __device__ __forceinline__ uint32_t grow_tile(const DomainArgs& a, int L, uint32
                 if (d[k] & kPend) {
                     w[k] = answered_velocity(a, fr, slot, d[k], ((const unsigned long long*)fr.vel)[slot]);
                     ((double*)fr.vel)[slot] = w[k];
-                } else if (REFRESH) {
+                } else if (REFRESH == 1) {
                     const uint32_t g = fr.defg[slot];
                     const double P = __longlong_as_double((long long)a.ptab[(unsigned long long)fr.rxg[slot] * a.ndefg + g]);
-                    w[k] = velocity_factor(a, P, g, d[k] & kCodeMask);
+                    const double mo = mobility(a, P);
+                    fr.mob[slot] = mo;
+                    w[k] = velocity_from_mobility(a, mo, g, d[k] & kCodeMask);
+                    ((double*)fr.vel)[slot] = w[k];
+                } else if (REFRESH == 2) {
+                    w[k] = velocity_from_mobility(a, fr.mob[slot], fr.defg[slot], d[k] & kCodeMask);
                     ((double*)fr.vel)[slot] = w[k];
                 } else if (a.dt_changed || (d[k] & kStale)) {
                     w[k] = ((const double*)fr.vel)[slot];
@@ -346,7 +359,7 @@ __device__ __forceinline__ uint32_t grow_tile(const DomainArgs& a, int L, uint32
                 ++sv;
                 const uint32_t slot = base + (uint32_t)(k * 32);
                 double inc = w[k];
-                if (REFRESH || a.dt_changed || (d[k] & kStale)) {
+                if (REFRESH != 0 || a.dt_changed || (d[k] & kStale)) {
                     if (__double_as_longlong(w[k]) >= 0) inc = __dmul_rn(__dmul_rn(w[k], a.dt), a.cinv);
                     fr.inc[slot] = inc;
                     if (d[k] & kStale) fr.dir[slot] = d[k] & kCodeMask;
@@ -368,10 +381,15 @@ __device__ __forceinline__ uint32_t grow_tile(const DomainArgs& a, int L, uint32
                 if (d[k] & kPend) {
                     vel[k] = (float)answered_velocity(a, fr, slot, d[k], ((const uint32_t*)fr.vel)[slot]);
                     ((float*)fr.vel)[slot] = vel[k];
-                } else if (REFRESH) {
+                } else if (REFRESH == 1) {
                     const uint32_t g = fr.defg[slot];
                     const double P = __longlong_as_double((long long)a.ptab[(unsigned long long)fr.rxg[slot] * a.ndefg + g]);
-                    vel[k] = (float)velocity_factor(a, P, g, d[k] & kCodeMask);
+                    const double mo = mobility(a, P);
+                    fr.mob[slot] = mo;
+                    vel[k] = (float)velocity_from_mobility(a, mo, g, d[k] & kCodeMask);
+                    ((float*)fr.vel)[slot] = vel[k];
+                } else if (REFRESH == 2) {
+                    vel[k] = (float)velocity_from_mobility(a, fr.mob[slot], fr.defg[slot], d[k] & kCodeMask);
                     ((float*)fr.vel)[slot] = vel[k];
                 } else {
                     vel[k] = ((const float*)fr.vel)[slot];
@@ -447,10 +465,12 @@ __global__ void __launch_bounds__(kBlock, ITEMS >= 16 ? 2 : 4) k_grow_fill(int b
             const uint32_t n = a.st->next_never[L];
             const uint32_t ntiles = (n + S::kTile - 1) / S::kTile;
             uint32_t sv = 0;
-            if (a.refresh) {
-                for (uint32_t tile = blockIdx.x; tile < ntiles; tile += gridDim.x) sv += grow_tile<FP32, true, ITEMS>(a, L, tile, n);
+            if (a.refresh == 1) {
+                for (uint32_t tile = blockIdx.x; tile < ntiles; tile += gridDim.x) sv += grow_tile<FP32, 1, ITEMS>(a, L, tile, n);
+            } else if (a.refresh == 2) {
+                for (uint32_t tile = blockIdx.x; tile < ntiles; tile += gridDim.x) sv += grow_tile<FP32, 2, ITEMS>(a, L, tile, n);
             } else {
-                for (uint32_t tile = blockIdx.x; tile < ntiles; tile += gridDim.x) sv += grow_tile<FP32, false, ITEMS>(a, L, tile, n);
+                for (uint32_t tile = blockIdx.x; tile < ntiles; tile += gridDim.x) sv += grow_tile<FP32, 0, ITEMS>(a, L, tile, n);
             }
             flush_sv(a, L, sv);
         }
@@ -473,8 +493,9 @@ __global__ void __launch_bounds__(kBlock, ITEMS >= 16 ? 2 : 4) k_grow_fill(int b
         const int L = s & 1;
         const uint32_t tile = u - s_pre[s];
         const uint32_t n = a.st->next_never[L];
-        if (a.refresh) sv += grow_tile<FP32, true, ITEMS>(a, L, tile, n);
-        else sv += grow_tile<FP32, false, ITEMS>(a, L, tile, n);
+        if (a.refresh == 1) sv += grow_tile<FP32, 1, ITEMS>(a, L, tile, n);
+        else if (a.refresh == 2) sv += grow_tile<FP32, 2, ITEMS>(a, L, tile, n);
+        else sv += grow_tile<FP32, 0, ITEMS>(a, L, tile, n);
     }
     if (cur >= 0) flush_sv(c_args[base + (cur >> 1)], cur & 1, sv);
 }
@@ -1000,8 +1021,10 @@ __global__ void __launch_bounds__(kBlock, 3) k_commit(int base, int ndom) {
             double P = 0.0;
             uint32_t tag = 0;
             if (lookup_p(a, rs, gt, P, tag)) {
-                if (!FP32) ((double*)dst.vel)[ns] = velocity_factor(a, P, gt, c_code[d]);
-                else ((float*)dst.vel)[ns] = (float)velocity_factor(a, P, gt, c_code[d]);
+                const double mo = mobility(a, P);
+                dst.mob[ns] = mo;
+                if (!FP32) ((double*)dst.vel)[ns] = velocity_from_mobility(a, mo, gt, c_code[d]);
+                else ((float*)dst.vel)[ns] = (float)velocity_from_mobility(a, mo, gt, c_code[d]);
                 dst.dir[ns] = c_code[d] | kStale;
                 if (P > pmax) pmax = P;
             } else {
