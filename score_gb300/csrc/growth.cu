@@ -476,6 +476,18 @@ struct Engine {
     int mark_run_end();
 };
 
+namespace {
+template <class Body>
+void for_grains(score_ctx* c, Body body) {
+    const size_t n = c->ndefg;
+    Engine& E = *c->eng;
+    if (n < 8192 || E.dom.size() != 1) { body(0, n); return; }
+    if (!E.pool) E.pool.reset(new WorkerPool(std::max(1u, std::min(7u, std::thread::hardware_concurrency() - 1))));
+    constexpr int kChunks = 16;
+    E.pool->run(kChunks, [&](int k) { body(n * (size_t)k / kChunks, n * (size_t)(k + 1) / kChunks); });
+}
+}  // namespace
+
 // (after Engine is complete: deleting it runs its destructor, which returns its
 // argument slots, stream, events and pinned buffers)
 void score_ctx::release_stream() {
@@ -492,6 +504,11 @@ void score_ctx::release_stream() {
 // ------------------------------------------------------------------ helpers
 namespace {
 
+// Per-grain host loop over [0, ndefg): split over the engine's worker threads for a
+// single domain with many grains (a batch already runs its domains in parallel).
+template <class Body>
+void for_grains(score_ctx* c, Body body);
+
 // Driving force per deformed grain, the grow step's p (SCORE_Kernel.cpp:4082).  When it or
 // the mobilities change, the front's velocity factors are recomputed in the next grow.
 int upload_physics(score_ctx* c) {
@@ -504,7 +521,7 @@ int upload_physics(score_ctx* c) {
     memcpy(c->pf_sig, sig, sizeof sig);
     c->pf_rho_version = c->rho_version;
     std::vector<double> pf(c->ndefg);
-    for (uint32_t g = 0; g < c->ndefg; ++g) pf[g] = c->ph.driving_force(c->rho[g]);
+    for_grains(c, [&](size_t lo, size_t hi) { for (size_t g = lo; g < hi; ++g) pf[g] = c->ph.driving_force(c->rho[g]); });
     if (pf == c->pforce_host && mob_same) return SCORE_OK;
     c->refresh = (c->refresh == 1 || !mob_same) ? 1 : 2;  // new mobilities need P again
     memcpy(c->mob_host, mob, sizeof mob);
@@ -859,7 +876,7 @@ int post_step(score_ctx* c, uint32_t newnuc, score_step_stats* out) {
     ph.update_microchemistry();
     ph.update_mobilities();
     if (c->prm.recovery_model != SCORE_RECOVERY_NONE && c->prm.recovery_model != SCORE_RECOVERY_NES_SOLUTEDRAG) {
-        ph.update_substructure(c->rho, c->rho0);
+        for_grains(c, [&](size_t lo, size_t hi) { ph.update_substructure(c->rho.data(), c->rho0.data(), lo, hi); });
         c->rho_version++;
     }
     ph.dt = ph.dt_minimum();

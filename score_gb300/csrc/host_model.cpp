@@ -261,14 +261,18 @@ double Physics::dt_minimum() const {
 // caHdl::update_deformedsubstructure, SCORE_Kernel.cpp:5409-5437 and SCORE_RecoveryModels.cpp:50-126;
 // SCORE_RECOVERY_HYPERBOLIC is rho(t) = rho0 / (1 + k t), which the reference does not have.
 void Physics::update_substructure(std::vector<double>& rho, const std::vector<double>& rho0) const {
+    update_substructure(rho.data(), rho0.data(), 0, rho.size());
+}
+
+// grains [lo, n) of the same update (the per-step scalars are recomputed, identically)
+void Physics::update_substructure(double* rho, const double* rho0, size_t lo, size_t n) const {
     const int m = prm->recovery_model;
-    const size_t n = rho.size();
     if (m == SCORE_RECOVERY_NES_VACCOREDIFF) {
         double B = kPi * prm->NesC3 * prm->NesC5 * prm->VacancyDiffD0 * std::exp(-1.0 * prm->VacancyDiffHact / (kBoltzmann * T));
         B /= prm->NesKappa2;
         double exponent = ((b) * (b)) / (kBoltzmann * T);
         double expterm = std::exp(prm->NesAlpha3 * prm->NesKappa2 * G * b * exponent);
-        for (size_t g = 0; g < n; ++g) {
+        for (size_t g = lo; g < n; ++g) {
             double r_t = 1.0 / std::pow(rho[g], 0.5);
             double Bx = (B / r_t) * expterm;
             double r_tdt = (Bx * dt) + r_t;
@@ -280,12 +284,12 @@ void Physics::update_substructure(std::vector<double>& rho, const std::vector<do
         const double f1 = 0.25, f2 = 0.75, tau2 = 0.3605, tau5 = 5.2824;
         double tm = t / 60.0;
         double factor = f1 * std::pow((1 + (tm / tau2)), -1.0) + f2 * std::pow((1 + (tm / tau5)), -0.5);
-        for (size_t g = 0; g < n; ++g) rho[g] = rho0[g] * ((factor) * (factor));
+        for (size_t g = lo; g < n; ++g) rho[g] = rho0[g] * ((factor) * (factor));
         return;
     }
     if (m == SCORE_RECOVERY_HYPERBOLIC) {
         double f = 1.0 + prm->recovery_k * t;
-        for (size_t g = 0; g < n; ++g) rho[g] = rho0[g] / f;
+        for (size_t g = lo; g < n; ++g) rho[g] = rho0[g] / f;
     }
 }
 
