@@ -22,6 +22,7 @@
 #include <atomic>
 #include <condition_variable>
 #include <functional>
+#include <limits>
 #include <memory>
 #include <mutex>
 #include <string>
@@ -520,17 +521,24 @@ int upload_physics(score_ctx* c) {
         return SCORE_OK;
     memcpy(c->pf_sig, sig, sizeof sig);
     c->pf_rho_version = c->rho_version;
-    std::vector<double> pf(c->ndefg);
-    for_grains(c, [&](size_t lo, size_t hi) { for (size_t g = lo; g < hi; ++g) pf[g] = c->ph.driving_force(c->rho[g]); });
-    if (pf == c->pforce_host && mob_same) return SCORE_OK;
+    // new p per grain, straight into the pinned staging buffer (its last copy to the device
+    // finished before the step that just ended), noting whether any value changed
+    if (c->pforce_host.size() != c->ndefg) c->pforce_host.assign(c->ndefg, std::numeric_limits<double>::quiet_NaN());
+    std::atomic<bool> pf_changed{false};
+    for_grains(c, [&](size_t lo, size_t hi) {
+        bool ch = false;
+        for (size_t g = lo; g < hi; ++g) {
+            const double v = c->ph.driving_force(c->rho[g]);
+            c->h_pforce[g] = v;
+            if (v != c->pforce_host[g]) { c->pforce_host[g] = v; ch = true; }
+        }
+        if (ch) pf_changed.store(true);
+    });
+    if (!pf_changed.load() && mob_same) return SCORE_OK;
     c->refresh = (c->refresh == 1 || !mob_same) ? 1 : 2;  // new mobilities need P again
     memcpy(c->mob_host, mob, sizeof mob);
-    if (pf == c->pforce_host) return SCORE_OK;
-    c->pforce_host = pf;
-    // pinned staging, stream-ordered before the next step's kernels; it is rewritten only
-    // after a later step's synchronisation
-    memcpy(c->h_pforce, pf.data(), pf.size() * 8);
-    const cudaError_t e = cudaMemcpyAsync(c->d_pforce, c->h_pforce, pf.size() * 8, cudaMemcpyHostToDevice, c->stream);
+    if (!pf_changed.load()) return SCORE_OK;
+    const cudaError_t e = cudaMemcpyAsync(c->d_pforce, c->h_pforce, (size_t)c->ndefg * 8, cudaMemcpyHostToDevice, c->stream);
     if (e != cudaSuccess) return c->cuda_fail(e, "upload driving force");
     return SCORE_OK;
 }
