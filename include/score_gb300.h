@@ -22,7 +22,7 @@
 extern "C" {
 #endif
 
-#define SCORE_ABI_VERSION 1
+#define SCORE_ABI_VERSION 2
 
 /* status codes */
 #define SCORE_OK                     0
@@ -218,6 +218,10 @@ typedef struct score_tune {
     int32_t claim_blocks_per_sm;   /* k_claim grid */
     int32_t commit_blocks_per_sm;  /* k_resolve / k_commit grid */
     int32_t use_graph;             /* 1: each step replays one captured CUDA graph */
+    int32_t spec_holes_pct;        /* k_grow_fill loads each slot's fill data together with its
+                                      infector byte while the last step's INACTIVE share of the
+                                      scanned slots was at most this percentage (0 never, 100
+                                      always); otherwise only for ACTIVE slots, after the byte */
     uint32_t steps;                /* autotuner: steps it ran */
     double fill_ns_per_slot;       /* autotuner: best grow time per front slot [ns] */
     double claim_ns_per_cell;      /* autotuner: best claim time per full cell [ns] */

@@ -79,7 +79,7 @@ class Timing(C.Structure):
 class Tune(C.Structure):
     _fields_ = [
         ("items", _i32), ("fill_blocks_per_sm", _i32), ("claim_blocks_per_sm", _i32), ("commit_blocks_per_sm", _i32),
-        ("use_graph", _i32), ("steps", _u32), ("fill_ns_per_slot", _d), ("claim_ns_per_cell", _d),
+        ("use_graph", _i32), ("spec_holes_pct", _i32), ("steps", _u32), ("fill_ns_per_slot", _d), ("claim_ns_per_cell", _d),
         ("commit_ns_per_cell", _d),
     ]
 

@@ -219,6 +219,8 @@ struct score_ctx {
     uint64_t rho_version = 0, pf_rho_version = ~0ull, rhomax_version = ~0ull;
     std::vector<uint32_t> rho_order;   // deformed grains by descending rho0 (rho max while rho == rho0)
     size_t rho_cursor = 0;             // rho_order[0, cursor) have no cells left
+    std::vector<double> rho_next;      // rho at the end of the running step (computed while it runs)
+    bool ahead = false;                // physics_ahead ran for the running step
 
     DomainArgs a{};
     DevState* d_state = nullptr;
@@ -302,6 +304,7 @@ struct TuneCfg {
     int fill_bpsm = 16;     // k_grow_fill blocks per SM
     int claim_bpsm = 2;     // k_claim blocks per SM (autotuner's choice on the 512^3 workload)
     int commit_bpsm = 8;    // k_resolve / k_commit blocks per SM (same)
+    int spec_pct = 30;      // fill data loaded with the infector byte up to this INACTIVE share [%]
     bool operator==(const TuneCfg& o) const {
         return items == o.items && fill_bpsm == o.fill_bpsm && claim_bpsm == o.claim_bpsm && commit_bpsm == o.commit_bpsm;
     }
@@ -510,17 +513,19 @@ namespace {
 template <class Body>
 void for_grains(score_ctx* c, Body body);
 
-// Driving force per deformed grain, the grow step's p (SCORE_Kernel.cpp:4082).  When it or
-// the mobilities change, the front's velocity factors are recomputed in the next grow.
-int upload_physics(score_ctx* c) {
+// Driving force per deformed grain, the grow step's p (SCORE_Kernel.cpp:4082), from `rho`
+// (whose version is `rho_ver`).  When it or the mobilities change, the front's velocity
+// factors are recomputed in the next grow.  The copy is stream-ordered after every launch
+// already enqueued, so a step in flight still reads the previous values.
+int upload_physics(score_ctx* c, const double* rho, uint64_t rho_ver) {
     const double mob[4] = {c->ph.mLAGB, c->ph.mHAGB, c->ph.mGS, c->ph.mRHHAGB};
     const bool mob_same = memcmp(mob, c->mob_host, sizeof mob) == 0;
     // p depends on Gb^2/2, the drag and rho only: skip the per-grain pass when none changed
     const double sig[2] = {c->ph.Gbhalfsq, c->ph.zener()};
-    if (mob_same && !c->pforce_host.empty() && memcmp(sig, c->pf_sig, sizeof sig) == 0 && c->pf_rho_version == c->rho_version)
+    if (mob_same && !c->pforce_host.empty() && memcmp(sig, c->pf_sig, sizeof sig) == 0 && c->pf_rho_version == rho_ver)
         return SCORE_OK;
     memcpy(c->pf_sig, sig, sizeof sig);
-    c->pf_rho_version = c->rho_version;
+    c->pf_rho_version = rho_ver;
     // new p per grain, straight into the pinned staging buffer (its last copy to the device
     // finished before the step that just ended), noting whether any value changed
     if (c->pforce_host.size() != c->ndefg) c->pforce_host.assign(c->ndefg, std::numeric_limits<double>::quiet_NaN());
@@ -528,7 +533,7 @@ int upload_physics(score_ctx* c) {
     for_grains(c, [&](size_t lo, size_t hi) {
         bool ch = false;
         for (size_t g = lo; g < hi; ++g) {
-            const double v = c->ph.driving_force(c->rho[g]);
+            const double v = c->ph.driving_force(rho[g]);
             c->h_pforce[g] = v;
             if (v != c->pforce_host[g]) { c->pforce_host[g] = v; ch = true; }
         }
@@ -562,6 +567,13 @@ void resolve_weights(score_ctx* c, const std::vector<unsigned long long>& idx, s
             val[i] = idx[i] == kMissVoid ? 0.0 : weight_of(c, (uint32_t)(idx[i] / c->ndefg), (uint32_t)(idx[i] % c->ndefg));
     };
     size_t n = idx.size();
+    Engine& E = *c->eng;
+    if (n >= 256 && E.dom.size() == 1) {  // one domain: the engine's workers (a batch runs its domains in parallel)
+        if (!E.pool) E.pool.reset(new WorkerPool(std::max(1u, std::min(7u, std::thread::hardware_concurrency() - 1))));
+        const int chunks = (int)std::min<size_t>(32, n / 64);
+        E.pool->run(chunks, [&](int k) { work(n * (size_t)k / chunks, n * (size_t)(k + 1) / chunks); });
+        return;
+    }
     unsigned nth = std::max(1u, std::min(32u, std::thread::hardware_concurrency()));
     if (n < 4096 || nth == 1) { work(0, n); return; }
     std::vector<std::thread> th;
@@ -761,8 +773,12 @@ int reset_state(score_ctx* c) {
     ph.dt = ph.dt_minimum();
     c->pforce_host.clear();
     memset(c->mob_host, 0, sizeof c->mob_host);
-    int s = upload_physics(c);
+    c->ahead = false;
+    int s = upload_physics(c, c->rho.data(), c->rho_version);
     if (s != SCORE_OK) return s;
+    // the staging buffer is rewritten while the first step runs: its copy must be done
+    e = cudaStreamSynchronize(st);
+    if (e != cudaSuccess) return c->cuda_fail(e, "reset domain");
     c->refresh = 0;  // the front is empty; new cells get their factors when they are created
     c->dt_cached = -1.0;
     c->Xcells = 0.0; c->step = 0; c->defrag_cnt = 0; c->n_nuclei = 0;
@@ -798,15 +814,41 @@ int pre_step(score_ctx* c, uint32_t* newnuc) {
     DomainArgs& a = c->a;
     a.dt_changed = (ph.dt != c->dt_cached) ? 1 : 0;
     a.refresh = c->refresh;
+    // load strategy of k_grow_fill from the INACTIVE share of the last step's scanned slots
+    const uint64_t scanned = (uint64_t)c->last.next_never[0] + c->last.next_never[1];
+    a.spec = 100 * (scanned - std::min<uint64_t>(c->last.Sv, scanned)) <= (uint64_t)c->eng->cfg.spec_pct * scanned ? 1 : 0;
     a.active = 1;
     c->dt_cached = ph.dt;
     c->refresh = 0;
     return SCORE_OK;
 }
 
+bool recovering(const score_ctx* c) {
+    return c->prm.recovery_model != SCORE_RECOVERY_NONE && c->prm.recovery_model != SCORE_RECOVERY_NES_SOLUTEDRAG;
+}
+
+// The part of the master block of solve_RXGROWTH (SCORE_Kernel.cpp:6691-6740) that does not
+// depend on the step's outcome, run while the step is on the GPU: t + dt, temperature, G and
+// b, drag, mobilities, the recovered rho (into rho_next: the rho max of the step still needs
+// the current values) and the next step's driving forces.  The rest (P max, X, rho max, dt)
+// follows in post_step, in the reference's order; none of it feeds back into this part.
+int physics_ahead(score_ctx* c) {
+    Physics& ph = c->ph;
+    ph.t += ph.dt;
+    ph.update_temperature();
+    ph.update_atomistic();
+    ph.update_microchemistry();
+    ph.update_mobilities();
+    c->ahead = true;
+    if (!recovering(c)) return upload_physics(c, c->rho.data(), c->rho_version);
+    c->rho_next.resize(c->ndefg);
+    for_grains(c, [&](size_t lo, size_t hi) { ph.update_substructure(c->rho_next.data(), c->rho.data(), c->rho0.data(), lo, hi); });
+    return upload_physics(c, c->rho_next.data(), c->rho_version + 1);
+}
+
 // After the step: the mailbox (scalars, weight requests, depleted grains), the host's
-// weights for the requests (applied at the start of the next step), and the master
-// block of solve_RXGROWTH (SCORE_Kernel.cpp:6691-6740).
+// weights for the requests (applied at the start of the next step), and the rest of the
+// master block of solve_RXGROWTH (SCORE_Kernel.cpp:6691-6740).
 int post_step(score_ctx* c, uint32_t newnuc, score_step_stats* out) {
     Physics& ph = c->ph;
     DomainArgs& a = c->a;
@@ -878,19 +920,17 @@ int post_step(score_ctx* c, uint32_t newnuc, score_step_stats* out) {
         c->rhomax_version = c->rho_version;
     }
     const double rhomax_step = ph.rhomax;
-    ph.t += ph.dt;
-    ph.update_temperature();
-    ph.update_atomistic();
-    ph.update_microchemistry();
-    ph.update_mobilities();
-    if (c->prm.recovery_model != SCORE_RECOVERY_NONE && c->prm.recovery_model != SCORE_RECOVERY_NES_SOLUTEDRAG) {
-        for_grains(c, [&](size_t lo, size_t hi) { ph.update_substructure(c->rho.data(), c->rho0.data(), lo, hi); });
+    if (!c->ahead) {
+        const int s = physics_ahead(c);
+        if (s != SCORE_OK) return s;
+    }
+    c->ahead = false;
+    if (recovering(c)) {
+        c->rho.swap(c->rho_next);
         c->rho_version++;
     }
     ph.dt = ph.dt_minimum();
     c->step++;
-    int s = upload_physics(c);
-    if (s != SCORE_OK) return s;
 
     score_step_stats& o = c->last;
     o = score_step_stats{};
@@ -1046,6 +1086,22 @@ int Engine::step(bool timed) {
     const auto pre_t1 = std::chrono::steady_clock::now();
     tm.pre_ms += std::chrono::duration<double, std::milli>(pre_t1 - host_t0).count();
     cudaError_t e = enqueue_step(n);
+    // while the GPU steps: each domain's outcome-independent physics for the next step
+    std::vector<int> status(n, SCORE_OK);
+    if (e == cudaSuccess) {
+        auto ahead = [&](int i) {
+            score_ctx* c = dom[i];
+            if (!c->running) return;
+            cudaSetDevice(device);  // the calling thread may be a worker
+            status[i] = physics_ahead(c);
+        };
+        if (n >= 4) {
+            if (!pool) pool.reset(new WorkerPool(std::max(1u, std::min(15u, std::thread::hardware_concurrency() - 1))));
+            pool->run(n, ahead);
+        } else {
+            for (int i = 0; i < n; ++i) ahead(i);
+        }
+    }
     const auto wait_t0 = std::chrono::steady_clock::now();
     if (e == cudaSuccess) e = cudaStreamSynchronize(stream);  // the one wait of the step: the mailboxes are filled
     const auto wait_t1 = std::chrono::steady_clock::now();
@@ -1066,8 +1122,9 @@ int Engine::step(bool timed) {
     }
     tm.grow_launches += 1;
     const double bpu = fp32 ? 21.0 : 25.0;  // algorithmic bytes per front-cell update of k_grow_fill
-    // the master-block work of each domain (weights, physics, dt) is independent
-    std::vector<int> status(n, SCORE_OK);
+    for (int i = 0; i < n; ++i)
+        if (status[i] != SCORE_OK) return fail(status[i], dom[i]->err);
+    // the master-block work of each domain (weights, P max, X, rho max, dt) is independent
     auto post = [&](int i) {
         score_ctx* c = dom[i];
         if (!c->running) return;
@@ -1242,13 +1299,16 @@ void Engine::get_tune(score_tune* out) const {
     out->claim_blocks_per_sm = cfg.claim_bpsm;
     out->commit_blocks_per_sm = cfg.commit_bpsm;
     out->use_graph = use_graph ? 1 : 0;
+    out->spec_holes_pct = cfg.spec_pct;
 }
 
 int Engine::set_tune(const score_tune* t) {
     if (t->items != 4 && t->items != 8 && t->items != 16) return fail(SCORE_ERR_ARG, "items must be 4, 8 or 16");
     for (int v : {t->fill_blocks_per_sm, t->claim_blocks_per_sm, t->commit_blocks_per_sm})
         if (v < 1 || v > 64) return fail(SCORE_ERR_ARG, "blocks per SM must be in 1..64");
+    if (t->spec_holes_pct < 0 || t->spec_holes_pct > 100) return fail(SCORE_ERR_ARG, "spec_holes_pct must be in 0..100");
     cfg.items = t->items;
+    cfg.spec_pct = t->spec_holes_pct;
     cfg.fill_bpsm = t->fill_blocks_per_sm;
     cfg.claim_bpsm = t->claim_blocks_per_sm;
     cfg.commit_bpsm = t->commit_blocks_per_sm;

@@ -4,9 +4,10 @@
 // FP64 instructions off the per-update critical path.  Every front cell stores
 //   vel = (m(P) * p(defg)) * f_geo(infector)      (the reference's first three roundings)
 //   inc = (vel * dt) * (1/cellsize)               (its fill increment for the current dt)
-// vel is computed once when the cell is infected (again only when T, rho or the drag
-// change); inc is recomputed only when dt changed or for cells infected in the last
-// step (kStale bit of the infector byte).  A typical update is then one DADD,
+// Both are computed when the cell is infected (with that step's dt); vel again only when
+// T, rho or the drag change, inc only when dt changed or for a cell whose vel was not
+// known at infection (a nucleus, or a weight the host computes: kStale bit of the
+// infector byte).  A typical update is then one DADD,
 //   fill = fill + inc,
 // with the "fill >= 1" test on the integer bit pattern (fill is never negative).
 // A cell whose driving force is <= 5e-16 stores vel = inc = -1 and is skipped, as the
@@ -114,6 +115,8 @@ struct DomainArgs {
     HostBox* box;               // device view of the domain's mailbox
     double mLAGB, mHAGB, mGS, mRH, dt, cinv;
     float dtc32;
+    int32_t spec;               // few INACTIVE slots: k_grow_fill loads every slot's fill data with its
+                                // infector byte instead of after it (no effect on results)
     // device classification of mobility weights whose value is an exact constant
     const double* rxq;          // nrxg x 4 orientation quaternions
     const double* dfq;          // ndefg x 4
@@ -295,7 +298,10 @@ __device__ __forceinline__ void tile_prefix(const uint32_t* cnt, const uint32_t*
 //                 slot order; the warp of a list's last tile stores the list totals.
 // REFRESH 1: recompute vel of every active slot from the P table and the current
 // physics (after T changed the mobilities); REFRESH 2: from the cell's cached mobility
-// (only rho or the drag changed the driving force), no table gather.
+// (only rho or the drag changed the driving force), no table gather; REFRESH 3: as 0 with
+// dt unchanged, the slot's cached increment and fill loaded together with its infector
+// byte, for every slot below the high-water mark (one memory round trip instead of two,
+// at the price of reading the fill data of INACTIVE slots too).
 // A cell created last step whose weight the host computed: P = answer `tag`; the table
 // entry (tagged until now) gets the value for later lookups.
 __device__ __forceinline__ double answered_velocity(const DomainArgs& a, const DFront& fr, uint32_t slot, uint8_t dir,
@@ -326,6 +332,29 @@ __device__ __forceinline__ uint32_t grow_tile(const DomainArgs& a, int L, uint32
     bool full[ITEMS];
     if (!FP32) {
         double w[ITEMS], fill[ITEMS];  // w: cached inc, or vel when the increment is stale
+        if (REFRESH == 3) {
+#pragma unroll
+            for (int k = 0; k < ITEMS; ++k) {
+                const uint32_t slot = base + (uint32_t)(k * 32);
+                w[k] = -1.0; fill[k] = 0.0;
+                if (slot < n) {
+                    w[k] = fr.inc[slot];
+                    fill[k] = ((const double*)fr.fill)[slot];
+                }
+            }
+#pragma unroll
+            for (int k = 0; k < ITEMS; ++k) {
+                const uint32_t slot = base + (uint32_t)(k * 32);
+                if (d[k] != kInactive && (d[k] & kStale)) {
+                    if (d[k] & kPend) {
+                        w[k] = answered_velocity(a, fr, slot, d[k], ((const unsigned long long*)fr.vel)[slot]);
+                        ((double*)fr.vel)[slot] = w[k];
+                    } else {
+                        w[k] = ((const double*)fr.vel)[slot];
+                    }
+                }
+            }
+        } else {
 #pragma unroll
         for (int k = 0; k < ITEMS; ++k) {
             const uint32_t slot = base + (uint32_t)(k * 32);
@@ -352,6 +381,7 @@ __device__ __forceinline__ uint32_t grow_tile(const DomainArgs& a, int L, uint32
                 fill[k] = ((const double*)fr.fill)[slot];
             }
         }
+        }
 #pragma unroll
         for (int k = 0; k < ITEMS; ++k) {
             full[k] = false;
@@ -359,7 +389,7 @@ __device__ __forceinline__ uint32_t grow_tile(const DomainArgs& a, int L, uint32
                 ++sv;
                 const uint32_t slot = base + (uint32_t)(k * 32);
                 double inc = w[k];
-                if (REFRESH != 0 || a.dt_changed || (d[k] & kStale)) {
+                if (REFRESH == 1 || REFRESH == 2 || (REFRESH == 0 && a.dt_changed) || (d[k] & kStale)) {
                     if (__double_as_longlong(w[k]) >= 0) inc = __dmul_rn(__dmul_rn(w[k], a.dt), a.cinv);
                     fr.inc[slot] = inc;
                     if (d[k] & kStale) fr.dir[slot] = d[k] & kCodeMask;
@@ -373,6 +403,26 @@ __device__ __forceinline__ uint32_t grow_tile(const DomainArgs& a, int L, uint32
         }
     } else {
         float vel[ITEMS], fill[ITEMS], comp[ITEMS];
+        if (REFRESH == 3) {
+#pragma unroll
+            for (int k = 0; k < ITEMS; ++k) {
+                const uint32_t slot = base + (uint32_t)(k * 32);
+                vel[k] = -1.0f; fill[k] = 0.0f; comp[k] = 0.0f;
+                if (slot < n) {
+                    vel[k] = ((const float*)fr.vel)[slot];
+                    fill[k] = ((const float*)fr.fill)[slot];
+                    comp[k] = fr.comp[slot];
+                }
+            }
+#pragma unroll
+            for (int k = 0; k < ITEMS; ++k) {
+                const uint32_t slot = base + (uint32_t)(k * 32);
+                if (d[k] != kInactive && (d[k] & kPend)) {
+                    vel[k] = (float)answered_velocity(a, fr, slot, d[k], ((const uint32_t*)fr.vel)[slot]);
+                    ((float*)fr.vel)[slot] = vel[k];
+                }
+            }
+        } else {
 #pragma unroll
         for (int k = 0; k < ITEMS; ++k) {
             const uint32_t slot = base + (uint32_t)(k * 32);
@@ -397,6 +447,7 @@ __device__ __forceinline__ uint32_t grow_tile(const DomainArgs& a, int L, uint32
                 fill[k] = ((const float*)fr.fill)[slot];
                 comp[k] = fr.comp[slot];
             }
+        }
         }
 #pragma unroll
         for (int k = 0; k < ITEMS; ++k) {
@@ -460,7 +511,7 @@ __global__ void __launch_bounds__(kBlock, ITEMS >= 16 ? 2 : 4) k_grow_fill(int b
     if (ONE) {
         const DomainArgs& a = c_args[base];
         if (!a.active) return;
-#pragma unroll
+#pragma unroll 1
         for (int L = 0; L < 2; ++L) {
             const uint32_t n = a.st->next_never[L];
             const uint32_t ntiles = (n + S::kTile - 1) / S::kTile;
@@ -469,6 +520,8 @@ __global__ void __launch_bounds__(kBlock, ITEMS >= 16 ? 2 : 4) k_grow_fill(int b
                 for (uint32_t tile = blockIdx.x; tile < ntiles; tile += gridDim.x) sv += grow_tile<FP32, 1, ITEMS>(a, L, tile, n);
             } else if (a.refresh == 2) {
                 for (uint32_t tile = blockIdx.x; tile < ntiles; tile += gridDim.x) sv += grow_tile<FP32, 2, ITEMS>(a, L, tile, n);
+            } else if (a.spec && !a.dt_changed) {
+                for (uint32_t tile = blockIdx.x; tile < ntiles; tile += gridDim.x) sv += grow_tile<FP32, 3, ITEMS>(a, L, tile, n);
             } else {
                 for (uint32_t tile = blockIdx.x; tile < ntiles; tile += gridDim.x) sv += grow_tile<FP32, 0, ITEMS>(a, L, tile, n);
             }
@@ -495,6 +548,7 @@ __global__ void __launch_bounds__(kBlock, ITEMS >= 16 ? 2 : 4) k_grow_fill(int b
         const uint32_t n = a.st->next_never[L];
         if (a.refresh == 1) sv += grow_tile<FP32, 1, ITEMS>(a, L, tile, n);
         else if (a.refresh == 2) sv += grow_tile<FP32, 2, ITEMS>(a, L, tile, n);
+        else if (a.spec && !a.dt_changed) sv += grow_tile<FP32, 3, ITEMS>(a, L, tile, n);
         else sv += grow_tile<FP32, 0, ITEMS>(a, L, tile, n);
     }
     if (cur >= 0) flush_sv(c_args[base + (cur >> 1)], cur & 1, sv);
@@ -1023,9 +1077,16 @@ __global__ void __launch_bounds__(kBlock, 3) k_commit(int base, int ndom) {
             if (lookup_p(a, rs, gt, P, tag)) {
                 const double mo = mobility(a, P);
                 dst.mob[ns] = mo;
-                if (!FP32) ((double*)dst.vel)[ns] = velocity_from_mobility(a, mo, gt, c_code[d]);
-                else ((float*)dst.vel)[ns] = (float)velocity_from_mobility(a, mo, gt, c_code[d]);
-                dst.dir[ns] = c_code[d] | kStale;
+                const double v = velocity_from_mobility(a, mo, gt, c_code[d]);
+                if (!FP32) {
+                    // the increment with this step's dt: valid next step unless dt changes, when
+                    // k_grow_fill recomputes every increment from vel anyway
+                    ((double*)dst.vel)[ns] = v;
+                    dst.inc[ns] = __double_as_longlong(v) >= 0 ? __dmul_rn(__dmul_rn(v, a.dt), a.cinv) : v;
+                } else {
+                    ((float*)dst.vel)[ns] = (float)v;
+                }
+                dst.dir[ns] = c_code[d];
                 if (P > pmax) pmax = P;
             } else {
                 // vel holds the answer tag until the next k_grow_fill

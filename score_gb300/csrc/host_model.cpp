@@ -266,6 +266,10 @@ void Physics::update_substructure(std::vector<double>& rho, const std::vector<do
 
 // grains [lo, n) of the same update (the per-step scalars are recomputed, identically)
 void Physics::update_substructure(double* rho, const double* rho0, size_t lo, size_t n) const {
+    update_substructure(rho, rho, rho0, lo, n);
+}
+
+void Physics::update_substructure(double* rho_out, const double* rho_in, const double* rho0, size_t lo, size_t n) const {
     const int m = prm->recovery_model;
     if (m == SCORE_RECOVERY_NES_VACCOREDIFF) {
         double B = kPi * prm->NesC3 * prm->NesC5 * prm->VacancyDiffD0 * std::exp(-1.0 * prm->VacancyDiffHact / (kBoltzmann * T));
@@ -273,10 +277,10 @@ void Physics::update_substructure(double* rho, const double* rho0, size_t lo, si
         double exponent = ((b) * (b)) / (kBoltzmann * T);
         double expterm = std::exp(prm->NesAlpha3 * prm->NesKappa2 * G * b * exponent);
         for (size_t g = lo; g < n; ++g) {
-            double r_t = 1.0 / std::pow(rho[g], 0.5);
+            double r_t = 1.0 / std::pow(rho_in[g], 0.5);
             double Bx = (B / r_t) * expterm;
             double r_tdt = (Bx * dt) + r_t;
-            rho[g] = 1.0 / ((r_tdt) * (r_tdt));
+            rho_out[g] = 1.0 / ((r_tdt) * (r_tdt));
         }
         return;
     }
@@ -284,12 +288,12 @@ void Physics::update_substructure(double* rho, const double* rho0, size_t lo, si
         const double f1 = 0.25, f2 = 0.75, tau2 = 0.3605, tau5 = 5.2824;
         double tm = t / 60.0;
         double factor = f1 * std::pow((1 + (tm / tau2)), -1.0) + f2 * std::pow((1 + (tm / tau5)), -0.5);
-        for (size_t g = lo; g < n; ++g) rho[g] = rho0[g] * ((factor) * (factor));
+        for (size_t g = lo; g < n; ++g) rho_out[g] = rho0[g] * ((factor) * (factor));
         return;
     }
     if (m == SCORE_RECOVERY_HYPERBOLIC) {
         double f = 1.0 + prm->recovery_k * t;
-        for (size_t g = lo; g < n; ++g) rho[g] = rho0[g] / f;
+        for (size_t g = lo; g < n; ++g) rho_out[g] = rho0[g] / f;
     }
 }
 

@@ -70,6 +70,8 @@ struct Physics {
     // recovery of the per-grain dislocation densities after t += dt
     void update_substructure(std::vector<double>& rho, const std::vector<double>& rho0) const;
     void update_substructure(double* rho, const double* rho0, size_t lo, size_t hi) const;
+    // the same update of grains [lo, hi) from rho_in into rho_out (rho_out may be rho_in)
+    void update_substructure(double* rho_out, const double* rho_in, const double* rho0, size_t lo, size_t hi) const;
     // driving force p = (Gb^2/2 (rho - rho_rx)) - p_zener, the grow step's inner expression
     double driving_force(double rho) const;
 };
