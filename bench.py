@@ -278,6 +278,9 @@ class PlainWorkload:
     def launches(self):
         return self.gm.timing().kernel_launches
 
+    def timing_every(self):
+        return self.gm.tune().timing_every
+
     def e2e(self, runs):
         sg, d, n = self.sg, self.d, self.n
         pin = [pinned_copy(x) for x in (d.grid, d.defg_quat, d.defg_rho0, d.rxg_quat, d.rxg_site, d.rxg_tincub)]
@@ -369,6 +372,9 @@ class BatchWorkload:
 
     def launches(self):
         return self.b.timing().kernel_launches
+
+    def timing_every(self):
+        return self.b.tune().timing_every
 
     def e2e(self, runs):
         sg, b = self.sg, self.b
@@ -466,7 +472,7 @@ def main():
         wl.run()
     barrier(dist)
     launches0 = wl.launches()
-    tot_sv, tot_steps, run_ms, grow_bytes, grow_launches = 0, 0, 0.0, 0.0, 0
+    tot_sv, tot_steps, run_ms, grow_bytes, grow_launches, timed_steps = 0, 0, 0.0, 0.0, 0, 0
     phase = {"grow_ms": 0.0, "fill_ms": 0.0, "claim_ms": 0.0, "commit_ms": 0.0, "host_ms": 0.0, "wait_ms": 0.0,
              "weights_ms": 0.0, "pre_ms": 0.0, "post_ms": 0.0}
     with ClockSampler(local) as clk:
@@ -477,9 +483,15 @@ def main():
             run_ms += tm.run_ms
             grow_bytes += tm.grow_bytes
             grow_launches += tm.grow_launches
+            timed_steps += tm.timed_steps
             for k in phase:
                 phase[k] += getattr(tm, k)
-    fill_ms = phase["fill_ms"]
+    fill_ms = phase["fill_ms"]  # over the timed steps, like grow_bytes
+    # device phases are timed with CUDA events on every k-th step only (events cost device
+    # time); scaled to whole runs for the breakdown
+    scale = grow_launches / timed_steps if timed_steps else 0.0
+    for k in ("grow_ms", "fill_ms", "claim_ms", "commit_ms"):
+        phase[k] *= scale
     launches = wl.launches() - launches0
     barrier(dist)
     t_max = reduce_max(dist, run_ms / 1e3)
@@ -496,6 +508,7 @@ def main():
         e_s = reduce_max(dist, e_s)
         e_value = reduce_sum(dist, float(e_sv)) / e_s
     fp32_err = wl.fp32_error() if args.precision == 1 else None
+    every = wl.timing_every()
     wl.close()
 
     if rank == 0:
@@ -507,13 +520,16 @@ def main():
         if tf.exists() and args.workload == "plain" and args.precision == 0:
             try:
                 tj = json.loads(tf.read_text())
-                traffic = tj["dram_bytes_per_update"] * (tot_sv / max(1, grow_launches))
+                traffic = tj["dram_bytes_per_update"] * (grow_bytes / bpu) / max(1, timed_steps)
             except Exception:
                 traffic = None
         cfg = wl.config()
         cfg.update({"growth_steps_per_run": tot_steps // args.steps, "updates_per_run": tot_sv // args.steps,
                     "time_to_X099_ms": run_ms / args.steps, "parallelism": f"{world} independent ranks",
                     "phase_ms_per_run": {k: v / args.steps for k, v in phase.items()},
+                    "phase_sampling": f"device phases (grow, fill, claim, commit) timed with CUDA events on {timed_steps} "
+                                      f"of {grow_launches} steps (every {every}th) and scaled to the runs; "
+                                      f"roofline over the timed fill launches; host phases every step",
                     "host_weight_misses_per_run": wl.misses})
         if wl.tuned is not None:
             t = wl.tuned

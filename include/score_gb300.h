@@ -22,7 +22,7 @@
 extern "C" {
 #endif
 
-#define SCORE_ABI_VERSION 2
+#define SCORE_ABI_VERSION 3
 
 /* status codes */
 #define SCORE_OK                     0
@@ -189,15 +189,18 @@ int  score_grain_counts(score_ctx* ctx, uint32_t* rxg_counts, uint32_t* defg_cou
  * stream): kernel-only ms per phase, ms of the dominant (grow) kernel, its
  * launches, the algorithmic bytes those launches moved, and run_ms = event time
  * from the start of the restart/reset to the end of the last score_run_until */
+/* Device phase times (total, grow, claim, commit, fill) and the algorithmic bytes are sums over
+ * the TIMED steps: every timing_every-th step of a run (score_tune), timed_steps of them; the
+ * steps in between run without phase events.  Host times and counts cover every step. */
 typedef struct score_timing {
     double total_ms;        /* device time of the step kernels */
     double grow_ms;         /* the fill update and the FullRX / recycle lists (k_grow_fill, k_grow_lists) */
     double claim_ms;        /* the infection attempts (k_claim) */
     double commit_ms;       /* resolve, commit (new cells, weights) and step end */
     double host_ms;         /* host wall time inside the step calls, the wait included */
-    uint64_t grow_launches;
-    double grow_bytes;      /* algorithmic bytes of all grow launches */
-    double step_bytes;      /* algorithmic bytes of all kernels */
+    uint64_t grow_launches; /* steps (every step launches the grow kernels once) */
+    double grow_bytes;      /* algorithmic bytes of the timed grow launches */
+    double step_bytes;      /* algorithmic bytes of all kernels of the timed steps */
     uint64_t kernel_launches;  /* kernels launched by this context since creation */
     double run_ms;          /* device span of the last restart .. score_run_until */
     double fill_ms;         /* the fill-update kernels alone (part of grow_ms) */
@@ -205,6 +208,7 @@ typedef struct score_timing {
     double weights_ms;      /* host time computing requested mobility weights (libm FP64) */
     double pre_ms;          /* host time before the launch (nucleation, arguments) */
     double post_ms;         /* host wall time after the wait (mailboxes, weights, physics) */
+    uint64_t timed_steps;   /* steps whose device phases were timed */
 } score_timing;
 int  score_get_timing(score_ctx* ctx, score_timing* out);
 
@@ -222,6 +226,8 @@ typedef struct score_tune {
                                       infector byte while the last step's INACTIVE share of the
                                       scanned slots was at most this percentage (0 never, 100
                                       always); otherwise only for ACTIVE slots, after the byte */
+    int32_t timing_every;          /* device phase events on every k-th step of a run (1 every
+                                      step, 0 never; default 8): events cost device time */
     uint32_t steps;                /* autotuner: steps it ran */
     double fill_ns_per_slot;       /* autotuner: best grow time per front slot [ns] */
     double claim_ns_per_cell;      /* autotuner: best claim time per full cell [ns] */

@@ -73,13 +73,14 @@ class Timing(C.Structure):
         ("total_ms", _d), ("grow_ms", _d), ("claim_ms", _d), ("commit_ms", _d), ("host_ms", _d),
         ("grow_launches", C.c_uint64), ("grow_bytes", _d), ("step_bytes", _d), ("kernel_launches", C.c_uint64),
         ("run_ms", _d), ("fill_ms", _d), ("wait_ms", _d), ("weights_ms", _d), ("pre_ms", _d), ("post_ms", _d),
+        ("timed_steps", C.c_uint64),
     ]
 
 
 class Tune(C.Structure):
     _fields_ = [
         ("items", _i32), ("fill_blocks_per_sm", _i32), ("claim_blocks_per_sm", _i32), ("commit_blocks_per_sm", _i32),
-        ("use_graph", _i32), ("spec_holes_pct", _i32), ("steps", _u32), ("fill_ns_per_slot", _d), ("claim_ns_per_cell", _d),
+        ("use_graph", _i32), ("spec_holes_pct", _i32), ("timing_every", _i32), ("steps", _u32), ("fill_ns_per_slot", _d), ("claim_ns_per_cell", _d),
         ("commit_ns_per_cell", _d),
     ]
 

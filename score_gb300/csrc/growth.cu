@@ -305,6 +305,8 @@ struct TuneCfg {
     int claim_bpsm = 2;     // k_claim blocks per SM (autotuner's choice on the 512^3 workload)
     int commit_bpsm = 8;    // k_resolve / k_commit blocks per SM (same)
     int spec_pct = 30;      // fill data loaded with the infector byte up to this INACTIVE share [%]
+    int timing_every = 8;   // phase events on every k-th step of a run (0 never): each event costs
+                            // microseconds of device time, so the steps in between run without
     bool operator==(const TuneCfg& o) const {
         return items == o.items && fill_bpsm == o.fill_bpsm && claim_bpsm == o.claim_bpsm && commit_bpsm == o.commit_bpsm;
     }
@@ -413,10 +415,12 @@ struct Engine {
     TuneCfg cfg;
     bool use_graph = true;
     bool capturing = false;
-    cudaGraphExec_t gexec = nullptr;
-    TuneCfg gcfg;
-    int gndom = -1;
-    bool gfp32 = false;
+    bool events = false;               // the sequence being launched records the phase events
+    cudaGraphExec_t gexec[2] = {nullptr, nullptr};  // the step without / with phase events
+    TuneCfg gcfg[2];
+    int gndom[2] = {-1, -1};
+    bool gfp32[2] = {false, false};
+    uint64_t run_steps = 0;            // steps since the run started (phase sampling)
     // 0 start, 1 end of fill, 2 end of lists, 3 end of claim, 4 end of step, 5/6 run span
     cudaEvent_t ev[7] = {nullptr, nullptr, nullptr, nullptr, nullptr, nullptr, nullptr};
     score_timing tm{};
@@ -449,9 +453,11 @@ struct Engine {
         return e == cudaSuccess ? SCORE_OK : SCORE_ERR_CUDA;
     }
     void drop_graph() {
-        if (gexec) cudaGraphExecDestroy(gexec);
-        gexec = nullptr;
-        gndom = -1;
+        for (int k = 0; k < 2; ++k) {
+            if (gexec[k]) cudaGraphExecDestroy(gexec[k]);
+            gexec[k] = nullptr;
+            gndom[k] = -1;
+        }
     }
     void release() {
         cudaSetDevice(device);
@@ -470,13 +476,14 @@ struct Engine {
     }
     int fail(int code, const std::string& m) { err = m; return code; }
     void launch_sequence(int n);
-    cudaError_t enqueue_step(int n);
+    cudaError_t enqueue_step(int n, bool timed);
     int step(bool timed);
     int run_until(double x_target, uint32_t max_steps, uint32_t* steps_done);
     int autotune(double x_target, uint32_t max_steps, score_tune* out);
     void get_tune(score_tune* out) const;
     int set_tune(const score_tune* t);
-    void mark_run_start() { cudaEventRecord(ev[5], stream); }
+    void mark_run_start() { cudaEventRecord(ev[5], stream); run_steps = 0; }
+    bool sample_step() const { return cfg.timing_every > 0 && run_steps % (uint64_t)cfg.timing_every == 0; }
     int mark_run_end();
 };
 
@@ -952,6 +959,7 @@ bool domain_done(const score_ctx* c, double xt) {
 
 // phase boundary: a real event record node when the sequence is captured into a graph
 inline void record(const Engine& E, int k) {
+    if (!E.events) return;
     if (E.capturing) cudaEventRecordWithFlags(E.ev[k], E.stream, cudaEventRecordExternal);
     else cudaEventRecord(E.ev[k], E.stream);
 }
@@ -998,7 +1006,7 @@ void Engine::launch_sequence(int n) {
 }
 
 // the argument copy and the kernels of one step, as a graph replay or direct launches
-cudaError_t Engine::enqueue_step(int n) {
+cudaError_t Engine::enqueue_step(int n, bool timed) {
     // the argument blocks only change when dt, the physics or a domain's state changes
     cudaError_t e = cudaSuccess;
     if (args_dirty || memcmp(h_args, h_args_dev.data(), (size_t)n * sizeof(DomainArgs)) != 0) {
@@ -1007,13 +1015,17 @@ cudaError_t Engine::enqueue_step(int n) {
         args_dirty = false;
     }
     if (e != cudaSuccess) return e;
+    events = timed;
     if (!use_graph) {
         launch_sequence(n);
         launches += kStepKernels;
         return cudaGetLastError();
     }
-    if (!gexec || gndom != n || !(gcfg == cfg) || gfp32 != fp32) {
-        drop_graph();
+    const int k = timed ? 1 : 0;
+    if (!gexec[k] || gndom[k] != n || !(gcfg[k] == cfg) || gfp32[k] != fp32) {
+        if (gexec[k]) cudaGraphExecDestroy(gexec[k]);
+        gexec[k] = nullptr;
+        gndom[k] = -1;
         cudaGraph_t g = nullptr;
         e = cudaStreamBeginCapture(stream, cudaStreamCaptureModeThreadLocal);
         if (e != cudaSuccess) return e;
@@ -1021,13 +1033,13 @@ cudaError_t Engine::enqueue_step(int n) {
         launch_sequence(n);
         capturing = false;
         e = cudaStreamEndCapture(stream, &g);
-        if (e == cudaSuccess) e = cudaGraphInstantiate(&gexec, g, 0);
+        if (e == cudaSuccess) e = cudaGraphInstantiate(&gexec[k], g, 0);
         if (g) cudaGraphDestroy(g);
-        if (e != cudaSuccess) { gexec = nullptr; return e; }
-        gndom = n; gcfg = cfg; gfp32 = fp32;
+        if (e != cudaSuccess) { gexec[k] = nullptr; return e; }
+        gndom[k] = n; gcfg[k] = cfg; gfp32[k] = fp32;
     }
     launches += kStepKernels;
-    return cudaGraphLaunch(gexec, stream);
+    return cudaGraphLaunch(gexec[k], stream);
 }
 
 // Pack every domain's answered weights into the pinned, device-mapped staging buffer
@@ -1085,7 +1097,8 @@ int Engine::step(bool timed) {
     if (nrun == 0) return SCORE_OK;
     const auto pre_t1 = std::chrono::steady_clock::now();
     tm.pre_ms += std::chrono::duration<double, std::milli>(pre_t1 - host_t0).count();
-    cudaError_t e = enqueue_step(n);
+    cudaError_t e = enqueue_step(n, timed);
+    ++run_steps;
     // while the GPU steps: each domain's outcome-independent physics for the next step
     std::vector<int> status(n, SCORE_OK);
     if (e == cudaSuccess) {
@@ -1119,6 +1132,7 @@ int Engine::step(bool timed) {
         if (e != cudaSuccess) return fail(SCORE_ERR_CUDA, std::string("phase timing: ") + cudaGetErrorString(e));
         tm.fill_ms += f; tm.grow_ms += g; tm.claim_ms += cl; tm.commit_ms += cm;
         tm.total_ms += g + cl + cm;
+        tm.timed_steps += 1;
     }
     tm.grow_launches += 1;
     const double bpu = fp32 ? 21.0 : 25.0;  // algorithmic bytes per front-cell update of k_grow_fill
@@ -1142,8 +1156,10 @@ int Engine::step(bool timed) {
         if (!c->running) continue;
         if (status[i] != SCORE_OK) return fail(status[i], c->err);
         const score_step_stats& st = c->last;
-        tm.grow_bytes += bpu * (double)st.Sv;
-        tm.step_bytes += bpu * (double)st.Sv + 120.0 * (double)st.n_full + 37.0 * (double)st.n_new;
+        if (timed) {  // bytes of the timed steps, so that bytes / time is a rate
+            tm.grow_bytes += bpu * (double)st.Sv;
+            tm.step_bytes += bpu * (double)st.Sv + 120.0 * (double)st.n_full + 37.0 * (double)st.n_new;
+        }
         tm.weights_ms += c->weights_ms;
         c->weights_ms = 0.0;
     }
@@ -1177,7 +1193,7 @@ int Engine::run_until(double x_target, uint32_t max_steps, uint32_t* steps_done)
             nrun += c->running;
         }
         if (nrun == 0 || (max_steps && k >= max_steps)) break;
-        const int s = step(true);
+        const int s = step(sample_step());
         if (s != SCORE_OK) { if (steps_done) *steps_done = k; return s; }
         for (score_ctx* c : dom) if (c->running) c->trace.push_back(c->last);
         ++k;
@@ -1277,7 +1293,7 @@ int Engine::autotune(double x_target, uint32_t max_steps, score_tune* out) {
         return b;
     };
     const int bf = best(ft, fu, 12), bc = best(ct, cu, 4), bm = best(mt, mu, 4);
-    TuneCfg t = TuneCfg{};
+    TuneCfg t = cfg;  // the load strategy and the timing sample stay as they were set
     if (bf >= 0) { t.items = kItems[bf / 4]; t.fill_bpsm = kFill[bf % 4]; }
     if (bc >= 0) t.claim_bpsm = kOther[bc];
     if (bm >= 0) t.commit_bpsm = kOther[bm];
@@ -1300,6 +1316,7 @@ void Engine::get_tune(score_tune* out) const {
     out->commit_blocks_per_sm = cfg.commit_bpsm;
     out->use_graph = use_graph ? 1 : 0;
     out->spec_holes_pct = cfg.spec_pct;
+    out->timing_every = cfg.timing_every;
 }
 
 int Engine::set_tune(const score_tune* t) {
@@ -1307,6 +1324,8 @@ int Engine::set_tune(const score_tune* t) {
     for (int v : {t->fill_blocks_per_sm, t->claim_blocks_per_sm, t->commit_blocks_per_sm})
         if (v < 1 || v > 64) return fail(SCORE_ERR_ARG, "blocks per SM must be in 1..64");
     if (t->spec_holes_pct < 0 || t->spec_holes_pct > 100) return fail(SCORE_ERR_ARG, "spec_holes_pct must be in 0..100");
+    if (t->timing_every < 0) return fail(SCORE_ERR_ARG, "timing_every must be >= 0");
+    cfg.timing_every = t->timing_every;
     cfg.items = t->items;
     cfg.spec_pct = t->spec_holes_pct;
     cfg.fill_bpsm = t->fill_blocks_per_sm;
@@ -1526,7 +1545,7 @@ int score_step(score_ctx* c, score_step_stats* out) {
     if (!c->loaded) return c->fail(SCORE_ERR_STATE, "no domain loaded");
     if (c->failed) return SCORE_ERR_STATE;  // a device error left the front lists undefined
     c->running = true;
-    const int s = c->eng->step(true);
+    const int s = c->eng->step(c->eng->sample_step());
     c->running = false;
     if (s != SCORE_OK) { if (c->err.empty()) c->err = c->eng->err; return s; }
     if (out) *out = c->last;

@@ -126,3 +126,20 @@ def test_batch_autotune_and_fp32(gpu, tmp_path):
             x64 = ref["trace"]["X"]
             m = min(len(x32), len(x64))
             assert np.max(np.abs(x32[:m] - x64[:m])) < 5e-3
+
+
+def test_phase_timing_is_sampled(gpu, tmp_path):
+    """Phase events on every k-th step only; results do not depend on it."""
+    p, d, g = load_case("base", tmp_path)
+    nsteps = len(g["t"])
+    with sg.GrowthMachine(p) as gm:
+        gm.load_domain(d)
+        for every, expect in ((1, nsteps), (0, 0), (8, (nsteps + 7) // 8)):
+            gm.set_tune(timing_every=every)
+            gm.restart()
+            gm.place_nuclei()
+            tr = gm.run_until()
+            t = gm.timing()
+            assert t.grow_launches == nsteps and t.timed_steps == expect, (every, t.timed_steps)
+            assert (t.fill_ms > 0) == (expect > 0) and t.fill_ms <= t.grow_ms
+            assert_trace(tr, g, f"timing_every={every}")
