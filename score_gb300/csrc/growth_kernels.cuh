@@ -971,9 +971,12 @@ __global__ void __launch_bounds__(kBlock, 3) k_commit(int base, int ndom) {
         const uint32_t unit = ONE ? u : u - s_pre[s];
         const uint32_t F0 = a.st->nfull[0], F = F0 + a.st->nfull[1];
         const uint32_t f = unit * 32u + (uint32_t)lane;
+        // the unit's own loads first, then its prefix: their latencies overlap
+        const int L = f >= F0 ? 1 : 0;
+        const uint32_t win = f < F ? a.amask[f] : 0u, tob = f < F ? a.tobm[f] : 0u;
+        const uint32_t slot = f < F ? a.f[L].full[L ? f - F0 : f] : 0u;
         uint32_t pa, pb;
         tile_prefix(a.ctcnt, a.csct, unit, pa, pb);
-        const uint32_t win = f < F ? a.amask[f] : 0u, tob = f < F ? a.tobm[f] : 0u;
         const uint32_t cB = __popc(tob), cA = __popc(win) - cB, cW = cA + cB;
         uint32_t iA = cA, iB = cB, iW = cW;
 #pragma unroll
@@ -989,11 +992,9 @@ __global__ void __launch_bounds__(kBlock, 3) k_commit(int base, int ndom) {
             a.st->nwin[1] = pb + iB;
         }
         // the lane's own full cell
-        const int L = f >= F0 ? 1 : 0;
-        uint32_t slot = 0, cell = 0, rsrc = 0, gsrc = 0;
+        uint32_t cell = 0, rsrc = 0, gsrc = 0;
         double over = 0.0;
         if (f < F) {
-            slot = a.f[L].full[L ? f - F0 : f];
             cell = a.f[L].xyz[slot];
             rsrc = a.f[L].rxg[slot];
             gsrc = a.f[L].defg[slot];
