@@ -75,6 +75,68 @@ __global__ void k_place_nuclei(DomainArgs a, const NucRec* rec, uint32_t n) {
     }
 }
 
+// Nuclei due during the run, placed on the device so that the host needs no round trip:
+// candidates in rxg order with the deformed grain of their site and P (computed by the
+// host from the loaded grid: a site that is still deformed has its loaded grain).  A
+// candidate is placed when its site is still deformed and no earlier candidate of the
+// batch has the same site, exactly as the host placement decides; placed nuclei take
+// the next slots of their list in candidate order.
+struct NucDue { uint32_t site, rxg, defg, list; double P; };
+constexpr uint32_t kDueMax = 1024;  // candidates per launch (one block)
+
+template <bool FP32>
+__global__ void __launch_bounds__(kDueMax) k_place_due(DomainArgs a, const NucDue* rec, uint32_t n) {
+    __shared__ uint32_t s_site[kDueMax];
+    __shared__ uint32_t s_wc[2][kDueMax / 32];
+    __shared__ uint32_t s_base[2];
+    const uint32_t i = threadIdx.x;
+    const int warp = (int)(i >> 5), lane = (int)(i & 31);
+    NucDue r{};
+    if (i < n) { r = rec[i]; s_site[i] = r.site; }
+    if (i == 0) { s_base[0] = a.st->next_never[0]; s_base[1] = a.st->next_never[1]; }
+    __syncthreads();
+    bool ok = false;
+    if (i < n && r.site < a.ncells && r.list < 2) {
+        ok = a.grid[r.site] < a.ndefg;
+        for (uint32_t j = 0; j < i && ok; ++j) if (s_site[j] == r.site) ok = false;
+    }
+    const uint32_t b0 = __ballot_sync(0xFFFFFFFFu, ok && r.list == 0), b1 = __ballot_sync(0xFFFFFFFFu, ok && r.list == 1);
+    if (lane == 0) { s_wc[0][warp] = __popc(b0); s_wc[1][warp] = __popc(b1); }
+    __syncthreads();
+    const int L = r.list == 1 ? 1 : 0;
+    uint32_t rank = __popc((L ? b1 : b0) & lanemask_lt());
+    for (int w = 0; w < warp; ++w) rank += s_wc[L][w];
+    if (ok) {
+        const uint32_t slot = s_base[L] + rank;
+        const DFront& f = a.f[L];
+        if (slot >= f.cap) {
+            atomicOr(&a.st->err, kErrCapacity);
+        } else if (L == 1 && a.border_policy == 0 && slot >= a.border_ref_cap) {
+            atomicOr(&a.st->err, kErrBorderRef);
+        } else {
+            const double mo = mobility(a, r.P);
+            const double v = velocity_from_mobility(a, mo, r.defg, 26);
+            f.mob[slot] = mo;
+            if (!FP32) { ((double*)f.fill)[slot] = 1.0; ((double*)f.vel)[slot] = v; }
+            else { ((float*)f.fill)[slot] = 1.0f; f.comp[slot] = 0.0f; ((float*)f.vel)[slot] = (float)v; }
+            f.dir[slot] = 26 | kStale;
+            f.defg[slot] = r.defg;
+            f.rxg[slot] = r.rxg;
+            f.xyz[slot] = r.site;
+            a.grid[r.site] = kCurrentlyInfected;
+            a.ptab[(unsigned long long)r.rxg * a.ndefg + r.defg] = (unsigned long long)__double_as_longlong(r.P);
+            if (r.P >= 0.0) atomicMax(&a.st->pmax_bits, (unsigned long long)__double_as_longlong(r.P));
+        }
+    }
+    if (i == 0) {
+        uint32_t t0 = 0, t1 = 0;
+        for (int w = 0; w < (int)(kDueMax / 32); ++w) { t0 += s_wc[0][w]; t1 += s_wc[1][w]; }
+        a.st->next_never[0] = s_base[0] + t0;
+        a.st->next_never[1] = s_base[1] + t1;
+        a.st->nnuc += t0 + t1;
+    }
+}
+
 __global__ void k_fill_ptab(unsigned long long* ptab, const unsigned long long* idx, const double* val, uint32_t n) {
     for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
         ptab[idx[i]] = (unsigned long long)__double_as_longlong(val[i]);
@@ -207,6 +269,7 @@ struct score_ctx {
     int refresh = 0;                   // next step: 1 full refresh from P, 2 from cached mobilities
     std::vector<double> defg_q, rxg_q, rho0, rho, tincub;
     std::vector<uint32_t> site;
+    std::vector<uint32_t> site_defg;   // deformed grain of each nucleus site in the loaded grid
     std::vector<uint8_t> placed;
     std::vector<uint32_t> nuc_order;   // rxg ids sorted by (tincub, id)
     size_t nuc_pos = 0;                // nuc_order[0, nuc_pos) already considered
@@ -229,6 +292,8 @@ struct score_ctx {
     HostBox* d_box = nullptr;          // its device address
     double* d_pforce = nullptr;
     double* h_pforce = nullptr;            // pinned staging of the driving forces
+    NucDue* h_due = nullptr;               // pinned staging of nuclei due during the run
+    NucDue* d_due = nullptr;
     uint32_t* d_grid_init = nullptr;       // the loaded deformed grid (restart source)
     double* d_rxq = nullptr;               // orientation quaternions on the device
     double* d_dfq = nullptr;
@@ -279,11 +344,13 @@ void score_ctx::release_domain() {
                     a.grid, a.claim, a.amask, a.ptab, a.defg_cnt, a.rxg_cnt, a.depleted, a.miss, a.tobm, a.ctcnt,
                     a.f[0].fmask, a.f[0].imask, a.f[0].tcnt, a.f[1].fmask, a.f[1].imask, a.f[1].tcnt,
                     a.f[0].scnt, a.f[1].scnt, a.csct,
-                    d_state, d_pforce, d_u32tmp, d_stage, d_grid_init, d_defg_cnt_init, d_rxq, d_dfq,
+                    d_state, d_pforce, d_u32tmp, d_stage, d_grid_init, d_defg_cnt_init, d_rxq, d_dfq, d_due,
                     scratch.fill, scratch.comp, scratch.vel, scratch.defg, scratch.rxg, scratch.xyz, scratch.dir};
     for (void* p : ptrs) if (p) cudaFree(p);
     if (h_pforce) cudaFreeHost(h_pforce);
     h_pforce = nullptr;
+    if (h_due) cudaFreeHost(h_due);
+    h_due = nullptr; d_due = nullptr;
     a = DomainArgs{};
     scratch = DFront{};
     d_state = nullptr; d_pforce = nullptr; d_u32tmp = nullptr; d_stage = nullptr;
@@ -600,13 +667,34 @@ int check_device_errors(score_ctx* c, uint32_t flags) {
 
 // site-saturated placement of nuclei with tincub <= t, rxg order
 // (ompshar_sim_myCA_sitesaturatedNucleation / infect_JuvenileNucleation, SCORE_GrowthMachine.cpp:50-189)
-int place_nuclei_upto(score_ctx* c, double tnow, uint32_t* nplaced) {
+// With `on_device`, up to kDueMax candidates are placed by k_place_due in stream order
+// before the step (no host round trip); the placed count, the slots and the P max reach
+// the host in the step's mailbox.  Otherwise the host reads the site values, decides and
+// uploads the nuclei (two synchronizations).
+int place_nuclei_upto(score_ctx* c, double tnow, uint32_t* nplaced, bool on_device) {
     std::vector<uint32_t> cand;
     while (c->nuc_pos < c->nuc_order.size() && c->tincub[c->nuc_order[c->nuc_pos]] <= tnow) cand.push_back(c->nuc_order[c->nuc_pos++]);
     std::sort(cand.begin(), cand.end());  // the reference places nuclei in rxg order
     if (nplaced) *nplaced = 0;
     if (cand.empty()) return SCORE_OK;
     const uint32_t n = (uint32_t)cand.size();
+    if (on_device && n <= kDueMax) {
+        const uint32_t nx = c->nx, ny = c->ny, nxy = nx * ny;
+        for (uint32_t i = 0; i < n; ++i) {
+            const uint32_t r = cand[i], s = c->site[r], g = c->site_defg[r];
+            const uint32_t z = s / nxy, y = (s - z * nxy) / nx, x = s - z * nxy - y * nx;
+            const bool inside = x > 0 && x < nx - 1 && y > 0 && y < ny - 1 && z > 0 && z < c->nz - 1;
+            c->placed[r] = 1;
+            c->h_due[i] = NucDue{s, r, g, inside ? 0u : 1u, weight_of(c, r, g)};
+        }
+        const cudaError_t e = cudaMemcpyAsync(c->d_due, c->h_due, (size_t)n * sizeof(NucDue), cudaMemcpyHostToDevice, c->stream);
+        if (e != cudaSuccess) return c->cuda_fail(e, "upload due nuclei");
+        set_step_args(c);
+        if (c->fp32) k_place_due<true><<<1, kDueMax, 0, c->stream>>>(c->a, c->d_due, n);
+        else k_place_due<false><<<1, kDueMax, 0, c->stream>>>(c->a, c->d_due, n);
+        c->launches++;
+        return SCORE_OK;
+    }
     std::vector<uint32_t> sites(n), gval(n);
     for (uint32_t i = 0; i < n; ++i) sites[i] = c->site[cand[i]];
     if (!c->stage((size_t)n * 8)) return c->fail(SCORE_ERR_NOMEM, "staging buffer");
@@ -810,10 +898,13 @@ namespace {
 // argument block of this step.
 int pre_step(score_ctx* c, uint32_t* newnuc) {
     Physics& ph = c->ph;
-    int s = place_nuclei_upto(c, ph.t, newnuc);  // time-dependent nucleation (no-op when site-saturated)
-    if (s != SCORE_OK) return s;
     // on-the-fly defragmentation at user X logpoints (SCORE_Kernel.cpp:6625-6630, thresholds in cells)
-    if (c->prm.defragmentation && c->defrag_cnt < c->prm.n_defrag && c->Xcells >= c->prm.defrag_x[c->defrag_cnt] * (double)c->N) {
+    const bool defrag = c->prm.defragmentation && c->defrag_cnt < c->prm.n_defrag && c->Xcells >= c->prm.defrag_x[c->defrag_cnt] * (double)c->N;
+    // time-dependent nucleation (no-op when site-saturated); on the device unless the host
+    // defragments this step (it needs the slot counts on the host)
+    int s = place_nuclei_upto(c, ph.t, newnuc, !defrag);
+    if (s != SCORE_OK) return s;
+    if (defrag) {
         for (int L = 0; L < 2; ++L) { s = defragment(c, L); if (s != SCORE_OK) return s; }
         c->defrag_cnt++;
     }
@@ -863,6 +954,8 @@ int post_step(score_ctx* c, uint32_t newnuc, score_step_stats* out) {
     const DevState hs = c->h_box->snap;
     if (hs.err) { c->failed = true; return check_device_errors(c, hs.err); }
     const uint64_t Sv = hs.sv[0] + hs.sv[1], nfull = (uint64_t)hs.nfull[0] + hs.nfull[1], nnew = (uint64_t)hs.nwin[0] + hs.nwin[1];
+    newnuc += hs.nnuc;  // nuclei the device placed before the grow
+    c->n_nuclei += hs.nnuc;
 
     // mobility weights requested this step: computed on the host (FP64, libm)
     double pmax_new = 0.0;
@@ -1415,6 +1508,8 @@ int score_load_domain(score_ctx* c, const uint32_t* grid, const double* defg_qua
     c->rxg_q.assign(rxg_quat, rxg_quat + 4 * (size_t)nrxg);
     c->rho0.assign(defg_rho0, defg_rho0 + ndefg);
     c->site.assign(rxg_site, rxg_site + nrxg);
+    c->site_defg.resize(nrxg);
+    for (uint32_t r = 0; r < nrxg; ++r) c->site_defg[r] = grid[rxg_site[r]];
     c->tincub.assign(nrxg, 0.0);
     if (rxg_tincub) c->tincub.assign(rxg_tincub, rxg_tincub + nrxg);
     c->rho_order.resize(ndefg);
@@ -1488,6 +1583,8 @@ int score_load_domain(score_ctx* c, const uint32_t* grid, const double* defg_qua
         if (e == cudaSuccess) e = dalloc(&c->d_state, 1);
         if (e == cudaSuccess) e = dalloc(&c->d_pforce, ndefg);
         if (e == cudaSuccess) e = cudaMallocHost((void**)&c->h_pforce, std::max<size_t>(ndefg, 1) * 8);
+        if (e == cudaSuccess) e = cudaMallocHost((void**)&c->h_due, kDueMax * sizeof(NucDue));
+        if (e == cudaSuccess) e = dalloc(&c->d_due, kDueMax);
         if (e == cudaSuccess) e = dalloc(&c->d_u32tmp, 64);
         if (e == cudaSuccess) e = dalloc(&c->d_rxq, 4 * (size_t)nrxg);
         if (e == cudaSuccess) e = dalloc(&c->d_dfq, 4 * (size_t)ndefg);
@@ -1537,7 +1634,7 @@ int score_place_nuclei(score_ctx* c, uint32_t* n_placed) {
     if (!c->loaded) return c->fail(SCORE_ERR_STATE, "no domain loaded");
     if (c->failed) return SCORE_ERR_STATE;
     cudaSetDevice(c->device);
-    return place_nuclei_upto(c, c->ph.t, n_placed);
+    return place_nuclei_upto(c, c->ph.t, n_placed, false);
 }
 
 int score_step(score_ctx* c, score_step_stats* out) {

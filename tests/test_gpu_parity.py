@@ -13,7 +13,7 @@ import score_gb300 as sg
 
 pytestmark = pytest.mark.gpu
 
-FIELDS_EXACT = ["Xcells", "Sv", "n_full", "n_new", "t", "dt", "dt_used", "Pmax", "rhomax"]
+FIELDS_EXACT = ["Xcells", "Sv", "n_full", "n_new", "t", "dt", "dt_used", "Pmax", "rhomax", "n_nuclei"]
 
 
 def run_gpu(p, d, ptable=None, x_target=-1.0):
@@ -85,6 +85,25 @@ def test_fp64_incubation_times(gpu, tmp_uds):
     d = sg.generate_domain(64, 64, 64, 50, 60, seed=16, nucleation_rate=3000.0)
     assert d.rxg_tincub.max() > 0
     compare(sg.read_uds(tmp_uds(sg.UdsSpec(nx=64, ny=64, nz=64))), d)
+
+
+def test_fp64_incubation_repeated_and_face_sites(gpu, tmp_uds):
+    """Nuclei due during the run are placed on the device: repeated sites (the later nucleus
+    is not placed), sites on the faces (Border list), and steps that defragment (placed by
+    the host) must all give the oracle's slots, counts and labels."""
+    d = sg.generate_domain(64, 64, 64, 50, 400, seed=21, nucleation_rate=2000.0)
+    site = d.rxg_site.copy()
+    site[1::7] = site[0::7][: len(site[1::7])]
+    k = np.arange(0, len(site), 11)
+    x, y, z = site[k] % 64, (site[k] // 64) % 64, site[k] // 4096
+    x[::2] = 0
+    z[1::2] = 63
+    site[k] = (z * 64 + y) * 64 + x
+    d2 = sg.Domain(d.nx, d.ny, d.nz, d.grid, d.defg_quat, d.defg_rho0, d.rxg_quat, site.astype(np.uint32), d.rxg_tincub)
+    (tr, *_), _ = compare(sg.read_uds(tmp_uds(sg.UdsSpec(nx=64, ny=64, nz=64))), d2)
+    assert sum(s.n_nuclei for s in tr) < len(site)  # some were not placeable
+    spec = sg.UdsSpec(nx=64, ny=64, nz=64, defragmentation=1, defrag_x=["0.1", "0.3", "0.6"])
+    compare(sg.read_uds(tmp_uds(spec)), d2)
 
 
 def test_fp64_recovery_refreshes_velocities(gpu, tmp_uds):
