@@ -483,10 +483,12 @@ struct Engine {
     bool use_graph = true;
     bool capturing = false;
     bool events = false;               // the sequence being launched records the phase events
-    cudaGraphExec_t gexec[2] = {nullptr, nullptr};  // the step without / with phase events
-    TuneCfg gcfg[2];
-    int gndom[2] = {-1, -1};
-    bool gfp32[2] = {false, false};
+    bool r2 = false;                   // ... and every stepping domain refreshes from cached mobilities
+    // the step without / with phase events, with the general / the refresh-only grow kernel
+    cudaGraphExec_t gexec[4] = {nullptr, nullptr, nullptr, nullptr};
+    TuneCfg gcfg[4];
+    int gndom[4] = {-1, -1, -1, -1};
+    bool gfp32[4] = {false, false, false, false};
     uint64_t run_steps = 0;            // steps since the run started (phase sampling)
     // 0 start, 1 end of fill, 2 end of lists, 3 end of claim, 4 end of step, 5/6 run span
     cudaEvent_t ev[7] = {nullptr, nullptr, nullptr, nullptr, nullptr, nullptr, nullptr};
@@ -520,7 +522,7 @@ struct Engine {
         return e == cudaSuccess ? SCORE_OK : SCORE_ERR_CUDA;
     }
     void drop_graph() {
-        for (int k = 0; k < 2; ++k) {
+        for (int k = 0; k < 4; ++k) {
             if (gexec[k]) cudaGraphExecDestroy(gexec[k]);
             gexec[k] = nullptr;
             gndom[k] = -1;
@@ -543,7 +545,7 @@ struct Engine {
     }
     int fail(int code, const std::string& m) { err = m; return code; }
     void launch_sequence(int n);
-    cudaError_t enqueue_step(int n, bool timed);
+    cudaError_t enqueue_step(int n, bool timed, bool refresh_only);
     int step(bool timed);
     int run_until(double x_target, uint32_t max_steps, uint32_t* steps_done);
     int autotune(double x_target, uint32_t max_steps, score_tune* out);
@@ -1059,8 +1061,14 @@ inline void record(const Engine& E, int k) {
 
 template <bool FP32, int ITEMS>
 void launch_grow(const Engine& E, int n) {
-    if (n == 1) k_grow_fill<FP32, ITEMS, true><<<(uint32_t)(E.sms * E.cfg.fill_bpsm), kBlock, 0, E.stream>>>(E.base, n);
-    else k_grow_fill<FP32, ITEMS, false><<<(uint32_t)(E.sms * E.cfg.fill_bpsm), kBlock, 0, E.stream>>>(E.base, n);
+    const uint32_t g = (uint32_t)(E.sms * E.cfg.fill_bpsm);
+    if (E.r2) {
+        if (n == 1) k_grow_fill<FP32, ITEMS, true, true><<<g, kBlock, 0, E.stream>>>(E.base, n);
+        else k_grow_fill<FP32, ITEMS, false, true><<<g, kBlock, 0, E.stream>>>(E.base, n);
+    } else {
+        if (n == 1) k_grow_fill<FP32, ITEMS, true, false><<<g, kBlock, 0, E.stream>>>(E.base, n);
+        else k_grow_fill<FP32, ITEMS, false, false><<<g, kBlock, 0, E.stream>>>(E.base, n);
+    }
     record(E, 1);
     k_grow_lists<ITEMS><<<(uint32_t)E.sms * 8, kBlock, 0, E.stream>>>(E.base, n);
 }
@@ -1099,7 +1107,7 @@ void Engine::launch_sequence(int n) {
 }
 
 // the argument copy and the kernels of one step, as a graph replay or direct launches
-cudaError_t Engine::enqueue_step(int n, bool timed) {
+cudaError_t Engine::enqueue_step(int n, bool timed, bool refresh_only) {
     // the argument blocks only change when dt, the physics or a domain's state changes
     cudaError_t e = cudaSuccess;
     if (args_dirty || memcmp(h_args, h_args_dev.data(), (size_t)n * sizeof(DomainArgs)) != 0) {
@@ -1109,12 +1117,13 @@ cudaError_t Engine::enqueue_step(int n, bool timed) {
     }
     if (e != cudaSuccess) return e;
     events = timed;
+    r2 = refresh_only;
     if (!use_graph) {
         launch_sequence(n);
         launches += kStepKernels;
         return cudaGetLastError();
     }
-    const int k = timed ? 1 : 0;
+    const int k = (timed ? 1 : 0) + (refresh_only ? 2 : 0);
     if (!gexec[k] || gndom[k] != n || !(gcfg[k] == cfg) || gfp32[k] != fp32) {
         if (gexec[k]) cudaGraphExecDestroy(gexec[k]);
         gexec[k] = nullptr;
@@ -1190,7 +1199,9 @@ int Engine::step(bool timed) {
     if (nrun == 0) return SCORE_OK;
     const auto pre_t1 = std::chrono::steady_clock::now();
     tm.pre_ms += std::chrono::duration<double, std::milli>(pre_t1 - host_t0).count();
-    cudaError_t e = enqueue_step(n, timed);
+    bool r2all = true;  // every stepping domain refreshes from its cached mobilities
+    for (int i = 0; i < n; ++i) if (dom[i]->running && h_args[i].refresh != 2) r2all = false;
+    cudaError_t e = enqueue_step(n, timed, r2all);
     ++run_steps;
     // while the GPU steps: each domain's outcome-independent physics for the next step
     std::vector<int> status(n, SCORE_OK);

@@ -301,7 +301,8 @@ __device__ __forceinline__ void tile_prefix(const uint32_t* cnt, const uint32_t*
 // (only rho or the drag changed the driving force), no table gather; REFRESH 3: as 0 with
 // dt unchanged, the slot's cached increment and fill loaded together with its infector
 // byte, for every slot below the high-water mark (one memory round trip instead of two,
-// at the price of reading the fill data of INACTIVE slots too).
+// at the price of reading the fill data of INACTIVE slots too); REFRESH 4: REFRESH 2 with
+// the same early loads (cached mobility, grain and fill).
 // A cell created last step whose weight the host computed: P = answer `tag`; the table
 // entry (tagged until now) gets the value for later lookups.
 __device__ __forceinline__ double answered_velocity(const DomainArgs& a, const DFront& fr, uint32_t slot, uint8_t dir,
@@ -354,6 +355,35 @@ __device__ __forceinline__ uint32_t grow_tile(const DomainArgs& a, int L, uint32
                     }
                 }
             }
+        } else if (REFRESH == 4) {
+            // in two halves of the items: the early loads of all of them do not fit the registers
+            constexpr int H = ITEMS / 2;
+#pragma unroll
+            for (int h = 0; h < 2; ++h) {
+                double mo[H];
+                uint32_t g[H];
+#pragma unroll
+                for (int j = 0; j < H; ++j) {
+                    const int k = h * H + j;
+                    const uint32_t slot = base + (uint32_t)(k * 32);
+                    w[k] = -1.0; fill[k] = 0.0; mo[j] = 0.0; g[j] = 0;
+                    if (slot < n) {
+                        mo[j] = fr.mob[slot];
+                        g[j] = fr.defg[slot];
+                        fill[k] = ((const double*)fr.fill)[slot];
+                    }
+                }
+#pragma unroll
+                for (int j = 0; j < H; ++j) {
+                    const int k = h * H + j;
+                    const uint32_t slot = base + (uint32_t)(k * 32);
+                    if (d[k] != kInactive) {
+                        if (d[k] & kPend) w[k] = answered_velocity(a, fr, slot, d[k], ((const unsigned long long*)fr.vel)[slot]);
+                        else w[k] = velocity_from_mobility(a, mo[j], g[j], d[k] & kCodeMask);
+                        ((double*)fr.vel)[slot] = w[k];
+                    }
+                }
+            }
         } else {
 #pragma unroll
         for (int k = 0; k < ITEMS; ++k) {
@@ -389,7 +419,7 @@ __device__ __forceinline__ uint32_t grow_tile(const DomainArgs& a, int L, uint32
                 ++sv;
                 const uint32_t slot = base + (uint32_t)(k * 32);
                 double inc = w[k];
-                if (REFRESH == 1 || REFRESH == 2 || (REFRESH == 0 && a.dt_changed) || (d[k] & kStale)) {
+                if (REFRESH == 1 || REFRESH == 2 || REFRESH == 4 || (REFRESH == 0 && a.dt_changed) || (d[k] & kStale)) {
                     if (__double_as_longlong(w[k]) >= 0) inc = __dmul_rn(__dmul_rn(w[k], a.dt), a.cinv);
                     fr.inc[slot] = inc;
                     if (d[k] & kStale) fr.dir[slot] = d[k] & kCodeMask;
@@ -420,6 +450,35 @@ __device__ __forceinline__ uint32_t grow_tile(const DomainArgs& a, int L, uint32
                 if (d[k] != kInactive && (d[k] & kPend)) {
                     vel[k] = (float)answered_velocity(a, fr, slot, d[k], ((const uint32_t*)fr.vel)[slot]);
                     ((float*)fr.vel)[slot] = vel[k];
+                }
+            }
+        } else if (REFRESH == 4) {
+            constexpr int H = ITEMS / 2;
+#pragma unroll
+            for (int h = 0; h < 2; ++h) {
+                double mo[H];
+                uint32_t g[H];
+#pragma unroll
+                for (int j = 0; j < H; ++j) {
+                    const int k = h * H + j;
+                    const uint32_t slot = base + (uint32_t)(k * 32);
+                    vel[k] = -1.0f; fill[k] = 0.0f; comp[k] = 0.0f; mo[j] = 0.0; g[j] = 0;
+                    if (slot < n) {
+                        mo[j] = fr.mob[slot];
+                        g[j] = fr.defg[slot];
+                        fill[k] = ((const float*)fr.fill)[slot];
+                        comp[k] = fr.comp[slot];
+                    }
+                }
+#pragma unroll
+                for (int j = 0; j < H; ++j) {
+                    const int k = h * H + j;
+                    const uint32_t slot = base + (uint32_t)(k * 32);
+                    if (d[k] != kInactive) {
+                        if (d[k] & kPend) vel[k] = (float)answered_velocity(a, fr, slot, d[k], ((const uint32_t*)fr.vel)[slot]);
+                        else vel[k] = (float)velocity_from_mobility(a, mo[j], g[j], d[k] & kCodeMask);
+                        ((float*)fr.vel)[slot] = vel[k];
+                    }
                 }
             }
         } else {
@@ -504,7 +563,9 @@ __device__ __forceinline__ uint32_t list_slots(const DomainArgs& a, int L) { ret
 
 // ONE: a single domain (the plain path): its argument block sits at a launch-uniform
 // slot and the two lists are walked in turn, so every argument read is uniform.
-template <bool FP32, int ITEMS, bool ONE>
+// R2: every stepping domain refreshes from cached mobilities (REFRESH 2, recovery); a
+// kernel of its own, so that its register-hungry early loads cost the other modes nothing.
+template <bool FP32, int ITEMS, bool ONE, bool R2>
 __global__ void __launch_bounds__(kBlock, ITEMS >= 16 ? 2 : 4) k_grow_fill(int base, int ndom) {
     using S = GrowShape<ITEMS>;
     __shared__ uint32_t s_pre[kMaxSegs + 1];
@@ -516,7 +577,13 @@ __global__ void __launch_bounds__(kBlock, ITEMS >= 16 ? 2 : 4) k_grow_fill(int b
             const uint32_t n = a.st->next_never[L];
             const uint32_t ntiles = (n + S::kTile - 1) / S::kTile;
             uint32_t sv = 0;
-            if (a.refresh == 1) {
+            if (R2) {
+                if (a.spec) {
+                    for (uint32_t tile = blockIdx.x; tile < ntiles; tile += gridDim.x) sv += grow_tile<FP32, 4, ITEMS>(a, L, tile, n);
+                } else {
+                    for (uint32_t tile = blockIdx.x; tile < ntiles; tile += gridDim.x) sv += grow_tile<FP32, 2, ITEMS>(a, L, tile, n);
+                }
+            } else if (a.refresh == 1) {
                 for (uint32_t tile = blockIdx.x; tile < ntiles; tile += gridDim.x) sv += grow_tile<FP32, 1, ITEMS>(a, L, tile, n);
             } else if (a.refresh == 2) {
                 for (uint32_t tile = blockIdx.x; tile < ntiles; tile += gridDim.x) sv += grow_tile<FP32, 2, ITEMS>(a, L, tile, n);
@@ -546,7 +613,10 @@ __global__ void __launch_bounds__(kBlock, ITEMS >= 16 ? 2 : 4) k_grow_fill(int b
         const int L = s & 1;
         const uint32_t tile = u - s_pre[s];
         const uint32_t n = a.st->next_never[L];
-        if (a.refresh == 1) sv += grow_tile<FP32, 1, ITEMS>(a, L, tile, n);
+        if (R2) {
+            if (a.spec) sv += grow_tile<FP32, 4, ITEMS>(a, L, tile, n);
+            else sv += grow_tile<FP32, 2, ITEMS>(a, L, tile, n);
+        } else if (a.refresh == 1) sv += grow_tile<FP32, 1, ITEMS>(a, L, tile, n);
         else if (a.refresh == 2) sv += grow_tile<FP32, 2, ITEMS>(a, L, tile, n);
         else if (a.spec && !a.dt_changed) sv += grow_tile<FP32, 3, ITEMS>(a, L, tile, n);
         else sv += grow_tile<FP32, 0, ITEMS>(a, L, tile, n);
