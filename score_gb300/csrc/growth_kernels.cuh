@@ -275,11 +275,22 @@ constexpr uint32_t kSuper = 64;  // tiles per supertile of the two-level tile pr
 // sup: per-supertile pairs) count array, computed by one warp; every lane returns both.
 __device__ __forceinline__ void tile_prefix(const uint32_t* cnt, const uint32_t* sup, uint32_t tile, uint32_t& pa, uint32_t& pb,
                                             uint32_t per = 1) {
-    const int lane = threadIdx.x & 31;
-    const uint32_t s = tile / kSuper;
+    // the supertile sums [0, s) then the count pairs [s kSuper per, tile per), as one
+    // index range of 8-byte loads with four in flight per lane before any add waits
+    const uint32_t s = tile / kSuper, lo = s * kSuper * per, n = s + (tile * per - lo);
+    const uint2* ps = (const uint2*)sup;
+    const uint2* pc = (const uint2*)cnt + lo - s;
     uint32_t a = 0, b = 0;
-    for (uint32_t i = lane; i < s; i += 32) { a += sup[2 * i]; b += sup[2 * i + 1]; }
-    for (uint32_t i = s * kSuper * per + lane; i < tile * per; i += 32) { a += cnt[2 * i]; b += cnt[2 * i + 1]; }
+    for (uint32_t i = threadIdx.x & 31; i < n; i += 128) {
+        uint2 x[4];
+#pragma unroll
+        for (int k = 0; k < 4; ++k) {
+            const uint32_t j = i + 32u * k;
+            x[k] = j < n ? (j < s ? ps[j] : pc[j]) : make_uint2(0u, 0u);
+        }
+#pragma unroll
+        for (int k = 0; k < 4; ++k) { a += x[k].x; b += x[k].y; }
+    }
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) {
         a += __shfl_xor_sync(0xFFFFFFFFu, a, o);
