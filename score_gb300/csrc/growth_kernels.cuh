@@ -791,7 +791,7 @@ __device__ __forceinline__ uint32_t full_cells(const DomainArgs& a) {
 }
 
 template <bool ONE>
-__global__ void __launch_bounds__(kBlock, 4) k_claim(int base, int ndom) {
+__global__ void __launch_bounds__(kBlock, 2) k_claim(int base, int ndom) {
     __shared__ uint32_t s_pre[kMaxSegs + 1], s_cnt[kMaxSegs];
     auto count = [&](int s) {
         const DomainArgs& a = c_args[base + (s)];
@@ -815,10 +815,24 @@ __global__ void __launch_bounds__(kBlock, 4) k_claim(int base, int ndom) {
         const uint32_t F0 = a.st->nfull[0];
         uint32_t mask;
         if (f < F0) {
+            // an Inside cell: all 26 grid reads in flight before the first claim
             const uint32_t cell = a.f[0].xyz[a.f[0].full[f]];
-            mask = claim_plane<0, 8, true>(a, cell, 0, 0, 0, f);
-            mask |= claim_plane<8, 17, true>(a, cell, 0, 0, 0, f);
-            mask |= claim_plane<17, 26, true>(a, cell, 0, 0, 0, f);
+            uint32_t gv[26];
+#pragma unroll
+            for (int d = 0; d < 26; ++d) {
+                const uint32_t t = cell + (uint32_t)a.noff[d];
+                gv[d] = t < a.ncells ? a.grid[t] : 0xFFFFFFFFu;
+            }
+            mask = 0;
+#pragma unroll
+            for (int d = 0; d < 26; ++d) {
+                const uint32_t t = cell + (uint32_t)a.noff[d];
+                if (t >= a.ncells) atomicOr(&a.st->err, kErrBounds);
+                else if (gv[d] < a.ndefg) {
+                    atomicMin(&a.claim[t], f * 26u + (uint32_t)d);
+                    mask |= 1u << d;
+                }
+            }
         } else {
             const uint32_t cell = a.f[1].xyz[a.f[1].full[f - F0]];
             int x, y, z;
