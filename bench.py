@@ -507,8 +507,8 @@ def main():
         barrier(dist)
         e_s = reduce_max(dist, e_s)
         e_value = reduce_sum(dist, float(e_sv)) / e_s
-    fp32_err = wl.fp32_error() if args.precision == 1 else None
     every = wl.timing_every()
+    fp32_err = wl.fp32_error() if args.precision == 1 else None
     wl.close()
 
     if rank == 0:
