@@ -1576,14 +1576,14 @@ int score_load_domain(score_ctx* c, const uint32_t* grid, const double* defg_qua
             if (e == cudaSuccess) e = dalloc(&f.tcnt, 2 * tiles * kWarps);
             if (e == cudaSuccess) e = dalloc(&f.scnt, c->scnt_words[L]);
         }
-        c->csct_words = 2 * ((N / 32 + 2) / kSuper + 2);
+        c->csct_words = 2 * ((N / kBlock + 2) / kSuper + 2);
         a.misscap = (uint32_t)std::min<uint64_t>(N, 1ull << 25);
         if (e == cudaSuccess) e = dalloc(&a.grid, N);
         if (e == cudaSuccess) e = dalloc(&c->d_grid_init, N);
         if (e == cudaSuccess) e = dalloc(&a.claim, N);
         if (e == cudaSuccess) e = dalloc(&a.amask, N);
         if (e == cudaSuccess) e = dalloc(&a.tobm, N);
-        if (e == cudaSuccess) e = dalloc(&a.ctcnt, 2 * (N / 32 + 2));
+        if (e == cudaSuccess) e = dalloc(&a.ctcnt, 2 * (N / kBlock + 2));
         if (e == cudaSuccess) e = dalloc(&a.csct, c->csct_words);
         if (e == cudaSuccess) e = dalloc(&a.ptab, ptab_words);
         if (e == cudaSuccess) e = dalloc(&a.defg_cnt, ndefg);

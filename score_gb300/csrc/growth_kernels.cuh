@@ -89,8 +89,8 @@ struct DomainArgs {
     uint32_t* claim;
     uint32_t* amask;            // per full cell: attempts made (bit d), then attempts won
     uint32_t* tobm;             // per full cell: won attempts that go to the Border list
-    uint32_t* ctcnt;            // per commit unit of 32 full cells: (Inside, Border) win counts
-    uint32_t* csct;             // per supertile of kSuper commit units: the same counts (zero between steps)
+    uint32_t* ctcnt;            // per commit tile: (Inside, Border) win counts
+    uint32_t* csct;             // per supertile of kSuper commit tiles: the same counts (zero between steps)
     unsigned long long* ptab;   // nrxg x ndefg mobility weights as bits (kPtabEmpty = unknown)
     const double* pforce;       // per deformed grain driving force (FP64)
     uint32_t* defg_cnt;
@@ -959,31 +959,28 @@ __device__ __forceinline__ bool lookup_p(const DomainArgs& a, uint32_t rxg, uint
 }
 
 // ------------------------------------------------------------------ K3 commit (+ finalize)
-// Both kernels work in units of 32 consecutive full cells, one warp per unit, and no
-// warp waits for another one (no block barrier).
-// k_resolve: a full cell's attempts whose claim holds the own ordinal won; writes the
-// win mask, the mask of wins that go to the Border list, the unit's two win counts and
-// adds them to its supertile of kSuper units.
-// k_commit: winners are ranked per destination list in full-cell then direction order
-// (the unit's prefix from the supertile and unit counts, then a warp scan) and take
-// recycled slots first, then appended slots, like omp_getNextFreeSlotInRXFront*
-// (CELLRECYCLE); the unit's wins are spread over its 32 lanes.  The full cell then
-// becomes recrystallized (grid = ndefg + rxg, counts, slot INACTIVE).
-__device__ __forceinline__ uint32_t commit_units(const DomainArgs& a) { return (full_cells(a) + 31u) / 32u; }
+// k_resolve: one thread per full cell, tiles of kBlock full cells: its attempts whose
+// claim holds the own ordinal won; writes the win mask, the mask of wins that go to
+// the Border list, the tile's two win counts and adds them to its supertile.
+// k_commit: winners are ranked per destination list in full-cell then direction
+// order (tile prefix from the supertile and tile counts) and take recycled slots
+// first, then appended slots, like omp_getNextFreeSlotInRXFront*(CELLRECYCLE); the
+// full cell then becomes recrystallized (grid = ndefg + rxg, counts, slot INACTIVE).
+__device__ __forceinline__ uint32_t commit_tiles(const DomainArgs& a) { return (full_cells(a) + kBlock - 1) / kBlock; }
 
 template <bool ONE>
 __global__ void __launch_bounds__(kBlock, 4) k_resolve(int base, int ndom) {
     __shared__ uint32_t s_pre[kMaxSegs + 1];
-    const uint32_t total = ONE ? commit_units(c_args[base])
-                               : seg_prefix(s_pre, ndom, [&](int s) { return commit_units(c_args[base + (s)]); });
-    const int lane = threadIdx.x & 31;
-    const uint32_t stride = gridDim.x * (uint32_t)kWarps;
-    for (uint32_t u = blockIdx.x * (uint32_t)kWarps + (threadIdx.x >> 5); u < total; u += stride) {
+    __shared__ uint32_t s_a[kWarps], s_b[kWarps];
+    const uint32_t total = ONE ? commit_tiles(c_args[base])
+                               : seg_prefix(s_pre, ndom, [&](int s) { return commit_tiles(c_args[base + (s)]); });
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    for (uint32_t u = blockIdx.x; u < total; u += gridDim.x) {
         const int s = ONE ? 0 : seg_find(s_pre, ndom, u);
         const DomainArgs& a = c_args[base + (s)];
-        const uint32_t unit = ONE ? u : u - s_pre[s];
+        const uint32_t tile = ONE ? u : u - s_pre[s];
         const uint32_t F0 = a.st->nfull[0], F = F0 + a.st->nfull[1];
-        const uint32_t f = unit * 32u + (uint32_t)lane;
+        const uint32_t f = tile * kBlock + threadIdx.x;
         uint32_t win = 0, tob = 0;
         if (f < F) {
             const uint32_t mask = a.amask[f];
@@ -1021,13 +1018,19 @@ __global__ void __launch_bounds__(kBlock, 4) k_resolve(int base, int ndom) {
         }
         uint32_t cB = __popc(tob), cA = __popc(win) - cB;
 #pragma unroll
-        for (int o = 16; o > 0; o >>= 1) { cA += __shfl_xor_sync(0xFFFFFFFFu, cA, o); cB += __shfl_xor_sync(0xFFFFFFFFu, cB, o); }
-        if (lane == 0) {
-            a.ctcnt[2 * unit] = cA;
-            a.ctcnt[2 * unit + 1] = cB;
-            if (cA) atomicAdd(&a.csct[2 * (unit / kSuper)], cA);
-            if (cB) atomicAdd(&a.csct[2 * (unit / kSuper) + 1], cB);
+        for (int o = 16; o > 0; o >>= 1) { cA += __shfl_down_sync(0xFFFFFFFFu, cA, o); cB += __shfl_down_sync(0xFFFFFFFFu, cB, o); }
+        if (lane == 0) { s_a[warp] = cA; s_b[warp] = cB; }
+        __syncthreads();
+        if (threadIdx.x == 0) {
+            uint32_t ta = 0, tb = 0;
+#pragma unroll
+            for (int w = 0; w < kWarps; ++w) { ta += s_a[w]; tb += s_b[w]; }
+            a.ctcnt[2 * tile] = ta;
+            a.ctcnt[2 * tile + 1] = tb;
+            if (ta) atomicAdd(&a.csct[2 * (tile / kSuper)], ta);
+            if (tb) atomicAdd(&a.csct[2 * (tile / kSuper) + 1], tb);
         }
+        __syncthreads();
     }
 }
 
@@ -1049,29 +1052,32 @@ __device__ __forceinline__ void flush_new(const DomainArgs& a, double pmax, uint
 template <bool FP32, bool ONE>
 __global__ void __launch_bounds__(kBlock, 3) k_commit(int base, int ndom) {
     __shared__ uint32_t s_pre[kMaxSegs + 1];
-    const uint32_t total = ONE ? commit_units(c_args[base])
-                               : seg_prefix(s_pre, ndom, [&](int s) { return commit_units(c_args[base + (s)]); });
-    const int lane = threadIdx.x & 31;
-    const uint32_t stride = gridDim.x * (uint32_t)kWarps;
+    __shared__ uint32_t s_a[kWarps], s_b[kWarps], s_w[kWarps], s_base[2];
+    // per full cell of the tile: win masks, first ranks, cell (| Border list << 31), grain, overshoot
+    __shared__ uint32_t s_off[kBlock + 1], s_win[kBlock], s_tob[kBlock], s_rA[kBlock], s_rB[kBlock], s_cell[kBlock], s_rsrc[kBlock];
+    __shared__ double s_over[kBlock];
+    const uint32_t total = ONE ? commit_tiles(c_args[base])
+                               : seg_prefix(s_pre, ndom, [&](int s) { return commit_tiles(c_args[base + (s)]); });
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     int cur = -1;           // domain whose P max and tag count are being accumulated
     double pmax = 0.0;      // max of the new positive weights
     uint32_t ntag = 0;      // new cells waiting for the host
-    for (uint32_t u = blockIdx.x * (uint32_t)kWarps + (threadIdx.x >> 5); u < total; u += stride) {
+    for (uint32_t u = blockIdx.x; u < total; u += gridDim.x) {
         const int s = ONE ? 0 : seg_find(s_pre, ndom, u);
         if (s != cur) {
             if (cur >= 0) flush_new(c_args[base + cur], pmax, ntag);
             cur = s; pmax = 0.0; ntag = 0;
         }
         const DomainArgs& a = c_args[base + (s)];
-        const uint32_t unit = ONE ? u : u - s_pre[s];
+        const uint32_t tile = ONE ? u : u - s_pre[s];
         const uint32_t F0 = a.st->nfull[0], F = F0 + a.st->nfull[1];
-        const uint32_t f = unit * 32u + (uint32_t)lane;
-        // the unit's own loads first, then its prefix: their latencies overlap
-        const int L = f >= F0 ? 1 : 0;
+        const uint32_t f = tile * kBlock + threadIdx.x;
+        if (warp == 0) {
+            uint32_t pa, pb;
+            tile_prefix(a.ctcnt, a.csct, tile, pa, pb);
+            if (lane == 0) { s_base[0] = pa; s_base[1] = pb; }
+        }
         const uint32_t win = f < F ? a.amask[f] : 0u, tob = f < F ? a.tobm[f] : 0u;
-        const uint32_t slot = f < F ? a.f[L].full[L ? f - F0 : f] : 0u;
-        uint32_t pa, pb;
-        tile_prefix(a.ctcnt, a.csct, unit, pa, pb);
         const uint32_t cB = __popc(tob), cA = __popc(win) - cB, cW = cA + cB;
         uint32_t iA = cA, iB = cB, iW = cW;
 #pragma unroll
@@ -1080,46 +1086,59 @@ __global__ void __launch_bounds__(kBlock, 3) k_commit(int base, int ndom) {
             const uint32_t xw = __shfl_up_sync(0xFFFFFFFFu, iW, o);
             if (lane >= o) { iA += xa; iB += xb; iW += xw; }
         }
-        const uint32_t rA = pa + iA - cA, rB = pb + iB - cB, oW = iW - cW;
-        const uint32_t W = __shfl_sync(0xFFFFFFFFu, iW, 31);
-        if (lane == 31 && unit + 1 == (ONE ? total : s_pre[s + 1] - s_pre[s])) {  // the domain's last unit: totals
-            a.st->nwin[0] = pa + iA;
-            a.st->nwin[1] = pb + iB;
-        }
-        // the lane's own full cell
-        uint32_t cell = 0, rsrc = 0, gsrc = 0;
-        double over = 0.0;
+        if (lane == 31) { s_a[warp] = iA; s_b[warp] = iB; s_w[warp] = iW; }
+        // the full cell's own data, loaded while the scans complete
+        const int L = f >= F0 ? 1 : 0;
+        uint32_t slot = 0, cell = 0, rsrc = 0, gsrc = 0;
         if (f < F) {
+            slot = a.f[L].full[L ? f - F0 : f];
             cell = a.f[L].xyz[slot];
             rsrc = a.f[L].rxg[slot];
             gsrc = a.f[L].defg[slot];
-            if (win) {
-                if (!FP32) over = __dsub_rn(((const double*)a.f[L].fill)[slot], 1.0);
-                else over = (double)((((const float*)a.f[L].fill)[slot] - 1.0f) - a.f[L].comp[slot]);
-            }
         }
-        const uint32_t scell = cell | ((uint32_t)L << 31);
-        // every win of the unit, spread over the lanes: win k belongs to lane t, the last
-        // lane with oW[t] <= k; its direction is the (k - oW[t])-th set bit of t's mask and
-        // its rank in the destination list counts t's earlier wins there
-        for (uint32_t k0 = 0; k0 < W; k0 += 32u) {
-            const uint32_t k = k0 + (uint32_t)lane;
-            int t = 0;
+        __syncthreads();
+        uint32_t rA = s_base[0] + iA - cA, rB = s_base[1] + iB - cB, oW = iW - cW;
 #pragma unroll
-            for (int step = 16; step > 0; step >>= 1) {
-                const uint32_t v = __shfl_sync(0xFFFFFFFFu, oW, t + step);
-                if (v <= k) t += step;
+        for (int w = 0; w < kWarps; ++w)
+            if (w < warp) { rA += s_a[w]; rB += s_b[w]; oW += s_w[w]; }
+        if (threadIdx.x == 0 && tile + 1 == (ONE ? total : s_pre[s + 1] - s_pre[s])) {  // the domain's last tile: totals
+            uint32_t ta = 0, tb = 0;
+#pragma unroll
+            for (int w = 0; w < kWarps; ++w) { ta += s_a[w]; tb += s_b[w]; }
+            a.st->nwin[0] = s_base[0] + ta;
+            a.st->nwin[1] = s_base[1] + tb;
+        }
+        s_off[threadIdx.x] = oW;
+        if (threadIdx.x == kBlock - 1) s_off[kBlock] = oW + cW;
+        s_win[threadIdx.x] = win;
+        s_tob[threadIdx.x] = tob;
+        s_rA[threadIdx.x] = rA;
+        s_rB[threadIdx.x] = rB;
+        s_cell[threadIdx.x] = cell | ((uint32_t)L << 31);
+        s_rsrc[threadIdx.x] = rsrc;
+        if (win) {
+            if (!FP32) s_over[threadIdx.x] = __dsub_rn(((const double*)a.f[L].fill)[slot], 1.0);
+            else s_over[threadIdx.x] = (double)((((const float*)a.f[L].fill)[slot] - 1.0f) - a.f[L].comp[slot]);
+        }
+        __syncthreads();
+        // every win of the tile by all threads: win k belongs to the full cell t with
+        // s_off[t] <= k < s_off[t + 1]; its direction is the (k - s_off[t])-th set bit and
+        // its rank in the destination list counts the cell's earlier wins there
+        const uint32_t W = s_off[kBlock];
+        for (uint32_t k = threadIdx.x; k < W; k += kBlock) {
+            int lo = 0, hi = kBlock - 1;
+            while (lo < hi) {
+                const int mid = (lo + hi + 1) >> 1;
+                if (s_off[mid] <= k) lo = mid;
+                else hi = mid - 1;
             }
-            const uint32_t m = __shfl_sync(0xFFFFFFFFu, win, t), tb = __shfl_sync(0xFFFFFFFFu, tob, t);
-            const uint32_t rAt = __shfl_sync(0xFFFFFFFFu, rA, t), rBt = __shfl_sync(0xFFFFFFFFu, rB, t);
-            const uint32_t ot = __shfl_sync(0xFFFFFFFFu, oW, t), sc = __shfl_sync(0xFFFFFFFFu, scell, t);
-            const uint32_t rs = __shfl_sync(0xFFFFFFFFu, rsrc, t);
-            const double ov = __shfl_sync(0xFFFFFFFFu, over, t);
-            if (k >= W) continue;
-            const int d = (int)__fns(m, 0u, (int)(k - ot) + 1);
+            const int t = lo;
+            const uint32_t m = s_win[t], tb = s_tob[t];
+            const int d = (int)__fns(m, 0u, (int)(k - s_off[t]) + 1);
             const int D = (tb >> d) & 1u;
             const uint32_t below = m & ((1u << d) - 1u);
-            const uint32_t r = D ? rBt + __popc(below & tb) : rAt + __popc(below & ~tb);
+            const uint32_t r = D ? s_rB[t] + __popc(below & tb) : s_rA[t] + __popc(below & ~tb);
+            const uint32_t sc = s_cell[t];
             const int Ls = (int)(sc >> 31);
             int x, y, z;
             decode(a, sc & 0x7FFFFFFFu, x, y, z);
@@ -1135,12 +1154,13 @@ __global__ void __launch_bounds__(kBlock, 3) k_commit(int base, int ndom) {
             const int cls = c_cls[d];
             if (!FP32) {
                 const double fac = cls == 1 ? 0.0682 : (cls == 2 ? 0.0542 : 0.0484);
-                ((double*)dst.fill)[ns] = __dmul_rn(ov, fac);
+                ((double*)dst.fill)[ns] = __dmul_rn(s_over[t], fac);
             } else {
                 const float fac = cls == 1 ? 0.0682f : (cls == 2 ? 0.0542f : 0.0484f);
-                ((float*)dst.fill)[ns] = (float)ov * fac;
+                ((float*)dst.fill)[ns] = (float)s_over[t] * fac;
                 dst.comp[ns] = 0.0f;
             }
+            const uint32_t rs = s_rsrc[t];
             dst.defg[ns] = gt;
             dst.rxg[ns] = rs;
             dst.xyz[ns] = tgt;
@@ -1196,6 +1216,7 @@ __global__ void __launch_bounds__(kBlock, 3) k_commit(int base, int ndom) {
                 }
             }
         }
+        __syncthreads();
     }
     if (cur >= 0) flush_new(c_args[base + cur], pmax, ntag);
 }
@@ -1223,7 +1244,7 @@ __global__ void __launch_bounds__(kBlock) k_step_end(int base, int ndom, uint32_
     if (threadIdx.x == 0) {
         const uint32_t F = st->nfull[0] + st->nfull[1];
         for (int L = 0; L < 2; ++L) s_sup[L] = ((st->next_never[L] + grow_tile - 1) / grow_tile + kSuper - 1) / kSuper;
-        s_sup[2] = ((F + 31u) / 32u + kSuper - 1) / kSuper;
+        s_sup[2] = ((F + kBlock - 1) / kBlock + kSuper - 1) / kSuper;
         const uint32_t cap[2] = {a.f[0].cap, a.f[1].cap};
         for (int D = 0; D < 2; ++D) {
             if (st->nwin[D] > st->nrec[D]) st->next_never[D] += st->nwin[D] - st->nrec[D];
