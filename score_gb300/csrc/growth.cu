@@ -341,7 +341,7 @@ void score_ctx::release_domain() {
     if (device >= 0) cudaSetDevice(device);
     void* ptrs[] = {a.f[0].inc, a.f[1].inc, scratch.inc, a.f[0].mob, a.f[1].mob, scratch.mob, a.f[0].fill, a.f[0].comp, a.f[0].vel, a.f[0].defg, a.f[0].rxg, a.f[0].xyz, a.f[0].dir, a.f[0].full, a.f[0].recyc,
                     a.f[1].fill, a.f[1].comp, a.f[1].vel, a.f[1].defg, a.f[1].rxg, a.f[1].xyz, a.f[1].dir, a.f[1].full, a.f[1].recyc,
-                    a.grid, a.claim, a.amask, a.ptab, a.defg_cnt, a.rxg_cnt, a.depleted, a.miss, a.tobm, a.ctcnt,
+                    a.grid, a.claim, a.amask, a.ptab, a.defg_cnt, a.rxg_cnt, a.depleted, a.miss, a.tobm, a.ctcnt, a.fcell,
                     a.f[0].fmask, a.f[0].imask, a.f[0].tcnt, a.f[1].fmask, a.f[1].imask, a.f[1].tcnt,
                     a.f[0].scnt, a.f[1].scnt, a.csct,
                     d_state, d_pforce, d_u32tmp, d_stage, d_grid_init, d_defg_cnt_init, d_rxq, d_dfq, d_due,
@@ -1583,6 +1583,7 @@ int score_load_domain(score_ctx* c, const uint32_t* grid, const double* defg_qua
         if (e == cudaSuccess) e = dalloc(&a.claim, N);
         if (e == cudaSuccess) e = dalloc(&a.amask, N);
         if (e == cudaSuccess) e = dalloc(&a.tobm, N);
+        if (e == cudaSuccess) e = dalloc(&a.fcell, N);
         if (e == cudaSuccess) e = dalloc(&a.ctcnt, 2 * (N / kBlock + 2));
         if (e == cudaSuccess) e = dalloc(&a.csct, c->csct_words);
         if (e == cudaSuccess) e = dalloc(&a.ptab, ptab_words);

@@ -89,6 +89,7 @@ struct DomainArgs {
     uint32_t* claim;
     uint32_t* amask;            // per full cell: attempts made (bit d), then attempts won
     uint32_t* tobm;             // per full cell: won attempts that go to the Border list
+    uint32_t* fcell;            // per full cell: its cell index (written by k_claim)
     uint32_t* ctcnt;            // per commit tile: (Inside, Border) win counts
     uint32_t* csct;             // per supertile of kSuper commit tiles: the same counts (zero between steps)
     unsigned long long* ptab;   // nrxg x ndefg mobility weights as bits (kPtabEmpty = unknown)
@@ -817,6 +818,7 @@ __global__ void __launch_bounds__(kBlock, 2) k_claim(int base, int ndom) {
         if (f < F0) {
             // an Inside cell: all 26 grid reads in flight before the first claim
             const uint32_t cell = a.f[0].xyz[a.f[0].full[f]];
+            a.fcell[f] = cell;
             uint32_t gv[26];
 #pragma unroll
             for (int d = 0; d < 26; ++d) {
@@ -835,6 +837,7 @@ __global__ void __launch_bounds__(kBlock, 2) k_claim(int base, int ndom) {
             }
         } else {
             const uint32_t cell = a.f[1].xyz[a.f[1].full[f - F0]];
+            a.fcell[f] = cell;
             int x, y, z;
             decode(a, cell, x, y, z);
             mask = claim_plane<0, 8, false>(a, cell, x, y, z, f);
@@ -986,7 +989,7 @@ __global__ void __launch_bounds__(kBlock, 4) k_resolve(int base, int ndom) {
             const uint32_t mask = a.amask[f];
             if (mask) {
                 const int L = f >= F0 ? 1 : 0;
-                const uint32_t cell = a.f[L].xyz[a.f[L].full[L ? f - F0 : f]];
+                const uint32_t cell = a.fcell[f];
                 int x, y, z;
                 decode(a, cell, x, y, z);
                 const bool allB = (L == 0) && !(x > 1 && x < (int)a.nx - 2 && y > 1 && y < (int)a.ny - 2 && z > 1 && z < (int)a.nz - 2);
@@ -1092,7 +1095,7 @@ __global__ void __launch_bounds__(kBlock, 3) k_commit(int base, int ndom) {
         uint32_t slot = 0, cell = 0, rsrc = 0, gsrc = 0;
         if (f < F) {
             slot = a.f[L].full[L ? f - F0 : f];
-            cell = a.f[L].xyz[slot];
+            cell = a.fcell[f];
             rsrc = a.f[L].rxg[slot];
             gsrc = a.f[L].defg[slot];
         }
