@@ -314,6 +314,7 @@ struct score_ctx {
     bool own_eng = false;
     bool running = false;              // steps in the next batched step
     double weights_ms = 0.0;           // host time in requested weights (summed into the engine's timing)
+    bool ans_ready = false;            // the engine computed this step's requested weights already
     std::vector<unsigned long long> ans_idx;  // weights computed for the last step's requests
     std::vector<double> ans_val;
     uint64_t launches = 0;             // kernels launched outside the step sequence
@@ -405,6 +406,12 @@ void free_slots(int device, int base, int n) {
 }
 
 // Persistent worker threads for the per-domain host work of a batched step.
+// Host worker threads for the per-domain and per-grain work between GPU steps.  A step's
+// host work comes in short rounds a few hundred microseconds apart, so an idle worker spins
+// (yielding) for up to kSpin before it sleeps: a round then starts and ends in about a
+// microsecond instead of the tens of microseconds of a condition-variable wake-up.
+// Jobs are handed out as tickets (round << 32 | index): a worker still finishing an older
+// round can never take, or lose, a job of a newer one.
 class WorkerPool {
 public:
     explicit WorkerPool(unsigned n) {
@@ -413,60 +420,68 @@ public:
     ~WorkerPool() {
         {
             std::lock_guard<std::mutex> l(mu_);
-            stop_ = true;
+            stop_.store(true);
         }
         cv_.notify_all();
         for (auto& t : th_) t.join();
     }
     // run f(0..n-1) on the workers and the calling thread; returns when all are done
     void run(int n, const std::function<void(int)>& f) {
+        const uint64_t g = ++round_;
+        ticket_.store(g << 32);  // first: tickets of the last round stop working
+        job_.store(&f);
+        njobs_.store((uint32_t)n);
+        pending_.store(n);
         {
             std::lock_guard<std::mutex> l(mu_);
-            job_ = &f;
-            njobs_ = n;
-            next_.store(0);
-            pending_ = n;
-            ++gen_;
+            gen_.store(g);
         }
-        cv_.notify_all();
-        work();
-        std::unique_lock<std::mutex> l(mu_);
-        done_.wait(l, [this] { return pending_ == 0; });
-        job_ = nullptr;
+        if (sleepers_.load() > 0) cv_.notify_all();
+        work(g);
+        while (pending_.load() > 0) std::this_thread::yield();
     }
 
 private:
-    void work() {
+    static constexpr std::chrono::microseconds kSpin{2000};
+    void work(uint64_t g) {
         for (;;) {
-            const int i = next_.fetch_add(1);
-            if (i >= njobs_.load()) return;
-            (*job_.load())(i);
-            std::lock_guard<std::mutex> l(mu_);
-            if (--pending_ == 0) done_.notify_all();
+            uint64_t t = ticket_.load();
+            for (;;) {
+                if ((t >> 32) != g || (uint32_t)t >= njobs_.load()) return;
+                if (ticket_.compare_exchange_weak(t, t + 1)) break;
+            }
+            (*job_.load())((int)(uint32_t)t);
+            pending_.fetch_sub(1);
         }
     }
     void loop() {
         uint64_t seen = 0;
         for (;;) {
-            {
+            const auto t0 = std::chrono::steady_clock::now();
+            while (gen_.load() == seen && !stop_.load()) {
+                if (std::chrono::steady_clock::now() - t0 < kSpin) {
+                    std::this_thread::yield();
+                    continue;
+                }
                 std::unique_lock<std::mutex> l(mu_);
-                cv_.wait(l, [&] { return stop_ || gen_ != seen; });
-                if (stop_) return;
-                seen = gen_;
-                if (!job_.load()) continue;
+                sleepers_.fetch_add(1);
+                cv_.wait(l, [&] { return stop_.load() || gen_.load() != seen; });
+                sleepers_.fetch_sub(1);
             }
-            work();
+            if (stop_.load()) return;
+            seen = gen_.load();
+            work(seen);
         }
     }
     std::vector<std::thread> th_;
     std::mutex mu_;
-    std::condition_variable cv_, done_;
+    std::condition_variable cv_;
     std::atomic<const std::function<void(int)>*> job_{nullptr};
-    std::atomic<int> njobs_{0};
-    int pending_ = 0;
-    std::atomic<int> next_{0};
-    uint64_t gen_ = 0;
-    bool stop_ = false;
+    std::atomic<uint64_t> ticket_{0}, gen_{0};
+    std::atomic<uint32_t> njobs_{0};
+    std::atomic<int> pending_{0}, sleepers_{0};
+    std::atomic<bool> stop_{false};
+    uint64_t round_ = 0;  // only the calling thread starts rounds
 };
 
 struct Engine {
@@ -547,6 +562,7 @@ struct Engine {
     void launch_sequence(int n);
     cudaError_t enqueue_step(int n, bool timed, bool refresh_only);
     int step(bool timed);
+    void balance_weights();
     int run_until(double x_target, uint32_t max_steps, uint32_t* steps_done);
     int autotune(double x_target, uint32_t max_steps, score_tune* out);
     void get_tune(score_tune* out) const;
@@ -650,8 +666,9 @@ void resolve_weights(score_ctx* c, const std::vector<unsigned long long>& idx, s
         E.pool->run(chunks, [&](int k) { work(n * (size_t)k / chunks, n * (size_t)(k + 1) / chunks); });
         return;
     }
+    // a batch computes its domains' weights on the engine's workers already: no nested threads
     unsigned nth = std::max(1u, std::min(32u, std::thread::hardware_concurrency()));
-    if (n < 4096 || nth == 1) { work(0, n); return; }
+    if (n < 4096 || nth == 1 || E.dom.size() > 1) { work(0, n); return; }
     std::vector<std::thread> th;
     for (unsigned t = 0; t < nth; ++t) th.emplace_back(work, n * t / nth, n * (t + 1) / nth);
     for (auto& t : th) t.join();
@@ -962,10 +979,14 @@ int post_step(score_ctx* c, uint32_t newnuc, score_step_stats* out) {
     // mobility weights requested this step: computed on the host (FP64, libm)
     double pmax_new = 0.0;
     if (hs.pmax_bits) memcpy(&pmax_new, &hs.pmax_bits, 8);
-    c->ans_idx.clear();
-    c->ans_val.clear();
     uint32_t nreq = 0;  // distinct weights requested (void race slots excluded)
-    if (hs.nmiss > 0) {
+    if (c->ans_ready) {  // computed by the engine over all domains' requests
+        c->ans_ready = false;
+        for (double v : c->ans_val) if (v > pmax_new) pmax_new = v;
+        for (unsigned long long x : c->ans_idx) nreq += x != kMissVoid;
+    } else if (hs.nmiss > 0) {
+        c->ans_idx.clear();
+        c->ans_val.clear();
         std::vector<unsigned long long> idx(hs.nmiss);
         std::vector<double> val;
         cudaError_t e = cudaSuccess;
@@ -984,6 +1005,9 @@ int post_step(score_ctx* c, uint32_t newnuc, score_step_stats* out) {
         // staged by the engine into one host-to-device copy before the next step
         c->ans_idx.swap(idx);
         c->ans_val.swap(val);
+    } else {
+        c->ans_idx.clear();
+        c->ans_val.clear();
     }
     // deformed grains that ran out of cells this step (synchronize_mydefpool_counts)
     if (hs.ndepleted > 0) {
@@ -1178,6 +1202,47 @@ int Engine::stage_answers() {
     return SCORE_OK;
 }
 
+// The requested weights of all running domains of a batch, spread evenly over the workers:
+// after nucleation a few domains request thousands of weights and would hold up a step
+// whose post-processing gives each domain to one worker.  Few requests stay with their
+// domain's post step.
+void Engine::balance_weights() {
+    std::vector<score_ctx*> req;
+    std::vector<size_t> off(1, 0);
+    for (score_ctx* c : dom) {
+        c->ans_ready = false;
+        if (!c->running) continue;
+        const DevState& hs = c->h_box->snap;
+        if (hs.err || hs.nmiss == 0 || hs.nmiss > kBoxMiss) continue;
+        req.push_back(c);
+        off.push_back(off.back() + hs.nmiss);
+    }
+    const size_t total = off.back();
+    if (total < 512) return;
+    const auto t0 = std::chrono::steady_clock::now();
+    for (size_t j = 0; j < req.size(); ++j) {
+        score_ctx* c = req[j];
+        c->ans_idx.assign(c->h_box->miss, c->h_box->miss + (off[j + 1] - off[j]));
+        c->ans_val.assign(off[j + 1] - off[j], 0.0);
+        c->ans_ready = true;
+    }
+    constexpr size_t kChunk = 64;
+    const int nchunks = (int)((total + kChunk - 1) / kChunk);
+    if (!pool) pool.reset(new WorkerPool(std::max(1u, std::min(15u, std::thread::hardware_concurrency() - 1))));
+    pool->run(nchunks, [&](int k) {
+        const size_t lo = (size_t)k * kChunk, hi = std::min(total, lo + kChunk);
+        size_t j = (size_t)(std::upper_bound(off.begin(), off.end(), lo) - off.begin()) - 1;
+        for (size_t i = lo; i < hi; ++i) {
+            while (i >= off[j + 1]) ++j;
+            score_ctx* c = req[j];
+            const unsigned long long x = c->ans_idx[i - off[j]];
+            // a void slot (lost race) keeps 0, which no cell reads
+            if (x != kMissVoid) c->ans_val[i - off[j]] = weight_of(c, (uint32_t)(x / c->ndefg), (uint32_t)(x % c->ndefg));
+        }
+    });
+    tm.weights_ms += std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
+}
+
 // One step of every running domain.
 int Engine::step(bool timed) {
     cudaSetDevice(device);
@@ -1242,6 +1307,7 @@ int Engine::step(bool timed) {
     const double bpu = fp32 ? 21.0 : 25.0;  // algorithmic bytes per front-cell update of k_grow_fill
     for (int i = 0; i < n; ++i)
         if (status[i] != SCORE_OK) return fail(status[i], dom[i]->err);
+    if (n >= 4) balance_weights();
     // the master-block work of each domain (weights, P max, X, rho max, dt) is independent
     auto post = [&](int i) {
         score_ctx* c = dom[i];
