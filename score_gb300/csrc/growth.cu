@@ -660,9 +660,9 @@ void resolve_weights(score_ctx* c, const std::vector<unsigned long long>& idx, s
     };
     size_t n = idx.size();
     Engine& E = *c->eng;
-    if (n >= 256 && E.dom.size() == 1) {  // one domain: the engine's workers (a batch runs its domains in parallel)
+    if (n >= 16 && E.dom.size() == 1) {  // one domain: the engine's workers (a batch runs its domains in parallel)
         if (!E.pool) E.pool.reset(new WorkerPool(std::max(1u, std::min(7u, std::thread::hardware_concurrency() - 1))));
-        const int chunks = (int)std::min<size_t>(32, n / 64);
+        const int chunks = (int)std::min<size_t>(32, n / 8);
         E.pool->run(chunks, [&](int k) { work(n * (size_t)k / chunks, n * (size_t)(k + 1) / chunks); });
         return;
     }
