@@ -112,6 +112,18 @@ def test_fp64_recovery_refreshes_velocities(gpu, tmp_uds):
     compare(sg.read_uds(tmp_uds(sg.UdsSpec(nx=64, ny=64, nz=64, recovery=3))), d)
 
 
+def test_fp64_recovery_refresh_mixes(gpu, tmp_uds):
+    """Recovery refreshes every velocity factor every step from the cached mobilities:
+    Rollett-Holm, distinct LAGB / GS mobilities, and a heating schedule that interleaves full
+    refreshes from the P table (new mobilities) with the cached-mobility refreshes."""
+    d = sg.generate_domain(64, 64, 64, 60, 40, seed=22)
+    compare(sg.read_uds(tmp_uds(sg.UdsSpec(nx=64, ny=64, nz=64, recovery=10, recovery_k="20.0", mobility_model=2))), d)
+    compare(sg.read_uds(tmp_uds(sg.UdsSpec(nx=64, ny=64, nz=64, recovery=10, recovery_k="20.0", LAGBm0="30.0", GSm0="600.0"))), d)
+    spec = sg.UdsSpec(nx=64, ny=64, nz=64, recovery=10, recovery_k="20.0",
+                      schedule=[("0.0", "700.0"), ("0.05", "760.0"), ("360000.0", "760.0")])
+    compare(sg.read_uds(tmp_uds(spec)), d)
+
+
 def test_fp64_heating_schedule(gpu, tmp_uds):
     d = sg.generate_domain(64, 64, 64, 50, 30, seed=18)
     spec = sg.UdsSpec(nx=64, ny=64, nz=64, schedule=[("0.0", "700.0"), ("0.05", "760.0"), ("360000.0", "760.0")])
