@@ -511,6 +511,11 @@ struct Engine {
     uint64_t launches = 0;
     std::string err;
     std::unique_ptr<WorkerPool> pool;  // batches of several domains
+    unsigned pool_threads = 0;         // workers of the pool (0: the caller's default)
+    WorkerPool& workers(unsigned dflt) {
+        if (!pool) pool.reset(new WorkerPool(std::max(1u, pool_threads ? pool_threads : std::min(dflt, std::thread::hardware_concurrency() - 1))));
+        return *pool;
+    }
     // the host's weights for all domains' requests, in pinned device-mapped memory: the
     // few cells that wait for them read them directly (no copy before the step)
     unsigned long long* h_ans_i = nullptr; double* h_ans_v = nullptr;
@@ -578,7 +583,7 @@ void for_grains(score_ctx* c, Body body) {
     const size_t n = c->ndefg;
     Engine& E = *c->eng;
     if (n < 8192 || E.dom.size() != 1) { body(0, n); return; }
-    if (!E.pool) E.pool.reset(new WorkerPool(std::max(1u, std::min(7u, std::thread::hardware_concurrency() - 1))));
+    E.workers(7);
     constexpr int kChunks = 16;
     E.pool->run(kChunks, [&](int k) { body(n * (size_t)k / kChunks, n * (size_t)(k + 1) / kChunks); });
 }
@@ -661,7 +666,7 @@ void resolve_weights(score_ctx* c, const std::vector<unsigned long long>& idx, s
     size_t n = idx.size();
     Engine& E = *c->eng;
     if (n >= 16 && E.dom.size() == 1) {  // one domain: the engine's workers (a batch runs its domains in parallel)
-        if (!E.pool) E.pool.reset(new WorkerPool(std::max(1u, std::min(7u, std::thread::hardware_concurrency() - 1))));
+        E.workers(7);
         const int chunks = (int)std::min<size_t>(32, n / 8);
         E.pool->run(chunks, [&](int k) { work(n * (size_t)k / chunks, n * (size_t)(k + 1) / chunks); });
         return;
@@ -1228,7 +1233,7 @@ void Engine::balance_weights() {
     }
     constexpr size_t kChunk = 64;
     const int nchunks = (int)((total + kChunk - 1) / kChunk);
-    if (!pool) pool.reset(new WorkerPool(std::max(1u, std::min(15u, std::thread::hardware_concurrency() - 1))));
+    workers(15);
     pool->run(nchunks, [&](int k) {
         const size_t lo = (size_t)k * kChunk, hi = std::min(total, lo + kChunk);
         size_t j = (size_t)(std::upper_bound(off.begin(), off.end(), lo) - off.begin()) - 1;
@@ -1278,7 +1283,7 @@ int Engine::step(bool timed) {
             status[i] = physics_ahead(c);
         };
         if (n >= 4) {
-            if (!pool) pool.reset(new WorkerPool(std::max(1u, std::min(15u, std::thread::hardware_concurrency() - 1))));
+            workers(15);
             pool->run(n, ahead);
         } else {
             for (int i = 0; i < n; ++i) ahead(i);
@@ -1316,7 +1321,7 @@ int Engine::step(bool timed) {
         status[i] = post_step(c, newnuc[i], nullptr);
     };
     if (n >= 4) {
-        if (!pool) pool.reset(new WorkerPool(std::max(1u, std::min(15u, std::thread::hardware_concurrency() - 1))));
+        workers(15);
         pool->run(n, post);
     } else {
         for (int i = 0; i < n; ++i) post(i);
@@ -1813,8 +1818,12 @@ int score_autotune(score_ctx* c, double x_target, uint32_t max_steps, score_tune
 }  // extern "C"
 
 // ------------------------------------------------------------------ batched ensemble
+// A batch splits its domains into groups of about equal cell count, each stepped by its own
+// engine (stream, argument slots, graphs, workers) from its own host thread: the groups'
+// latency-bound kernels overlap on the GPU and their host work overlaps on the CPU.  Within a
+// group the domains step in lock-step, one sequence of launches per step.
 struct score_batch {
-    Engine eng;
+    std::vector<std::unique_ptr<Engine>> engs;
     std::vector<score_ctx*> dom;
     std::string err;
     ~score_batch() {
@@ -1823,7 +1832,24 @@ struct score_batch {
     }
     int fail(int code, const std::string& m) { err = m; return code; }
     int dom_fail(score_ctx* c, int code) { err = c->err; return code; }
+    // f(g) for every group on its own thread (the calling thread takes group 0); first error wins
+    template <class F>
+    int each_group(F f) {
+        const size_t G = engs.size();
+        std::vector<int> st(G, SCORE_OK);
+        std::vector<std::thread> th;
+        for (size_t g = 1; g < G; ++g) th.emplace_back([&, g] { st[g] = f(g); });
+        st[0] = f(0);
+        for (auto& t : th) t.join();
+        for (size_t g = 0; g < G; ++g)
+            if (st[g] != SCORE_OK) return fail(st[g], engs[g]->err);
+        return SCORE_OK;
+    }
 };
+
+namespace {
+constexpr uint32_t kGroupDomains = 32;  // domains per group (per engine and stream) of a batch
+}
 
 extern "C" {
 
@@ -1836,12 +1862,29 @@ int score_batch_create(score_batch** out, const score_params* params, uint32_t n
         if (params[i].precision != params[0].precision) return SCORE_ERR_ARG;  // one precision per batch
     }
     score_batch* b = new score_batch();
-    const int si = b->eng.init(device, (int)n);
-    if (si != SCORE_OK) { delete b; return si; }
-    b->eng.fp32 = params[0].precision == SCORE_PRECISION_FP32_KAHAN;
+    // groups of about equal cell count: largest domain first, to the lightest group
+    const uint32_t G = std::max(1u, std::min(n / kGroupDomains, 4u));
+    std::vector<uint32_t> order(n), group(n), count(G, 0);
+    std::vector<uint64_t> load(G, 0);
+    for (uint32_t i = 0; i < n; ++i) order[i] = i;
+    auto cells = [&](uint32_t i) { return (uint64_t)params[i].nx * params[i].ny * params[i].nz; };
+    std::stable_sort(order.begin(), order.end(), [&](uint32_t x, uint32_t y) { return cells(x) > cells(y); });
+    for (uint32_t i : order) {
+        const uint32_t g = (uint32_t)(std::min_element(load.begin(), load.end()) - load.begin());
+        group[i] = g; load[g] += cells(i); ++count[g];
+    }
+    const unsigned hw = std::max(2u, std::thread::hardware_concurrency());
+    for (uint32_t g = 0; g < G; ++g) {
+        b->engs.emplace_back(new Engine());
+        Engine& E = *b->engs.back();
+        const int si = E.init(device, (int)count[g]);
+        if (si != SCORE_OK) { delete b; return si; }
+        E.fp32 = params[0].precision == SCORE_PRECISION_FP32_KAHAN;
+        E.pool_threads = std::max(1u, (hw - 1) / G);
+    }
     for (uint32_t i = 0; i < n; ++i) {
         score_ctx* c = nullptr;
-        const int s = make_ctx(&params[i], &b->eng, false, &c);
+        const int s = make_ctx(&params[i], b->engs[group[i]].get(), false, &c);
         if (s != SCORE_OK) { delete b; return s; }
         b->dom.push_back(c);
     }
@@ -1868,7 +1911,7 @@ int score_batch_restart(score_batch* b) {
         const int s = score_restart(c);
         if (s != SCORE_OK) return b->dom_fail(c, s);
     }
-    b->eng.mark_run_start();
+    for (auto& E : b->engs) E->mark_run_start();
     return SCORE_OK;
 }
 
@@ -1885,8 +1928,10 @@ int score_batch_place_nuclei(score_batch* b) {
 int score_batch_run_until(score_batch* b, double x_target, uint32_t max_steps, uint32_t* steps_done) {
     if (!b) return SCORE_ERR_ARG;
     for (score_ctx* c : b->dom) c->trace.clear();
-    const int s = b->eng.run_until(x_target, max_steps, steps_done);
-    return s == SCORE_OK ? s : b->fail(s, b->eng.err);
+    std::vector<uint32_t> steps(b->engs.size(), 0);
+    const int s = b->each_group([&](size_t g) { return b->engs[g]->run_until(x_target, max_steps, &steps[g]); });
+    if (steps_done) *steps_done = *std::max_element(steps.begin(), steps.end());
+    return s;
 }
 
 int score_batch_get_stats(score_batch* b, uint32_t d, score_step_stats* out) {
@@ -1916,23 +1961,36 @@ int score_batch_grain_counts(score_batch* b, uint32_t d, uint32_t* rxg_counts, u
 
 int score_batch_get_timing(score_batch* b, score_timing* out) {
     if (!b || !out) return SCORE_ERR_ARG;
-    *out = b->eng.tm;
-    uint64_t extra = 0;
-    for (score_ctx* c : b->dom) extra += c->launches;
-    out->kernel_launches = b->eng.launches + extra;
+    // device and host times summed over the groups (they run concurrently), the run span the longest
+    *out = score_timing{};
+    uint64_t launches = 0;
+    for (auto& E : b->engs) {
+        const score_timing& t = E->tm;
+        out->total_ms += t.total_ms; out->grow_ms += t.grow_ms; out->claim_ms += t.claim_ms; out->commit_ms += t.commit_ms;
+        out->host_ms += t.host_ms; out->grow_launches += t.grow_launches; out->grow_bytes += t.grow_bytes;
+        out->step_bytes += t.step_bytes; out->fill_ms += t.fill_ms; out->wait_ms += t.wait_ms; out->weights_ms += t.weights_ms;
+        out->pre_ms += t.pre_ms; out->post_ms += t.post_ms; out->timed_steps += t.timed_steps;
+        out->run_ms = std::max(out->run_ms, t.run_ms);
+        launches += E->launches;
+    }
+    for (score_ctx* c : b->dom) launches += c->launches;
+    out->kernel_launches = launches;
     return SCORE_OK;
 }
 
 int score_batch_get_tune(score_batch* b, score_tune* out) {
     if (!b || !out) return SCORE_ERR_ARG;
-    b->eng.get_tune(out);
+    b->engs[0]->get_tune(out);
     return SCORE_OK;
 }
 
 int score_batch_set_tune(score_batch* b, const score_tune* t) {
     if (!b || !t) return SCORE_ERR_ARG;
-    const int s = b->eng.set_tune(t);
-    return s == SCORE_OK ? s : b->fail(s, b->eng.err);
+    for (auto& E : b->engs) {
+        const int s = E->set_tune(t);
+        if (s != SCORE_OK) return b->fail(s, E->err);
+    }
+    return SCORE_OK;
 }
 
 int score_batch_autotune(score_batch* b, double x_target, uint32_t max_steps, score_tune* out) {
@@ -1940,8 +1998,10 @@ int score_batch_autotune(score_batch* b, double x_target, uint32_t max_steps, sc
     int s = score_batch_restart(b);
     if (s == SCORE_OK) s = score_batch_place_nuclei(b);
     if (s != SCORE_OK) return s;
-    s = b->eng.autotune(x_target, max_steps, out);
-    if (s != SCORE_OK) return b->fail(s, b->eng.err);
+    std::vector<score_tune> tunes(b->engs.size());
+    s = b->each_group([&](size_t g) { return b->engs[g]->autotune(x_target, max_steps, &tunes[g]); });
+    if (s != SCORE_OK) return s;
+    if (out) *out = tunes[0];
     s = score_batch_restart(b);
     if (s == SCORE_OK) s = score_batch_place_nuclei(b);
     return s;
