@@ -242,9 +242,10 @@ int  score_autotune(score_ctx* ctx, double x_target, uint32_t max_steps, score_t
 
 /*
  * Batched ensemble: many independent domains (own sizes, grains, nuclei, parameters;
- * one precision) stepped together.  Each step is one sequence of kernels over all
- * running domains, replayed as one CUDA graph; a domain that meets its stop rule
- * leaves the launches.  Mirrors the reference's ensemble of solitary units that its
+ * one precision) stepped together.  The domains form groups of about equal cell count
+ * (two from 64 domains on), each stepped concurrently on its own stream; within a group
+ * each step is one sequence of kernels over its running domains, replayed as one CUDA
+ * graph, and a domain that meets its stop rule leaves the launches.  Mirrors the reference's ensemble of solitary units that its
  * ranks step one after another (SCORE_Kernel.cpp:1640-1756).  Domain d of a batch
  * accepts the single-domain functions' arguments.  The domains of all live contexts
  * and batches of one device share 64 argument slots: a batch holds at most 64 domains,
