@@ -295,8 +295,6 @@ struct score_ctx {
     NucDue* h_due = nullptr;               // pinned staging of nuclei due during the run
     NucDue* d_due = nullptr;
     uint32_t* d_grid_init = nullptr;       // the loaded deformed grid (restart source)
-    double* d_rxq = nullptr;               // orientation quaternions on the device
-    double* d_dfq = nullptr;
     uint32_t* d_defg_cnt_init = nullptr;   // its per-grain cell counts
     uint32_t* d_u32tmp = nullptr;
     void* d_stage = nullptr;
@@ -345,7 +343,7 @@ void score_ctx::release_domain() {
                     a.grid, a.claim, a.amask, a.ptab, a.defg_cnt, a.rxg_cnt, a.depleted, a.miss, a.tobm, a.ctcnt, a.fcell,
                     a.f[0].fmask, a.f[0].imask, a.f[0].tcnt, a.f[1].fmask, a.f[1].imask, a.f[1].tcnt,
                     a.f[0].scnt, a.f[1].scnt, a.csct,
-                    d_state, d_pforce, d_u32tmp, d_stage, d_grid_init, d_defg_cnt_init, d_rxq, d_dfq, d_due,
+                    d_state, d_pforce, d_u32tmp, d_stage, d_grid_init, d_defg_cnt_init, d_due,
                     scratch.fill, scratch.comp, scratch.vel, scratch.defg, scratch.rxg, scratch.xyz, scratch.dir};
     for (void* p : ptrs) if (p) cudaFree(p);
     if (h_pforce) cudaFreeHost(h_pforce);
@@ -355,7 +353,7 @@ void score_ctx::release_domain() {
     a = DomainArgs{};
     scratch = DFront{};
     d_state = nullptr; d_pforce = nullptr; d_u32tmp = nullptr; d_stage = nullptr;
-    d_grid_init = nullptr; d_defg_cnt_init = nullptr; d_rxq = nullptr; d_dfq = nullptr;
+    d_grid_init = nullptr; d_defg_cnt_init = nullptr;
     stage_cap = 0; scratch_cap = 0;
     loaded = false;
 }
@@ -1669,23 +1667,16 @@ int score_load_domain(score_ctx* c, const uint32_t* grid, const double* defg_qua
         if (e == cudaSuccess) e = cudaMallocHost((void**)&c->h_due, kDueMax * sizeof(NucDue));
         if (e == cudaSuccess) e = dalloc(&c->d_due, kDueMax);
         if (e == cudaSuccess) e = dalloc(&c->d_u32tmp, 64);
-        if (e == cudaSuccess) e = dalloc(&c->d_rxq, 4 * (size_t)nrxg);
-        if (e == cudaSuccess) e = dalloc(&c->d_dfq, 4 * (size_t)ndefg);
         if (e != cudaSuccess) { c->release_domain(); return c->fail(SCORE_ERR_NOMEM, std::string("device allocation: ") + cudaGetErrorString(e)); }
         a.pforce = c->d_pforce;
         a.st = c->d_state;
         a.box = c->d_box;
-        a.rxq = c->d_rxq; a.dfq = c->d_dfq;
-        weight_constants(p, &a.pc_fac, &a.pc_lagb, &a.pc_maxdev, a.pc_m40, &a.pc_theta_sat);
-        a.pc_margin = 1e-9;
         c->high_water[0] = a.f[0].cap; c->high_water[1] = a.f[1].cap;  // the reset clears every slot once
     } else {
         c->high_water[0] = std::max(c->high_water[0], c->next_never[0]);
         c->high_water[1] = std::max(c->high_water[1], c->next_never[1]);
     }
     e = cudaMemcpyAsync(c->d_grid_init, grid, N * 4, cudaMemcpyHostToDevice, c->stream);
-    if (e == cudaSuccess && nrxg) e = cudaMemcpyAsync(c->d_rxq, rxg_quat, 4 * (size_t)nrxg * 8, cudaMemcpyHostToDevice, c->stream);
-    if (e == cudaSuccess) e = cudaMemcpyAsync(c->d_dfq, defg_quat, 4 * (size_t)ndefg * 8, cudaMemcpyHostToDevice, c->stream);
     if (e == cudaSuccess && ptable) e = cudaMemcpyAsync(a.ptab, ptable, ptab_words * 8, cudaMemcpyHostToDevice, c->stream);
     if (e == cudaSuccess) e = cudaMemsetAsync(c->d_defg_cnt_init, 0, (size_t)ndefg * 4, c->stream);
     if (e == cudaSuccess) e = cudaMemsetAsync(c->d_state, 0, sizeof(DevState), c->stream);

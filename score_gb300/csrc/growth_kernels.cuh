@@ -118,15 +118,7 @@ struct DomainArgs {
     float dtc32;
     int32_t spec;               // few INACTIVE slots: k_grow_fill loads every slot's fill data with its
                                 // infector byte instead of after it (no effect on results)
-    // device classification of mobility weights whose value is an exact constant
-    const double* rxq;          // nrxg x 4 orientation quaternions
-    const double* dfq;          // ndefg x 4
-    double pc_fac;              // 1/sqrt(2) as the host computes it
-    double pc_lagb;             // 15 deg in rad (LAGB/HAGB threshold)
-    double pc_maxdev;           // 10 deg in rad (proximity to 40 deg <111>)
-    double pc_m40[4];           // the 40 deg <111> quaternion as the host computes it
-    double pc_theta_sat;        // Rollett-Holm: P is exactly 1.0 for theta above this (inf = never)
-    double pc_margin;           // safety margin around every threshold [rad]
+    double pc_fac;              // 1/sqrt(2) as the host computes it (the disorientation of d_grimmer)
 };
 
 __device__ __forceinline__ void decode(const DomainArgs& a, uint32_t cell, int& x, int& y, int& z) {
@@ -848,13 +840,9 @@ __global__ void __launch_bounds__(kBlock, 2) k_claim(int base, int ndom) {
     }
 }
 
-// ---- device classification of mobility weights ----
-// The weight P(rxg,defg) is -1 (LAGB), 0 (HAGB away from 40deg<111>) or, for the
-// Rollett-Holm sigmoid at large disorientation, exactly 1.0.  The disorientation's
-// scalar part omega is computed with the host's exact operation sequence (no FMA),
-// so only acos differs between device and host libm (a few ulp); a case whose angle
-// lies within pc_margin of a threshold, and every case whose weight is a genuine
-// libm expression, is left to the host.
+// ---- device disorientation (the no-allocation weight table) ----
+// The disorientation's scalar part omega in the host's exact operation sequence (no FMA),
+// so only acos differs between device and host libm (a few ulp).
 __device__ __forceinline__ void d_quat_mul(const double a[4], const double b[4], double r[4]) {
     r[0] = __dsub_rn(__dsub_rn(__dsub_rn(__dmul_rn(a[0], b[0]), __dmul_rn(a[1], b[1])), __dmul_rn(a[2], b[2])), __dmul_rn(a[3], b[3]));
     r[1] = __dadd_rn(__dadd_rn(__dmul_rn(b[0], a[1]), __dmul_rn(a[0], b[1])), __dsub_rn(__dmul_rn(a[2], b[3]), __dmul_rn(a[3], b[2])));
@@ -891,70 +879,29 @@ __device__ __forceinline__ double d_disori(const DomainArgs& A, const double p[4
     if (om < (1.0 - 5.0e-16)) return 2.0 * acos(om);
     return 0.0;
 }
-__device__ __noinline__ bool device_weight(const DomainArgs& A, uint32_t rxg, uint32_t defg, double& P) {
-    const double* p = A.rxq + 4 * (size_t)rxg;
-    const double* q = A.dfq + 4 * (size_t)defg;
-    const double pr[4] = {p[0], p[1], p[2], p[3]}, qd[4] = {q[0], q[1], q[2], q[3]};
-    const double theta = d_disori(A, pr, qd, nullptr);
-    const double m = A.pc_margin;
-    if (A.mobility_model == 2) {
-        if (theta > A.pc_theta_sat) { P = 1.0; return true; }
-        return false;
-    }
-    if (theta == 0.0 || theta < A.pc_lagb - m) { P = -1.0; return true; }
-    if (!(theta > A.pc_lagb + m)) return false;
-    // HAGB: distance of the disorientation to 40deg<111>
-    double c[6][4];
-    d_grimmer(A, pr, qd, c);
-    int mi = 0;
-    double mx = 0.0;
-#pragma unroll
-    for (int i = 0; i < 6; ++i)
-#pragma unroll
-        for (int j = 0; j < 4; ++j)
-            if (fabs(c[i][j]) > mx) { mx = fabs(c[i][j]); mi = i; }
-    double s[4] = {fabs(c[mi][0]), fabs(c[mi][1]), fabs(c[mi][2]), fabs(c[mi][3])};
-    // ascending sort of four values (the order of equal values is immaterial)
-#pragma unroll
-    for (int i = 0; i < 3; ++i)
-#pragma unroll
-        for (int k = 0; k < 3 - i; ++k)
-            if (s[k] > s[k + 1]) { const double t = s[k]; s[k] = s[k + 1]; s[k + 1] = t; }
-    const double qdis[4] = {s[3], s[2], s[1], s[0]};
-    const double dev = d_disori(A, qdis, A.pc_m40, nullptr);
-    if (dev > A.pc_maxdev + m) { P = 0.0; return true; }
-    return false;
-}
-
-// P of a new cell from the table.  An unknown entry is classified on the device when
-// its value is exact; otherwise it is requested from the host: the first requester
-// takes miss slot m (atomicAdd) and tags the entry kPtabTag | m; every cell of the pair
-// carries m and gets P from the host's answer m in the next step's k_grow_fill.  A
-// requester that loses the race to tag the entry voids its slot.  Returns true with P,
-// or false with the tag.
+// P of a new cell from the table.  An unknown entry is requested from the host (FP64,
+// libm, on its worker threads): the first requester takes miss slot m (atomicAdd) and
+// tags the entry kPtabTag | m; every cell of the pair carries m and gets P from the host's
+// answer m in the next step's k_grow_fill.  A requester that loses the race to tag the
+// entry voids its slot.  Returns true with P, or false with the tag.  (Classifying the
+// exact-constant weights on the device cost more than it saved: FP64 runs at 1/64 rate,
+// cells racing on a new pair all classify it, and the classifier's registers took a
+// quarter of this kernel's occupancy.)
 __device__ __forceinline__ bool lookup_p(const DomainArgs& a, uint32_t rxg, uint32_t defg, double& P, uint32_t& tag) {
     const unsigned long long idx = (unsigned long long)rxg * a.ndefg + defg;
     unsigned long long* e = &a.ptab[idx];
     unsigned long long bits = *(volatile unsigned long long*)e;
     if (bits == kPtabEmpty) {
-        double v;
-        if (device_weight(a, rxg, defg, v)) {
-            const unsigned long long vb = (unsigned long long)__double_as_longlong(v);
-            const unsigned long long old = atomicCAS(e, kPtabEmpty, vb);
-            if (old == kPtabEmpty || old == vb) { P = v; return true; }
-            bits = old;
-        } else {
-            const uint32_t m = atomicAdd(&a.st->nmiss, 1u);
-            if (m >= a.misscap) { atomicOr(&a.st->err, kErrMissCap); tag = 0; return false; }
-            const unsigned long long old = atomicCAS(e, kPtabEmpty, kPtabTag | m);
-            if (old == kPtabEmpty) {
-                a.miss[m] = idx;
-                tag = m;
-                return false;
-            }
-            a.miss[m] = kMissVoid;
-            bits = old;
+        const uint32_t m = atomicAdd(&a.st->nmiss, 1u);
+        if (m >= a.misscap) { atomicOr(&a.st->err, kErrMissCap); tag = 0; return false; }
+        const unsigned long long old = atomicCAS(e, kPtabEmpty, kPtabTag | m);
+        if (old == kPtabEmpty) {
+            a.miss[m] = idx;
+            tag = m;
+            return false;
         }
+        a.miss[m] = kMissVoid;
+        bits = old;
     }
     if ((bits >> 48) == (kPtabTag >> 48)) { tag = (uint32_t)bits; return false; }
     P = __longlong_as_double((long long)bits);
