@@ -72,6 +72,11 @@ double mobility_weight(const score_params& prm, const double qr[4], const double
     }
     if (theta <= lagb_hagb) return -1.0;
     const double maxDev = (10.0) / (180.0) * (kPi);
+    // The deviation from 40deg<111> is at least |theta - 40 deg| (triangle inequality of the
+    // disorientation, a metric on orientations modulo the cubic group), so far from 40 deg the
+    // weight is the reference's 0 without its second disorientation; the 1e-9 rad margin is
+    // many orders above the rounding of either angle.
+    if (std::fabs(theta - 2.0 * kPi / 9.0) > maxDev + 1e-9) return 0.0;
     const double sqrt3inv = 1 / std::sqrt(3.0);
     const double oneNinth = 1.0 / 9.0;
     double qdis[4];

@@ -61,3 +61,37 @@ def test_oracle_matches_live_reference(built, tmp_path, uds_kw, gen_kw):
                   ("rhomax", "rhomax")]:
         assert np.array_equal(tr[f], rt[rf]), f"{f}: {first_difference(tr[f], rt[rf])}"
     assert np.array_equal(oracle.run(p, d)["labels"], ref["labels"])
+
+
+def test_host_weight_matches_oracle_on_random_and_boundary_pairs(built, tmp_path):
+    """The library's host weight (which skips the 40deg<111> deviation far from 40 deg) against
+    the oracle's restatement, bit for bit: random orientation pairs, and pairs rotated to lie
+    just inside and outside the 15 deg and the 30 / 50 deg (40 +- 10) thresholds."""
+    rng = np.random.default_rng(7)
+    p = sg.read_uds(sg.UdsSpec(nx=50, ny=50, nz=50).write(tmp_path / "w.uds"))
+
+    def unit(q):
+        return q / np.linalg.norm(q, axis=-1, keepdims=True)
+
+    def axis_angle(axis, deg):
+        axis = unit(np.asarray(axis, dtype=np.float64))
+        h = np.radians(deg) / 2.0
+        return np.concatenate([np.cos(h)[..., None], np.sin(h)[..., None] * axis], axis=-1)
+
+    def qmul(a, b):
+        a0, a1, a2, a3 = np.moveaxis(a, -1, 0)
+        b0, b1, b2, b3 = np.moveaxis(b, -1, 0)
+        return np.stack([a0 * b0 - a1 * b1 - a2 * b2 - a3 * b3, a0 * b1 + a1 * b0 + a2 * b3 - a3 * b2,
+                         a0 * b2 - a1 * b3 + a2 * b0 + a3 * b1, a0 * b3 + a1 * b2 - a2 * b1 + a3 * b0], axis=-1)
+
+    qd = unit(rng.normal(size=(3000, 4)))
+    qr = unit(rng.normal(size=(3000, 4)))
+    # near the thresholds: rotations about random axes and about <111> by 15, 30, 40, 50 deg +- tiny
+    k = 1200
+    angles = rng.choice([15.0, 30.0, 50.0, 40.0], size=k) + rng.choice([-1e-7, 1e-7, -1e-4, 1e-4, 0.0], size=k)
+    axes = np.where(rng.random((k, 1)) < 0.5, np.ones((k, 3)) + rng.normal(scale=1e-3, size=(k, 3)), rng.normal(size=(k, 3)))
+    qr[:k] = unit(qmul(qd[:k], axis_angle(axes, angles)))
+    host = np.array([sg.mobility_weight(p, qr[i], qd[i]) for i in range(len(qr))])
+    orc = np.array([oracle.mobility_weight(p, qr[i], qd[i]) for i in range(len(qr))])
+    assert np.array_equal(host.view(np.uint64), orc.view(np.uint64))
+    assert (host == -1.0).any() and (host == 0.0).any() and ((host > 0.0) & (host < 1.0)).any()
