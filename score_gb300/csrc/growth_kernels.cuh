@@ -32,8 +32,8 @@
 //             recrystallized (grid = ndefg + rxg, counts, slot INACTIVE) — the tail of
 //             updateFullRX{Inside,Border}, SCORE_Kernel.cpp:4559-4774.  The wins of a
 //             tile are spread over all its threads; each new cell gets its mobility
-//             weight P (table, device classification, or a tag for the host) and
-//             cached velocity factor.
+//             weight P (from the table, or a tag for the host) and cached velocity
+//             factor.
 //   k_step_end  slot high-water marks, stats snapshot, reset of the per-step fields.
 #pragma once
 #include <cstdint>

@@ -40,7 +40,7 @@ constexpr double kOverFac1 = 0.0682, kOverFac2 = 0.0542, kOverFac3 = 0.0484;
 double mobility_weight(const score_params& p, const double qr[4], const double qd[4]);
 // minimum disorientation angle for cubic symmetry, Grimmer's 24 expressions
 double disori_angle_cubic(const double p[4], const double q[4]);
-// the constants mobility_weight uses, for the device's exact-case classifier
+// the constants mobility_weight uses, for the device's weight table (no-allocation entry point)
 void weight_constants(const score_params& prm, double* fac, double* lagb, double* maxdev, double m40[4], double* theta_sat);
 void disori_quat_cubic(const double p[4], const double q[4], double out[4]);
 
