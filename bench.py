@@ -23,9 +23,9 @@ until X > 0.99.  Inputs are synthetic and seeded (rank r uses seed r).
 FP64 path), `--autotune` picks the launch configuration first.
 
 `--impl reference` times the reference's CPU path instead: the oracle port (the
-SCORE reference cannot be compiled on this host) as independent same-density
-192^3 domains, one per host core, like the reference's MPI ensemble of solitary
-units; rank 0 only.
+SCORE reference's sources are not on the GPU host) on the same 512^3 workload, one
+whole run per process on every host core, like the reference's MPI ensemble of
+solitary units; loop time only; rank 0 only.
 """
 from __future__ import annotations
 
@@ -37,7 +37,6 @@ import subprocess
 import sys
 import tempfile
 import time
-from concurrent.futures import ProcessPoolExecutor
 from pathlib import Path
 
 import numpy as np
@@ -206,36 +205,139 @@ def cpu_baseline(n: int = 256) -> dict:
                       f"({sv} updates in {loop_s:.2f} s)"}
 
 
+REF_RSS_BYTES = 3.0e9     # peak resident memory of one 512^3 oracle process (2.4 GB measured) with headroom
+REF_WARM_EDGE = 64        # warm-up domains of the reference arm: same densities, 64^3
+
+
+def _mem_available() -> float:
+    try:
+        for line in Path("/proc/meminfo").read_text().splitlines():
+            if line.startswith("MemAvailable:"):
+                return float(line.split()[1]) * 1024.0
+    except OSError:
+        pass
+    return 0.0
+
+
+def _ref_worker(conn, shared: str):
+    """One process of the reference arm: the headline workload's 512^3 domain (shared by
+    the parent as .npy files in `shared`, mapped read-only), stepped by the oracle port in
+    pieces on command.  Nothing here loads the CUDA library."""
+    sys.path.insert(0, str(ROOT))
+    import score_gb300 as sg
+    import oracle
+    try:
+        def load(tag):
+            a = [np.load(Path(shared) / f"{tag}_{k}.npy", mmap_mode="r") for k in range(6)]
+            return sg.Domain(int(a[0].shape[2]), int(a[0].shape[1]), int(a[0].shape[0]), *a)
+        d, dw = load("main"), load("warm")
+        p, pw = read_params(N_EDGE), read_params(REF_WARM_EDGE)
+        sim = oracle.Sim(p, d)
+        conn.send(("ready", None))
+        while True:
+            cmd, arg = conn.recv()
+            if cmd == "warm":      # one whole same-density 64^3 run (untimed)
+                oracle.run(pw, dw, x_target=X_TARGET)
+                conn.send(("ok", None))
+            elif cmd == "advance":  # the 512^3 run up to X > arg: this piece's updates, steps and loop seconds
+                r = sim.advance(x_target=arg)
+                conn.send(("ok", (int(r["trace"]["Sv"].sum()), int(r["n_steps"]), float(r["seconds"]), int(r["status"]))))
+            else:
+                sim.close()
+                conn.send(("ok", None))
+                return
+    except Exception as e:  # reported to the parent, which stops the arm
+        conn.send(("error", repr(e)))
+
+
 def run_reference_arm(args) -> None:
-    """The reference's CPU algorithm on the host cores; under torchrun only rank 0
-    works and prints, the other ranks exit at once (no process group needed)."""
+    """The reference's CPU algorithm (the C oracle port of solve_RXGROWTH) on the host cores,
+    on the headline workload itself: every process steps the GPU arm's 512^3 domain (20,000
+    grains, 50,000 nuclei, seed 0, the same physics) from nucleation to X > 0.99, like the
+    reference's ensemble of solitary units over MPI ranks.  The parent makes the inputs
+    once, before the timed region, and shares them through files in /dev/shm.  Bench step k advances every process's run to
+    X > 0.99 k / steps; its time is the longest process's loop time of that piece, so the
+    timed steps cover exactly one whole run per process.  Warm-up steps run whole
+    same-density 64^3 domains.  Under torchrun only rank 0 works and prints."""
     rank, world, _ = dist_env()
     if rank != 0:
         return
+    import multiprocessing as mp
     import oracle
+    import score_gb300 as sg
+    sg.build()          # host-only library for the inputs (the CUDA library is not loaded)
     oracle.build_oracle()
     cores = os.cpu_count() or 1
-    n = 192
-    def one_round(k):
-        with ProcessPoolExecutor(max_workers=cores, mp_context=__import__("multiprocessing").get_context("spawn")) as ex:
-            t0 = time.perf_counter()
-            res = list(ex.map(oracle_sample, [(n, 5000 + 131 * k + i) for i in range(cores)]))
-            return sum(r[0] for r in res), time.perf_counter() - t0
-    for w in range(args.warmup):
-        one_round(w)
-    tot_sv, tot_s = 0, 0.0
-    for k in range(args.steps):
-        sv, s = one_round(100 + k)
-        tot_sv += sv
-        tot_s += s
+    avail = _mem_available()
+    # one oracle process per core, as many as the host's free memory holds (the shared inputs aside)
+    nproc = max(1, min(cores, int(0.8 * (avail - 1.5e9) / REF_RSS_BYTES))) if avail > 0 else cores
+    t_setup = time.perf_counter()
+    shm = Path("/dev/shm") if Path("/dev/shm").is_dir() else Path(tempfile.gettempdir())
+    shared = Path(tempfile.mkdtemp(prefix="score_refarm_", dir=shm))
+    fw = (REF_WARM_EDGE / N_EDGE) ** 3
+    for tag, dom in (("main", sg.generate_domain(N_EDGE, N_EDGE, N_EDGE, N_GRAINS, N_NUCLEI, seed=0)),
+                     ("warm", sg.generate_domain(REF_WARM_EDGE, REF_WARM_EDGE, REF_WARM_EDGE, max(1, round(N_GRAINS * fw)),
+                                                 max(1, round(N_NUCLEI * fw)), seed=1))):
+        for k, a in enumerate((dom.grid, dom.defg_quat, dom.defg_rho0, dom.rxg_quat, dom.rxg_site, dom.rxg_tincub)):
+            np.save(shared / f"{tag}_{k}.npy", a)
+        del dom
+    ctx = mp.get_context("spawn")
+    pipes, procs = [], []
+    for i in range(nproc):
+        a, b = ctx.Pipe()
+        pr = ctx.Process(target=_ref_worker, args=(b, str(shared)), daemon=True)
+        pr.start()
+        pipes.append(a)
+        procs.append(pr)
+
+    def gather():
+        out = []
+        for c in pipes:
+            tag, val = c.recv()
+            if tag == "error":
+                raise RuntimeError(f"reference arm worker failed: {val}")
+            out.append(val)
+        return out
+
+    try:
+        gather()  # every process has its inputs
+        t_setup = time.perf_counter() - t_setup
+        for _ in range(args.warmup):
+            for c in pipes:
+                c.send(("warm", None))
+            gather()
+        tot_sv, tot_s, tot_steps = 0, 0.0, 0
+        for k in range(1, args.steps + 1):
+            xt = X_TARGET * k / args.steps
+            for c in pipes:
+                c.send(("advance", xt))
+            res = gather()
+            if any(r[3] != 0 for r in res):
+                raise RuntimeError(f"oracle status {[r[3] for r in res]}")
+            tot_sv += sum(r[0] for r in res)
+            tot_steps += max(r[1] for r in res)
+            tot_s += max(r[2] for r in res)
+        for c in pipes:
+            c.send(("close", None))
+        gather()
+    finally:
+        for pr in procs:
+            pr.join(timeout=30)
+            if pr.is_alive():
+                pr.kill()
+        import shutil
+        shutil.rmtree(shared, ignore_errors=True)
     v = tot_sv / tot_s
+    sample = (f"C oracle port of solve_RXGROWTH (the reference's sources are not on this host), {nproc} processes on "
+              f"{cores} host cores, each one whole run of the 512^3 workload's domain (seed 0) from nucleation to X>0.99, "
+              f"split into {args.steps} pieces by X; loop time only (inputs made before, {t_setup:.0f} s)")
     line = {"impl": "reference", "metric": METRIC, "value": v, "unit": "updates/s", "n_gpus": args.gpus, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": 1e3 * tot_s / max(1, args.steps), "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-            "config": {"workload": WORKLOAD, "sample": f"{cores} independent {n}^3 domains per step at the same densities"},
-            "cpu_baseline": {"value": v, "unit": "updates/s", "cores": cores, "kind": "port",
-                             "sample": f"C oracle (the reference's algorithm restated; the reference itself does not build on this host), "
-                                       f"{cores} processes x one {n}^3 domain each, to X>0.99"},
+            "config": {"workload": WORKLOAD, "cells": N_EDGE ** 3, "grains": N_GRAINS, "nuclei": N_NUCLEI,
+                       "processes": nproc, "runs_timed": nproc, "updates_timed": tot_sv,
+                       "growth_steps_per_run": tot_steps, "mem_available_gb": round(avail / 1e9, 1)},
+            "cpu_baseline": {"value": v, "unit": "updates/s", "cores": nproc, "kind": "port", "sample": sample},
             "e2e": {"value": v, "unit": "updates/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line), flush=True)
 
@@ -431,6 +533,80 @@ class BatchWorkload:
         self.b.close()
 
 
+def measure_batched(sg, args, local) -> dict:
+    """The metric's ratio on the batched ensemble (64 domains, edges uniform in [64, 256]
+    per axis, 100-5000 grains, 50-2000 nuclei; domain i from seed i): the batched path in
+    FP64 and in FP32+Kahan (updates/s over whole runs to X > 0.99, inputs resident, CUDA
+    events), against the same 64 domains stepped one after another, each through its own
+    single-domain context (score_run_until, FP64): the reference steps its solitary units
+    one after another the same way.  FP32 error against the FP64 batch (bit-exact)."""
+    shapes = batch_shapes(64)
+    doms, p64, p32 = [], [], []
+    with tempfile.TemporaryDirectory() as td:
+        for k, (nx, ny, nz, ng, nn, seed) in enumerate(shapes):
+            p64.append(sg.read_uds(sg.UdsSpec(nx=nx, ny=ny, nz=nz, precision=0).write(Path(td) / f"{k}a.uds")))
+            p32.append(sg.read_uds(sg.UdsSpec(nx=nx, ny=ny, nz=nz, precision=1).write(Path(td) / f"{k}b.uds")))
+            doms.append(sg.generate_domain(nx, ny, nz, ng, nn, seed=seed))
+    runs = max(1, min(args.steps, 5))
+    out = {"workload": "64 domains, edges uniform in [64,256] per axis, 100-5000 grains, 50-2000 nuclei, until X>0.99",
+           "cells": int(sum(a * b * c for a, b, c, *_ in shapes)), "runs_timed": runs}
+
+    def batch_rate(params):
+        with sg.Batch(params, device=local) as b:
+            for k, d in enumerate(doms):
+                b.load_domain(k, d)
+            sv, ms = 0, 0.0
+            for r in range(1 + runs):  # the first run is a warm-up
+                b.restart()
+                b.place_nuclei()
+                b.run_until(X_TARGET)
+                if r:
+                    sv += sum(s.Sv for k in range(len(doms)) for s in b.trace(k))
+                    ms += b.timing().run_ms
+            labs = [b.labels(k) for k in range(len(doms))]
+            xs = [np.array([s.X for s in b.trace(k)]) for k in range(len(doms))]
+            launches = b.timing().kernel_launches
+        return sv / (ms / 1e3), labs, xs, launches
+
+    v64, lab64, x64, _ = batch_rate(p64)
+    v32, lab32, x32, _ = batch_rate(p32)
+    errs = []
+    for k, d in enumerate(doms):
+        m = min(len(x32[k]), len(x64[k]))
+        errs.append(label_error(lab32[k], lab64[k], x32[k][:m], x64[k][:m], d.ndefg))
+    # the same domains one after another through single-domain contexts
+    gms = []
+    try:
+        for k, d in enumerate(doms):
+            gm = sg.GrowthMachine(p64[k], device=local)
+            gms.append(gm)
+            gm.load_domain(d)
+        sv, ms = 0, 0.0
+        for r in range(1 + runs):
+            for gm in gms:
+                gm.restart()
+                gm.place_nuclei()
+                tr = gm.run_until(X_TARGET)
+                if r:
+                    sv += sum(s.Sv for s in tr)
+                    ms += gm.timing().run_ms
+        vseq = sv / (ms / 1e3)
+    finally:
+        for gm in gms:
+            gm.close()
+    out.update({
+        "fp64_batched_updates_per_s": v64, "fp32_kahan_batched_updates_per_s": v32,
+        "plain_fp64_same_domains_updates_per_s": vseq,
+        "ratio_fp32_batched_vs_plain_fp64_same_domains": v32 / vseq,
+        "ratio_fp64_batched_vs_plain_fp64_same_domains": v64 / vseq,
+        "fp32_error_vs_fp64": {"label_mismatch": max(e["label_mismatch"] for e in errs),
+                               "max_abs_dX": max(e["max_abs_dX"] for e in errs),
+                               "mean_grain_size_rel_err": max(e["mean_grain_size_rel_err"] for e in errs),
+                               "aggregate": "max over the 64 domains"},
+        "plain_path": "each domain through score_create / score_load_domain / score_run_until, one after another"})
+    return out
+
+
 def label_error(lab32, lab64, x32, x64, ndefg):
     """fraction of cells with a different final label, max |dX(t)|, relative error of the
     mean recrystallized grain size (cells per recrystallized grain)."""
@@ -458,6 +634,7 @@ def main():
     ap.add_argument("--autotune", action="store_true", help="pick the launch configuration before timing")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true", help="skip the end-to-end runs (profiling captures)")
+    ap.add_argument("--no-batched", action="store_true", help="skip the batched-ensemble ratio (profiling captures)")
     args = ap.parse_args()
     if args.impl == "reference":
         run_reference_arm(args)
@@ -510,6 +687,10 @@ def main():
     every = wl.timing_every()
     fp32_err = wl.fp32_error() if args.precision == 1 else None
     wl.close()
+    batched = None
+    if args.workload == "plain" and args.edge == N_EDGE and args.precision == 0 and not args.no_batched:
+        batched = measure_batched(sg, args, local)
+        batched["ratio_fp32_batched_vs_plain_fp64_512"] = batched["fp32_kahan_batched_updates_per_s"] / value
 
     if rank == 0:
         peak, peak_kind = measured_peak_gbs()
@@ -537,6 +718,7 @@ def main():
                                 "claim_blocks_per_sm": t.claim_blocks_per_sm, "commit_blocks_per_sm": t.commit_blocks_per_sm}
         if fp32_err is not None:
             cfg["fp32_error_vs_fp64"] = fp32_err
+        cfg["ms_per_growth_step"] = run_ms / max(1, tot_steps)
         line = {
             "metric": METRIC, "value": value, "unit": "updates/s", "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": run_ms / args.steps, "higher_is_better": True, "scaling": "weak",
@@ -549,6 +731,8 @@ def main():
             "gpu_launches": int(launches),
             "clocks": clk.summary(),
         }
+        if batched is not None:
+            line["batched"] = batched
         if not args.no_cpu_baseline:
             line["cpu_baseline"] = cpu_baseline()
         print(json.dumps(line), flush=True)

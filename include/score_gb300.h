@@ -294,11 +294,13 @@ int  score_mobility_weight(const score_params* p, const double* rxg_q, const dou
  * results are ready when the stream reaches that point.  Allocates nothing: its
  * only scratch is a static 512 KiB device array with one word per row, so nrxg is
  * at most 65536 (SCORE_ERR_SCRATCH_LIMIT above that, nothing launched).  The
- * scratch holds a completion counter that must be 0 when a launch starts; the
- * library's last block of every launch resets it, so it stays 0 between calls.
- * The first call on a device resolves the scratch address (cudaGetSymbolAddress,
- * which may load the library's device code); a caller that captures streams into
- * graphs makes that first call before it begins a capture.  Calls on the same
+ * scratch holds a completion counter, cleared on the stream (cudaMemsetAsync, no
+ * allocation) before every launch.  The first call on a device resolves the
+ * scratch address (cudaGetSymbolAddress, which may load the library's device code)
+ * and keeps it for the life of the process: a caller that resets the device
+ * (cudaDeviceReset) after that first call must not call this entry point again.  A
+ * caller that captures streams into graphs makes that first call before it begins
+ * a capture.  Calls on the same
  * device share the scratch: calls that overlap in time (two streams, two host
  * threads) race and must be serialized by the caller.  Entries agree with
  * score_mobility_weight to a few ulp (CUDA's acos/cos/exp/pow instead of libm);

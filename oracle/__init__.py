@@ -24,7 +24,9 @@ import numpy as np
 HERE = Path(__file__).resolve().parent
 BUILD = HERE / "_build"
 REFOUT = HERE / "_ref"
-REFERENCE_SRC = Path(os.environ.get("SCORE_REFERENCE", "/root/reference"))
+# the reference's source tree: only from $SCORE_REFERENCE (no default location); without
+# it, the harness prebuilt into oracle/_ref/ is used when present
+REFERENCE_SRC = Path(os.environ["SCORE_REFERENCE"]) if os.environ.get("SCORE_REFERENCE") else None
 
 STEP_DTYPE = np.dtype([("step", "<u4"), ("n_nuclei", "<u4"), ("t", "<f8"), ("dt", "<f8"), ("dt_used", "<f8"),
                        ("Xcells", "<f8"), ("X", "<f8"), ("Sv", "<u8"), ("n_full", "<u8"), ("n_new", "<u8"),
@@ -52,14 +54,21 @@ def build_oracle(force: bool = False) -> Path:
     return out
 
 
+def reference_sources() -> bool:
+    """True when $SCORE_REFERENCE points at the reference's source tree."""
+    return REFERENCE_SRC is not None and (REFERENCE_SRC / "src" / "SCORE_Kernel.cpp").exists()
+
+
 def reference_available() -> bool:
-    return (REFERENCE_SRC / "src" / "SCORE_Kernel.cpp").exists() or (REFOUT / "score_ref_driver").exists()
+    return reference_sources() or (REFOUT / "score_ref_driver").exists()
 
 
 def build_ref() -> Path | None:
-    """Compile the reference harness (only where the reference sources exist)."""
+    """Compile the reference harness from $SCORE_REFERENCE; without the sources, the
+    prebuilt harness in oracle/_ref/ if there is one, else None ("reference sources not
+    found")."""
     exe = REFOUT / "score_ref_driver"
-    if not (REFERENCE_SRC / "src" / "SCORE_Kernel.cpp").exists():
+    if not reference_sources():
         return exe if exe.exists() else None
     subprocess.run(["make", "-s", "-C", str(HERE / "ref"), f"REF={REFERENCE_SRC}", f"-j{os.cpu_count() or 4}"], check=True)
     return exe
@@ -75,6 +84,13 @@ def _load():
         lib.oracle_run.restype = C.c_int
         lib.oracle_mobility_weight.restype = C.c_double
         lib.oracle_mobility_weight.argtypes = [C.c_void_p, C.c_void_p, C.c_void_p]
+        lib.oracle_create.restype = C.c_void_p
+        lib.oracle_advance.restype = C.c_int
+        lib.oracle_advance.argtypes = [C.c_void_p, C.c_double, C.c_uint32, C.c_void_p, C.c_uint32, C.c_void_p]
+        lib.oracle_done.restype = C.c_int
+        lib.oracle_done.argtypes = [C.c_void_p, C.c_double]
+        lib.oracle_finish.argtypes = [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]
+        lib.oracle_destroy.argtypes = [C.c_void_p]
         _lib = lib
     return _lib
 
@@ -102,6 +118,52 @@ def run(params, domain, ptable=None, x_target: float = -1.0, max_steps: int = 0,
             "dt0": out.dt0, "Pmax0": out.Pmax0, "n_nuclei": out.n_nuclei, "seconds": out.seconds, "n_steps": out.n_steps}
 
 
+class Sim:
+    """One oracle run advanced in pieces (bounded CPU samples of a long run).
+
+    ``advance(x_target, max_steps)`` runs the step loop until the stop rule with
+    ``x_target`` holds or ``max_steps`` more steps are done, and returns this piece's
+    trace rows and loop seconds; pieces concatenate to exactly the trace of ``run``."""
+
+    def __init__(self, params, domain, ptable=None):
+        self._lib = _load()
+        d = domain
+        self.params = params
+        self.ncells, self.nrxg, self.ndefg = d.ncells, d.nrxg, d.ndefg
+        self._keep = [np.ascontiguousarray(x) for x in (d.grid, d.defg_quat, d.defg_rho0, d.rxg_quat, d.rxg_site, d.rxg_tincub)]
+        self._pt = None if ptable is None else np.ascontiguousarray(ptable, dtype=np.float64)
+        k = self._keep
+        self._h = self._lib.oracle_create(C.byref(params), _p(k[0]), _p(k[1]), _p(k[2]), C.c_uint32(d.ndefg), _p(k[3]), _p(k[4]),
+                                          _p(k[5]), C.c_uint32(d.nrxg), _p(self._pt))
+        if not self._h:
+            raise MemoryError("oracle_create failed")
+
+    def advance(self, x_target: float = -1.0, max_steps: int = 0, trace_cap: int = 200000) -> dict:
+        trace = np.zeros(trace_cap, dtype=STEP_DTYPE)
+        out = OracleOut()
+        s = self._lib.oracle_advance(self._h, C.c_double(x_target), C.c_uint32(max_steps), _p(trace), C.c_uint32(trace_cap),
+                                     C.byref(out))
+        return {"status": s, "trace": trace[:min(out.n_steps, trace_cap)], "seconds": out.seconds, "n_steps": out.n_steps}
+
+    def done(self, x_target: float = -1.0) -> bool:
+        return bool(self._lib.oracle_done(self._h, C.c_double(x_target)))
+
+    def finish(self) -> dict:
+        labels = np.empty(self.ncells, dtype=np.uint32)
+        rc = np.empty(max(self.nrxg, 1), dtype=np.uint32)
+        dc = np.empty(self.ndefg, dtype=np.uint32)
+        self._lib.oracle_finish(self._h, _p(labels), _p(rc), _p(dc))
+        return {"labels": labels, "rxg_counts": rc[: self.nrxg], "defg_counts": dc}
+
+    def close(self) -> None:
+        if self._h:
+            self._lib.oracle_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        self.close()
+
+
 def mobility_weight(params, qr, qd) -> float:
     lib = _load()
     a = np.ascontiguousarray(qr, dtype=np.float64)
@@ -124,7 +186,8 @@ def run_ref(mode: str, uds_path, domain, workdir=None, threads: int = 1, timeout
     """Run the reference harness in `mode` (loop | asis | ptab) on `domain`."""
     exe = build_ref()
     if exe is None or not exe.exists():
-        raise RuntimeError("reference harness unavailable (no reference sources and no prebuilt driver)")
+        raise RuntimeError("reference sources not found: set SCORE_REFERENCE to the SCORE source tree "
+                           "(no prebuilt harness in oracle/_ref/ either)")
     wd = Path(workdir or tempfile.mkdtemp(prefix="scoreref_"))
     wd.mkdir(parents=True, exist_ok=True)
     scdm = domain.write_scdm(wd / "domain.scdm")

@@ -454,13 +454,23 @@ static uint32_t place_nuclei(sim* s, const uint32_t* site, const double* tincub,
     return n;
 }
 
-int oracle_run(const score_params* p, const uint32_t* grid, const double* defg_q, const double* defg_rho0, uint32_t ndefg,
-               const double* rxg_q, const uint32_t* rxg_site, const double* rxg_tincub, uint32_t nrxg, const double* ptable,
-               double x_target, uint32_t max_steps, oracle_step* trace, uint32_t trace_cap, uint32_t* labels,
-               uint32_t* rxg_counts, uint32_t* defg_counts, oracle_out* out) {
+/* the step loop's state between oracle_advance calls */
+struct oracle_sim {
     sim S;
-    memset(&S, 0, sizeof S);
-    sim* s = &S;
+    const uint32_t* site;
+    const double* tincub;
+    uint8_t* considered;
+    double Xcells, X;
+    uint32_t step, it, defrag_cnt, nnuc;
+    double dt0, Pmax0;
+};
+
+oracle_sim* oracle_create(const score_params* p, const uint32_t* grid, const double* defg_q, const double* defg_rho0, uint32_t ndefg,
+                          const double* rxg_q, const uint32_t* rxg_site, const double* rxg_tincub, uint32_t nrxg,
+                          const double* ptable) {
+    oracle_sim* o = calloc(1, sizeof *o);
+    if (!o) return NULL;
+    sim* s = &o->S;
     s->p = p; s->nx = p->nx; s->ny = p->ny; s->nz = p->nz; s->nxy = p->nx * p->ny;
     s->N = (uint64_t)p->nx * p->ny * p->nz;
     s->ndefg = ndefg; s->nrxg = nrxg; s->rq = rxg_q; s->dq = defg_q; s->ptab = ptable;
@@ -485,7 +495,9 @@ int oracle_run(const score_params* p, const uint32_t* grid, const double* defg_q
         s->f[L].rec = malloc(4ull * (s->f[L].reccap + 1));
         fl_grow(&s->f[L], 1024);
     }
-    uint8_t* considered = calloc(nrxg ? nrxg : 1, 1);
+    o->site = rxg_site;
+    o->tincub = rxg_tincub;
+    o->considered = calloc(nrxg ? nrxg : 1, 1);
 
     /* solve_RXGROWTH prologue, SCORE_Kernel.cpp:6513-6530 */
     phys* ph = &s->ph;
@@ -495,26 +507,31 @@ int oracle_run(const score_params* p, const uint32_t* grid, const double* defg_q
     ph->rhomax = rhomax_of(s->rho, s->defg_cnt, ndefg);
     ph_temperature(ph); ph_atomistic(ph); ph_mobilities(ph);
     ph->dt = ph_dtmin(ph);
-    if (out) out->dt0 = ph->dt;
+    o->dt0 = ph->dt;
     s->regPmax = 0.0;
-    uint32_t nnuc = place_nuclei(s, rxg_site, rxg_tincub, considered, 0.0);
+    o->nnuc = place_nuclei(s, rxg_site, rxg_tincub, o->considered, 0.0);
     if (s->regPmax >= ph->Pmax) ph->Pmax = s->regPmax;
-    if (out) { out->Pmax0 = ph->Pmax; out->n_nuclei = nnuc; }
+    o->Pmax0 = ph->Pmax;
+    return o;
+}
 
+int oracle_advance(oracle_sim* o, double x_target, uint32_t max_steps, oracle_step* trace, uint32_t trace_cap, oracle_out* out) {
+    sim* s = &o->S;
+    const score_params* p = s->p;
+    phys* ph = &s->ph;
     const double xt = x_target < 0 ? p->xmax : x_target;
-    double Xcells = 0.0, X = 0.0;
-    uint32_t step = 0, defrag_cnt = 0;
+    uint32_t done = 0;
     struct timespec t0, t1;
     clock_gettime(CLOCK_MONOTONIC, &t0);
-    for (uint32_t it = 0; it < 1000000u && s->status == SCORE_OK; it++) {
-        if ((Xcells >= (double)s->N) || (X > xt) || (it > p->nmax) || (ph->t > ph->tend) || (ph->t > p->tmax)) break;
-        if (max_steps && step >= max_steps) break;
-        uint32_t newnuc = rxg_tincub ? place_nuclei(s, rxg_site, rxg_tincub, considered, ph->t) : 0;
-        nnuc += newnuc;
-        if (p->defragmentation && defrag_cnt < p->n_defrag && Xcells >= p->defrag_x[defrag_cnt] * (double)s->N) {
+    for (; o->it < 1000000u && s->status == SCORE_OK; o->it++) {
+        if ((o->Xcells >= (double)s->N) || (o->X > xt) || (o->it > p->nmax) || (ph->t > ph->tend) || (ph->t > p->tmax)) break;
+        if (max_steps && done >= max_steps) break;
+        uint32_t newnuc = o->tincub ? place_nuclei(s, o->site, o->tincub, o->considered, ph->t) : 0;
+        o->nnuc += newnuc;
+        if (p->defragmentation && o->defrag_cnt < p->n_defrag && o->Xcells >= p->defrag_x[o->defrag_cnt] * (double)s->N) {
             defragment(&s->f[0]);
             defragment(&s->f[1]);
-            defrag_cnt++;
+            o->defrag_cnt++;
         }
         uint64_t Sv = 0;
         double dV = 0.0;
@@ -528,45 +545,74 @@ int oracle_run(const score_params* p, const uint32_t* grid, const double* defg_q
         double mymob = 0.0;
         if (s->regPmax >= mymob) mymob = s->regPmax;
         ph->Pmax = mymob;
-        Xcells = Xcells + (double)nfull;
-        X = (Xcells / (double)s->N);
-        ph->rhomax = rhomax_of(s->rho, s->defg_cnt, ndefg);
+        o->Xcells = o->Xcells + (double)nfull;
+        o->X = (o->Xcells / (double)s->N);
+        ph->rhomax = rhomax_of(s->rho, s->defg_cnt, s->ndefg);
         double rhomax_step = ph->rhomax, dt_used = ph->dt;
         ph->t += ph->dt;
         ph_temperature(ph); ph_atomistic(ph); ph_micro(ph); ph_mobilities(ph);
-        ph_recovery(ph, s->rho, s->rho0, ndefg);
+        ph_recovery(ph, s->rho, s->rho0, s->ndefg);
         ph->dt = ph_dtmin(ph);
-        step++;
-        if (trace && step <= trace_cap) {
-            oracle_step* o = &trace[step - 1];
-            memset(o, 0, sizeof *o);
-            o->step = step; o->n_nuclei = newnuc; o->t = ph->t; o->dt = ph->dt; o->dt_used = dt_used; o->Xcells = Xcells; o->X = X;
-            o->Sv = Sv; o->n_full = nfull; o->n_new = s->nnew; o->Pmax = ph->Pmax; o->rhomax = rhomax_step; o->dXstep = dV;
-            o->next_never[0] = s->f[0].never; o->next_never[1] = s->f[1].never;
-            o->n_recycled[0] = s->f[0].rec_first; o->n_recycled[1] = s->f[1].rec_first;
+        o->step++;
+        if (trace && done < trace_cap) {
+            oracle_step* r = &trace[done];
+            memset(r, 0, sizeof *r);
+            r->step = o->step; r->n_nuclei = newnuc; r->t = ph->t; r->dt = ph->dt; r->dt_used = dt_used; r->Xcells = o->Xcells; r->X = o->X;
+            r->Sv = Sv; r->n_full = nfull; r->n_new = s->nnew; r->Pmax = ph->Pmax; r->rhomax = rhomax_step; r->dXstep = dV;
+            r->next_never[0] = s->f[0].never; r->next_never[1] = s->f[1].never;
+            r->n_recycled[0] = s->f[0].rec_first; r->n_recycled[1] = s->f[1].rec_first;
         }
+        done++;
     }
     clock_gettime(CLOCK_MONOTONIC, &t1);
     if (out) {
-        out->n_steps = step; out->status = s->status;
+        out->n_steps = done; out->status = s->status; out->dt0 = o->dt0; out->Pmax0 = o->Pmax0; out->n_nuclei = o->nnuc;
         out->seconds = (double)(t1.tv_sec - t0.tv_sec) + 1e-9 * (double)(t1.tv_nsec - t0.tv_nsec);
     }
+    return s->status;
+}
+
+int oracle_done(const oracle_sim* o, double x_target) {
+    const sim* s = &o->S;
+    const double xt = x_target < 0 ? s->p->xmax : x_target;
+    return s->status != SCORE_OK || (o->Xcells >= (double)s->N) || (o->X > xt) || (o->it > s->p->nmax) || (s->ph.t > s->ph.tend) ||
+           (s->ph.t > s->p->tmax) || o->it >= 1000000u;
+}
+
+void oracle_finish(const oracle_sim* o, uint32_t* labels, uint32_t* rxg_counts, uint32_t* defg_counts) {
+    const sim* s = &o->S;
     /* final labels, ompcrit_clarify_status_infectedcells (SCORE_Io_Characterization.cpp:925-1000) */
     if (labels) {
         memcpy(labels, s->grid, s->N * 4);
         for (int L = 0; L < 2; L++) {
-            flist* f = &s->f[L];
+            const flist* f = &s->f[L];
             for (uint32_t c = 0; c < f->never; c++) {
                 if (!f->act[c]) continue;
                 uint32_t cell = (uint32_t)f->x[c] + s->nx * ((uint32_t)f->y[c] + s->ny * (uint32_t)f->z[c]);
-                labels[cell] = (f->fill[c] < 0.5) ? f->defg[c] : ndefg + f->rxg[c];
+                labels[cell] = (f->fill[c] < 0.5) ? f->defg[c] : s->ndefg + f->rxg[c];
             }
         }
     }
-    if (rxg_counts) memcpy(rxg_counts, s->rxg_cnt, nrxg * 4ull);
-    if (defg_counts) memcpy(defg_counts, s->defg_cnt, ndefg * 4ull);
-    int status = s->status;
+    if (rxg_counts) memcpy(rxg_counts, s->rxg_cnt, s->nrxg * 4ull);
+    if (defg_counts) memcpy(defg_counts, s->defg_cnt, s->ndefg * 4ull);
+}
+
+void oracle_destroy(oracle_sim* o) {
+    if (!o) return;
+    sim* s = &o->S;
     fl_free(&s->f[0]); fl_free(&s->f[1]);
-    free(s->grid); free(s->rxg_cnt); free(s->defg_cnt); free(s->rho); free(s->rho0); free(s->pcache); free(considered);
+    free(s->grid); free(s->rxg_cnt); free(s->defg_cnt); free(s->rho); free(s->rho0); free(s->pcache); free(o->considered);
+    free(o);
+}
+
+int oracle_run(const score_params* p, const uint32_t* grid, const double* defg_q, const double* defg_rho0, uint32_t ndefg,
+               const double* rxg_q, const uint32_t* rxg_site, const double* rxg_tincub, uint32_t nrxg, const double* ptable,
+               double x_target, uint32_t max_steps, oracle_step* trace, uint32_t trace_cap, uint32_t* labels,
+               uint32_t* rxg_counts, uint32_t* defg_counts, oracle_out* out) {
+    oracle_sim* o = oracle_create(p, grid, defg_q, defg_rho0, ndefg, rxg_q, rxg_site, rxg_tincub, nrxg, ptable);
+    if (!o) return SCORE_ERR_NOMEM;
+    const int status = oracle_advance(o, x_target, max_steps, trace, trace_cap, out);
+    oracle_finish(o, labels, rxg_counts, defg_counts);
+    oracle_destroy(o);
     return status;
 }

@@ -47,6 +47,20 @@ int oracle_run(const score_params* p, const uint32_t* grid, const double* defg_q
                double x_target, uint32_t max_steps, oracle_step* trace, uint32_t trace_cap, uint32_t* labels,
                uint32_t* rxg_counts, uint32_t* defg_counts, oracle_out* out);
 
+/* The same run in pieces, for timing bounded samples of a long run: create (the
+ * solve_RXGROWTH prologue and site-saturated nucleation), advance (the step loop until
+ * the stop rule with x_target, or max_steps more steps; out->n_steps and out->seconds
+ * cover this call only, trace rows are this call's steps), done (the stop rule holds),
+ * finish (labels and counts), destroy.  The input arrays must outlive the handle. */
+typedef struct oracle_sim oracle_sim;
+oracle_sim* oracle_create(const score_params* p, const uint32_t* grid, const double* defg_q, const double* defg_rho0, uint32_t ndefg,
+                          const double* rxg_q, const uint32_t* rxg_site, const double* rxg_tincub, uint32_t nrxg,
+                          const double* ptable);
+int oracle_advance(oracle_sim* o, double x_target, uint32_t max_steps, oracle_step* trace, uint32_t trace_cap, oracle_out* out);
+int oracle_done(const oracle_sim* o, double x_target);
+void oracle_finish(const oracle_sim* o, uint32_t* labels, uint32_t* rxg_counts, uint32_t* defg_counts);
+void oracle_destroy(oracle_sim* o);
+
 /* P(rxg,defg) by the reference's formula, for pinning the table against the reference */
 double oracle_mobility_weight(const score_params* p, const double* qr, const double* qd);
 

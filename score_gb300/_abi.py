@@ -162,6 +162,28 @@ def load(path: str | Path | None = None) -> C.CDLL:
     return lib
 
 
+# entry points of the host-only library (host_api.cpp, host_generate.cpp)
+HOST_FUNCTIONS = ("score_params_default", "score_uds_read", "score_mobility_weight", "score_gen_default", "score_generate_domain")
+_host = None
+
+
+def load_host() -> C.CDLL:
+    """Load libscore_host.so (parameters, host mobility weight, domain generator; no CUDA)."""
+    global _host
+    if _host is not None:
+        return _host
+    from .build import host_library_path
+    path = host_library_path()
+    if not path.exists():
+        raise RuntimeError(f"{path} is missing: run score_gb300.build.build() (or __graft_entry__.build()) first")
+    lib = C.CDLL(str(path))
+    for name in HOST_FUNCTIONS:
+        fn = getattr(lib, name)
+        fn.restype, fn.argtypes = SIGNATURES[name]
+    _host = lib
+    return lib
+
+
 class ScoreError(RuntimeError):
     def __init__(self, status: int, msg: str):
         super().__init__(f"score_gb300 status {status}: {msg}")

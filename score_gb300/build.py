@@ -1,9 +1,15 @@
-"""Build the in-tree native library libscore_gb300.so (CUDA sm_103a + host C++).
+"""Build the in-tree native libraries (score_gb300/_lib/).
 
-The library is built next to the package (score_gb300/_lib/) so the process that
-uses it loads it from the source tree.  Three translation units compile in
-parallel; -ffp-contract=off / -fmad=false keep FP64 rounding identical to the
-reference's x86/aarch64 builds (no fused multiply-add contraction anywhere).
+libscore_gb300.so  the CUDA sm_103a growth step and its host engine, plus the host
+                   entry points (.uds parameters, host mobility weight, generator);
+libscore_host.so   the host entry points alone (no CUDA): input preparation for the
+                   CPU timing of the reference's algorithm, which must not load the
+                   CUDA library.
+
+Both are built next to the package so the process that uses them loads them from the
+source tree.  The translation units compile in parallel; -ffp-contract=off /
+-fmad=false keep FP64 rounding identical to the reference's x86/aarch64 builds (no
+fused multiply-add contraction anywhere).
 """
 from __future__ import annotations
 
@@ -18,6 +24,8 @@ HERE = Path(__file__).resolve().parent
 CSRC = HERE / "csrc"
 LIBDIR = HERE / "_lib"
 LIBNAME = "libscore_gb300.so"
+HOSTLIB = "libscore_host.so"
+HOST_SRCS = ("host_api.cpp", "host_model.cpp", "host_generate.cpp")  # the host-only library's sources
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
 
@@ -38,12 +46,18 @@ def library_path() -> Path:
     return LIBDIR / LIBNAME
 
 
+def host_library_path() -> Path:
+    return LIBDIR / HOSTLIB
+
+
 def build(force: bool = False, verbose: bool = False) -> Path:
-    """Compile libscore_gb300.so if any source is newer than it; return its path."""
+    """Compile libscore_gb300.so and libscore_host.so if any source is newer than them;
+    return the CUDA library's path."""
     out = library_path()
+    hout = host_library_path()
     srcs = sorted(CSRC.glob("*.cu")) + sorted(CSRC.glob("*.cpp"))
     deps = srcs + sorted(CSRC.glob("*.h")) + sorted(CSRC.glob("*.cuh")) + [HERE.parent / "include" / "score_gb300.h"]
-    if not force and out.exists() and all(out.stat().st_mtime >= p.stat().st_mtime for p in deps):
+    if not force and all(o.exists() and all(o.stat().st_mtime >= p.stat().st_mtime for p in deps) for o in (out, hout)):
         return out
     LIBDIR.mkdir(exist_ok=True)
     nvcc = nvcc_path()
@@ -63,6 +77,9 @@ def build(force: bool = False, verbose: bool = False) -> Path:
     tmp = out.with_suffix(".so.tmp")
     _run([nvcc, *ARCH, "-shared", "-o", str(tmp), *[str(o) for _, o in jobs], "-lcudart", "-lpthread"])
     os.replace(tmp, out)
+    htmp = hout.with_suffix(".so.tmp")
+    _run([nvcc, "-shared", "-o", str(htmp), *[str(objdir / (Path(n).stem + ".o")) for n in HOST_SRCS], "-lpthread"])
+    os.replace(htmp, hout)
     return out
 
 

@@ -1531,26 +1531,6 @@ const char* score_status_string(int s) {
     }
 }
 
-int score_params_default(score_params* out) {
-    if (!out) return SCORE_ERR_ARG;
-    params_default(out);
-    return SCORE_OK;
-}
-
-int score_uds_read(const char* path, score_params* out) {
-    if (!path || !out) return SCORE_ERR_ARG;
-    char buf[512];
-    int s = uds_read(path, out, buf, sizeof buf);
-    if (s != SCORE_OK) fprintf(stderr, "score_uds_read: %s\n", buf);
-    return s;
-}
-
-int score_mobility_weight(const score_params* p, const double* rq, const double* dq, double* P) {
-    if (!p || !rq || !dq || !P) return SCORE_ERR_ARG;
-    *P = mobility_weight(*p, rq, dq);
-    return SCORE_OK;
-}
-
 const char* score_last_error(const score_ctx* c) { return c ? c->err.c_str() : "null context"; }
 
 int score_create(score_ctx** out, const score_params* p, int device) {
@@ -2014,9 +1994,9 @@ int score_batch_autotune(score_batch* b, double x_target, uint32_t max_steps, sc
 namespace {
 
 // Static scratch of the entry point: 256 B of header + one word per table row.
-//   word 0          blocks of the current launch that have finished.  MUST be 0 when a
-//                   launch starts: it is 0 after module load, and the last block of
-//                   every launch sets it back to 0.
+//   word 0          blocks of the current launch that have finished.  Cleared on the
+//                   stream before every launch (a launch that was cut short could leave
+//                   it non-zero), and set back to 0 by the last block of each launch.
 //   words 32 .. 32 + nrxg - 1   maximum P of each row (FP64 bits), written before read.
 constexpr uint32_t kTableMaxRows = 65536;
 constexpr uint32_t kTableHeaderWords = 32;
@@ -2029,20 +2009,23 @@ struct TableArgs {
 };
 
 __device__ double d_weight(const DomainArgs& A, const TableArgs& t, const double pr[4], const double qd[4]) {
-    const double theta = d_disori(A, pr, qd, nullptr);
-    if (t.model == SCORE_MOBILITY_ROLLETT_HOLM)
-        return 1.0 - (t.rh_cut * exp(-1.0 * t.rh_trans * pow(theta / t.lagb, t.rh_expo)));
-    if (theta <= t.lagb) return -1.0;
-    // disorientation quaternion of the best symmetry candidate, components sorted descending
+    // the 24 Grimmer candidates once: their largest |component| gives the disorientation
+    // angle and, for the Sebald-Gottstein weight, the candidate whose axis is compared
+    // with 40deg<111>
     double c[6][4];
     d_grimmer(A, pr, qd, c);
     int mi = 0;
-    double mx = 0.0;
+    double om = 0.0;
 #pragma unroll
     for (int i = 0; i < 6; ++i)
 #pragma unroll
         for (int j = 0; j < 4; ++j)
-            if (fabs(c[i][j]) > mx) { mx = fabs(c[i][j]); mi = i; }
+            if (fabs(c[i][j]) > om) { om = fabs(c[i][j]); mi = i; }
+    const double theta = om < (1.0 - 5.0e-16) ? 2.0 * acos(om) : 0.0;
+    if (t.model == SCORE_MOBILITY_ROLLETT_HOLM)
+        return 1.0 - (t.rh_cut * exp(-1.0 * t.rh_trans * pow(theta / t.lagb, t.rh_expo)));
+    if (theta <= t.lagb) return -1.0;
+    // disorientation quaternion of the best symmetry candidate, components sorted descending
     double s[4] = {fabs(c[mi][0]), fabs(c[mi][1]), fabs(c[mi][2]), fabs(c[mi][3])};
 #pragma unroll
     for (int i = 0; i < 3; ++i)
@@ -2146,6 +2129,13 @@ extern "C" int score_mobility_table_noalloc(const score_params* p, const double*
     t.rh_cut = p->RH_cut;
     t.rh_trans = p->RH_trans;
     t.rh_expo = p->RH_exponent;
-    k_mobility_table<<<nrxg, 256, 0, (cudaStream_t)stream>>>(t, d_rxg_quat, nrxg, d_defg_quat, ndefg, d_table, d_pmax, scratch);
-    return cudaGetLastError() == cudaSuccess ? SCORE_OK : SCORE_ERR_CUDA;
+    cudaStream_t st = (cudaStream_t)stream;
+    // the completion counter starts at 0 whatever an earlier launch left behind
+    if (cudaMemsetAsync(scratch, 0, sizeof(unsigned long long), st) != cudaSuccess) return SCORE_ERR_CUDA;
+    // the launch's own status (not cudaGetLastError, which would also report, and clear,
+    // an error left behind by the caller's earlier work)
+    void* args[] = {(void*)&t, (void*)&d_rxg_quat, (void*)&nrxg, (void*)&d_defg_quat, (void*)&ndefg, (void*)&d_table,
+                    (void*)&d_pmax, (void*)&scratch};
+    const cudaError_t e = cudaLaunchKernel((const void*)k_mobility_table, dim3(nrxg), dim3(256), args, 0, st);
+    return e == cudaSuccess ? SCORE_OK : SCORE_ERR_CUDA;
 }

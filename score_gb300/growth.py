@@ -29,17 +29,22 @@ def lib():
     return _abi.load()
 
 
+def host_lib():
+    """The host-only library: parameters, host weights and the generator never need CUDA."""
+    return _abi.load_host()
+
+
 # ---------------------------------------------------------------- parameters
 def default_params() -> Params:
     p = Params()
-    lib().score_params_default(C.byref(p))
+    host_lib().score_params_default(C.byref(p))
     return p
 
 
 def read_uds(path: str | Path) -> Params:
     """Parse a SCORE .uds input file (ensembleHdl::init_parameter semantics)."""
     p = Params()
-    s = lib().score_uds_read(str(path).encode(), C.byref(p))
+    s = host_lib().score_uds_read(str(path).encode(), C.byref(p))
     if s != _abi.OK:
         raise ScoreError(s, f"cannot read {path}")
     return p
@@ -234,7 +239,7 @@ def generate_domain(nx: int, ny: int, nz: int, ngrains: int, nnuclei: int, seed:
     gb_fraction, nucleation_rate.
     """
     g = GenParams()
-    lib().score_gen_default(C.byref(g))
+    host_lib().score_gen_default(C.byref(g))
     g.nx, g.ny, g.nz, g.ngrains, g.nnuclei, g.seed = nx, ny, nz, ngrains, nnuclei, seed
     for k, v in kw.items():
         if k == "aspect":
@@ -248,7 +253,7 @@ def generate_domain(nx: int, ny: int, nz: int, ngrains: int, nnuclei: int, seed:
     rq = np.empty((nnuclei, 4), dtype=np.float64)
     site = np.empty(nnuclei, dtype=np.uint32)
     tinc = np.empty(nnuclei, dtype=np.float64)
-    s = lib().score_generate_domain(C.byref(g), _ptr(grid), _ptr(dq), _ptr(rho), _ptr(rq), _ptr(site), _ptr(tinc))
+    s = host_lib().score_generate_domain(C.byref(g), _ptr(grid), _ptr(dq), _ptr(rho), _ptr(rq), _ptr(site), _ptr(tinc))
     if s != _abi.OK:
         raise ScoreError(s, "domain generation failed")
     return Domain(nx, ny, nz, grid, dq, rho, rq, site, tinc)

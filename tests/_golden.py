@@ -38,3 +38,40 @@ def first_difference(a: np.ndarray, b: np.ndarray) -> str:
         return f"lengths {len(a)} vs {len(b)}"
     i = int(np.argmax(a[:m] != b[:m]))
     return f"step {i}: {a[i]!r} vs {b[i]!r}"
+
+
+def config_cases() -> list[str]:
+    """Fixtures of the benchmark configurations (config0_128, config1_512)."""
+    return sorted(p.stem for p in GOLDEN.glob("config*_*.npz"))
+
+
+def input_digest(d) -> str:
+    """SHA-256 over a domain's inputs, as tests/golden/make_golden.py computes it."""
+    import hashlib
+    h = hashlib.sha256()
+    for a in (d.grid, d.defg_quat, d.defg_rho0, d.rxg_quat, d.rxg_site, d.rxg_tincub):
+        h.update(np.ascontiguousarray(a).tobytes())
+    return h.hexdigest()
+
+
+def labels_digest(labels) -> str:
+    import hashlib
+    return hashlib.sha256(np.ascontiguousarray(labels, dtype=np.uint32).tobytes()).hexdigest()
+
+
+def load_config(name: str, tmp_path: Path):
+    """(params, domain, golden dict) of a benchmark-configuration fixture: the domain is
+    regenerated from the stored generator arguments and checked against the stored
+    input digest before anything is compared."""
+    z = np.load(GOLDEN / f"{name}.npz")
+    uds = tmp_path / f"{name}.uds"
+    uds.write_text(str(z["uds"]))
+    p = sg.read_uds(uds)
+    n, ng, nn, seed = (int(v) for v in z["gen"])
+    d = sg.generate_domain(n, n, n, ng, nn, seed=seed)
+    assert input_digest(d) == str(z["input_sha256"]), "the generator no longer reproduces the fixture's inputs"
+    g = {k: z[k] for k in TRACE_FIELDS}
+    g["labels_sha256"] = str(z["labels_sha256"])
+    g["rxg_counts"] = z["rxg_counts"]
+    g["defg_counts"] = z["defg_counts"]
+    return p, d, g

@@ -11,7 +11,19 @@ if str(ROOT) not in sys.path:
 
 def pytest_configure(config):
     config.addinivalue_line("markers", "gpu: needs a CUDA device (GB300); runs the sm_103a kernels")
-    config.addinivalue_line("markers", "slow: longer CPU cases (reference runs at 128^3)")
+    config.addinivalue_line("markers", "slow: long cases (the 512^3 benchmark domain); on the CPU they run only with "
+                                       "SCORE_SLOW_TESTS=1, on the GPU always")
+
+
+def pytest_collection_modifyitems(config, items):
+    """CPU cases marked slow (minutes of single-threaded oracle work) run only on request;
+    GPU cases marked slow take seconds on the device and always run."""
+    if os.environ.get("SCORE_SLOW_TESTS") == "1":
+        return
+    skip = pytest.mark.skip(reason="slow CPU case: set SCORE_SLOW_TESTS=1 to run it")
+    for item in items:
+        if "slow" in item.keywords and "gpu" not in item.keywords:
+            item.add_marker(skip)
 
 
 @pytest.fixture(scope="session")

@@ -11,8 +11,17 @@ reference's per-step trace and final labels.
 The ptab case stores the reference's mobility weights P(rxg, defg) for every pair
 (reg_calc_mobilityweight, SCORE_Kernel.cpp:2460-2527) of a small grain set.
 
-Run from the repository root where the reference sources exist:
-    python tests/golden/make_golden.py
+The two benchmark-configuration cases run the reference on the full-size domains of the
+benchmark: config 0 (128^3, 500 Voronoi grains, 200 site-saturated nuclei) and config 1
+(512^3, 20,000 grains, 50,000 nuclei: the headline workload's domain, seed 0).  Their
+inputs are too large to store, so the fixture keeps the generator arguments and a
+SHA-256 of the generated inputs (the generator gives identical bits on x86-64 and
+aarch64), the reference's full per-step trace, a SHA-256 of its final labels and its
+per-grain cell counts.
+
+Run from the repository root, with the reference sources at $SCORE_REFERENCE:
+    python tests/golden/make_golden.py            # every case
+    python tests/golden/make_golden.py config0    # only the named cases
 """
 from __future__ import annotations
 
@@ -45,6 +54,8 @@ CASES = {
                         {"ori_mode": 1, "ncomp": 3, "scatter_deg": 10.0, "rho_mode": 1, "rho_lo": 1e14, "rho_hi": 5e15}),
 }
 PTAB = (40, 80, 111)  # nrxg, ndefg, seed
+# benchmark configurations: name -> (edge, grains, nuclei, seed)
+CONFIGS = {"config0": (128, 500, 200, 0), "config1": (512, 20000, 50000, 0)}
 
 
 def narrow(a: np.ndarray) -> np.ndarray:
@@ -75,6 +86,34 @@ def make_case(name: str, kw: dict, geo: tuple, gkw: dict, wd: Path) -> Path:
     return out
 
 
+def input_digest(d: sg.Domain) -> str:
+    """SHA-256 over the generated inputs (grid, orientations, rho, nucleus sites and times)."""
+    import hashlib
+    h = hashlib.sha256()
+    for a in (d.grid, d.defg_quat, d.defg_rho0, d.rxg_quat, d.rxg_site, d.rxg_tincub):
+        h.update(np.ascontiguousarray(a).tobytes())
+    return h.hexdigest()
+
+
+def make_config(name: str, wd: Path) -> Path:
+    import hashlib
+    n, ng, nn, seed = CONFIGS[name]
+    d = sg.generate_domain(n, n, n, ng, nn, seed=seed)
+    spec = sg.UdsSpec(nx=n, ny=n, nz=n)
+    uds = spec.write(wd / f"{name}.uds")
+    r = oracle.run_ref("loop", uds, d, workdir=wd / name)
+    tr = r["trace"][1:]
+    out = HERE / f"{name}_{n}.npz"
+    np.savez_compressed(
+        out, uds=np.array(spec.text()), gen=np.array([n, ng, nn, seed], dtype=np.int64), input_sha256=np.array(input_digest(d)),
+        t=tr["t"], dt=tr["dt"], Xcells=tr["Xcells"], Sv=tr["Sv"], n_full=tr["nfull"], Pmax=tr["Pmax"], rhomax=tr["rhomax"],
+        labels_sha256=np.array(hashlib.sha256(np.ascontiguousarray(r["labels"], dtype=np.uint32).tobytes()).hexdigest()),
+        rxg_counts=np.array([r["rxg"].get(i, 0) for i in range(d.nrxg)], dtype=np.uint32),
+        defg_counts=np.array([r["defg"].get(i, 0) for i in range(d.ndefg)], dtype=np.uint32))
+    print(f"{out.name}: {len(tr)} steps, X={tr['Xcells'][-1] / d.ncells:.4f}, {out.stat().st_size // 1024} KiB")
+    return out
+
+
 def make_ptab(wd: Path) -> Path:
     nrxg, ndefg, seed = PTAB
     d = sg.generate_domain(50, 50, 50, ndefg, nrxg, seed=seed)
@@ -95,11 +134,17 @@ def main() -> None:
     if not oracle.reference_available():
         sys.exit("the reference sources are required to generate the golden fixtures")
     oracle.build_ref()
+    only = set(sys.argv[1:])
     with tempfile.TemporaryDirectory() as td:
         wd = Path(td)
         for name, (kw, geo, gkw) in CASES.items():
-            make_case(name, kw, geo, gkw, wd)
-        make_ptab(wd)
+            if not only or name in only:
+                make_case(name, kw, geo, gkw, wd)
+        if not only or "ptab" in only:
+            make_ptab(wd)
+        for name in CONFIGS:
+            if not only or name in only:
+                make_config(name, wd)
 
 
 if __name__ == "__main__":

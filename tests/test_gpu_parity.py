@@ -195,3 +195,24 @@ def test_gpu_reproduces_reference_golden(gpu, tmp_path, name):
         assert np.array_equal(a, g[f]), f"{f}: {first_difference(a, g[f])}"
     assert np.array_equal(lab.ravel(), g["labels"]), "final labels"
     assert np.array_equal(rc, g["rxg_counts"]) and np.array_equal(dc, g["defg_counts"])
+
+
+# ---------------------------------------------------------------- the benchmark configurations
+from _golden import config_cases, labels_digest, load_config  # noqa: E402
+
+
+@pytest.mark.parametrize("name", ["config0_128", pytest.param("config1_512", marks=pytest.mark.slow)])
+def test_gpu_reproduces_reference_at_benchmark_size(gpu, tmp_path, name):
+    """The benchmark configurations at their full sizes against the reference's own run of
+    them: config 0 (128^3, 500 grains, 200 nuclei) and config 1, the headline workload's
+    512^3 domain (20,000 grains, 50,000 nuclei).  Every step's t, dt, X cells, Sv, full
+    cells, P max and rho max, the final labels (SHA-256 of all N labels) and every grain's
+    cell count, bit for bit."""
+    assert name in config_cases()
+    p, d, g = load_config(name, tmp_path)
+    tr, lab, rc, dc = run_gpu(p, d)
+    for f in TRACE_FIELDS:
+        a = np.array([getattr(s, f) for s in tr])
+        assert np.array_equal(a, g[f]), f"{f}: {first_difference(a, g[f])}"
+    assert labels_digest(lab) == g["labels_sha256"], "final labels"
+    assert np.array_equal(rc, g["rxg_counts"]) and np.array_equal(dc, g["defg_counts"])

@@ -8,7 +8,8 @@ import pytest
 
 import oracle
 import score_gb300 as sg
-from _golden import GOLDEN, TRACE_FIELDS, first_difference, growth_cases, load_case
+from _golden import (GOLDEN, TRACE_FIELDS, config_cases, first_difference, growth_cases, labels_digest, load_case,
+                     load_config)
 
 
 @pytest.mark.parametrize("name", growth_cases())
@@ -26,6 +27,39 @@ def test_oracle_reproduces_reference(built, tmp_path, name):
 def test_golden_set_is_complete():
     assert len(growth_cases()) >= 10
     assert (GOLDEN / "mobility_weights.npz").exists()
+    assert config_cases() == ["config0_128", "config1_512"]
+
+
+@pytest.mark.parametrize("name", ["config0_128", pytest.param("config1_512", marks=pytest.mark.slow)])
+def test_oracle_reproduces_reference_at_benchmark_size(built, tmp_path, name):
+    """The benchmark configurations themselves (128^3 / 500 grains / 200 nuclei, and the
+    512^3 / 20,000 grains / 50,000 nuclei headline domain), run by the reference's growth
+    loop: per-step trace, final labels (SHA-256) and per-grain counts, bit for bit."""
+    p, d, g = load_config(name, tmp_path)
+    r = oracle.run(p, d)
+    assert r["status"] == 0
+    tr = r["trace"]
+    for f in TRACE_FIELDS:
+        assert np.array_equal(tr[f], g[f]), f"{f}: {first_difference(tr[f], g[f])}"
+    assert labels_digest(r["labels"]) == g["labels_sha256"], "final labels"
+    assert np.array_equal(r["rxg_counts"], g["rxg_counts"]) and np.array_equal(r["defg_counts"], g["defg_counts"])
+
+
+@pytest.mark.skipif(not oracle.reference_available(), reason="reference sources not found (SCORE_REFERENCE unset, no prebuilt harness)")
+@pytest.mark.parametrize("name", ["base", "rollett_holm"])
+def test_harness_replay_matches_unmodified_solve(built, tmp_path, name):
+    """The fixtures come from the harness's replay of solve_RXGROWTH (without its logging);
+    the unmodified caHdl::solve_RXGROWTH (SCORE_Kernel.cpp:6497-6792) must end at the same
+    time (bit for bit), after the same number of steps, with the same per-grain counts."""
+    p, d, g = load_case(name, tmp_path)
+    uds = tmp_path / f"{name}.uds"
+    asis = oracle.run_ref("asis", uds, d, workdir=tmp_path / "asis")
+    loop = oracle.run_ref("loop", uds, d, workdir=tmp_path / "loop")
+    assert asis["t_end"] == loop["t_end"], (asis["t_end"], loop["t_end"])
+    assert int(asis["step_end"]) == int(loop["steps"]) == len(g["t"])
+    assert float.fromhex(asis["t_end"]) == g["t"][-1]
+    assert asis["rxg"] == loop["rxg"] and asis["defg"] == loop["defg"]
+    assert [asis["rxg"][i] for i in range(d.nrxg)] == list(g["rxg_counts"])
 
 
 @pytest.mark.parametrize("model", [1, 2])
@@ -95,3 +129,20 @@ def test_host_weight_matches_oracle_on_random_and_boundary_pairs(built, tmp_path
     orc = np.array([oracle.mobility_weight(p, qr[i], qd[i]) for i in range(len(qr))])
     assert np.array_equal(host.view(np.uint64), orc.view(np.uint64))
     assert (host == -1.0).any() and (host == 0.0).any() and ((host > 0.0) & (host < 1.0)).any()
+
+
+def test_oracle_in_pieces_equals_one_run(built, tmp_path):
+    """The bounded-sample form of the oracle (advance in pieces, as the CPU timing of the
+    benchmark uses it) gives exactly the one-call run: trace, labels, counts."""
+    p, d, g = load_case("base", tmp_path)
+    whole = oracle.run(p, d)
+    sim = oracle.Sim(p, d)
+    parts = [sim.advance(x_target=0.99 * k / 7) for k in range(1, 8)] + [sim.advance(max_steps=5), sim.advance()]
+    assert sim.done()
+    tr = np.concatenate([q["trace"] for q in parts])
+    assert all(q["status"] == 0 for q in parts)
+    assert np.array_equal(tr, whole["trace"])
+    fin = sim.finish()
+    sim.close()
+    assert np.array_equal(fin["labels"], whole["labels"]) and np.array_equal(fin["labels"], g["labels"])
+    assert np.array_equal(fin["rxg_counts"], whole["rxg_counts"]) and np.array_equal(fin["defg_counts"], whole["defg_counts"])
