@@ -22,7 +22,7 @@
 extern "C" {
 #endif
 
-#define SCORE_ABI_VERSION 3
+#define SCORE_ABI_VERSION 4
 
 /* status codes */
 #define SCORE_OK                     0
@@ -106,6 +106,12 @@ typedef struct score_params {
     int32_t precision;                /* SCORE_PRECISION_* */
     int32_t border_policy;            /* SCORE_BORDER_* */
     int32_t reserved;
+    /* on-the-fly characterization (SCORE_OnTheFlyCharacterization.cpp:635-650) */
+    uint32_t n_logpoints;             /* SingleGrainVolOverTime X logpoints (sorted; X read as float, as the reference) */
+    double logpoint_x[SCORE_MAX_TABLE];
+    uint32_t rxarea_threshold;        /* RXAreaThreshold (GB300Options): rx grain sections of fewer cells are not
+                                         counted in the RX area profile; 13 in log_OUTPUT_Diehl */
+    uint32_t reserved2;
 } score_params;
 
 /* per-step scalars (the master block of solve_RXGROWTH, SCORE_Kernel.cpp:6688-6740) */
@@ -128,6 +134,14 @@ typedef struct score_step_stats {
     uint32_t p_misses;       /* mobility weights computed on the host this step */
     uint32_t reserved;
 } score_step_stats;
+
+/* one grain-evolution snapshot (loginfo_grainevo_ca, src/SCORE_Kernel.h:642-651) */
+typedef struct score_grainevo_info {
+    double t;             /* time at the start of the logged step [s]: the reference logs before t += dt */
+    double X;             /* recrystallized fraction after the step */
+    uint32_t step;        /* steps completed before the logged one */
+    uint32_t Sv;          /* front cells updated in the logged step (32-bit, as the reference logs it) */
+} score_grainevo_info;
 
 /* library */
 int  score_abi_version(void);
@@ -272,6 +286,44 @@ int  score_batch_get_timing(score_batch* b, score_timing* out);
 int  score_batch_get_tune(score_batch* b, score_tune* out);
 int  score_batch_set_tune(score_batch* b, const score_tune* t);
 int  score_batch_autotune(score_batch* b, double x_target, uint32_t max_steps, score_tune* out);
+
+/*
+ * On-the-fly characterization (caHdl::log_OUTPUT_Diehl, src/SCORE_OnTheFlyCharacterization.cpp:635-650).
+ * After a step whose X reaches the next SingleGrainVolOverTime logpoint (params n_logpoints /
+ * logpoint_x; at most one snapshot per step, as the reference) the device records every grain's
+ * cell count (log_grainevo, :478-531: deformed grains, then rx grains) and the RX area profile
+ * (log_rxareaprofile(threshold), :274-384: per z slice the cells of the rx grains whose section has
+ * at least params rxarea_threshold cells, then the slice's other cells; labels by the clarify rule).
+ * The log belongs to the last run (score_restart / score_load_domain clear it).
+ *   counts  ndefg + nrxg values, or NULL      rxarea  2 nz values (rx, rest per slice), or NULL
+ */
+int  score_grainevo_count(score_ctx* c, uint32_t* n);
+int  score_grainevo(score_ctx* c, uint32_t i, score_grainevo_info* info, uint32_t* counts, uint32_t* rxarea);
+int  score_batch_grainevo_count(score_batch* b, uint32_t d, uint32_t* n);
+int  score_batch_grainevo(score_batch* b, uint32_t d, uint32_t i, score_grainevo_info* info, uint32_t* counts,
+                          uint32_t* rxarea);
+
+/*
+ * Ensemble post-processing on the device (ensembleHdl::postprocess_*, src/SCORE_SolitaryUnitAveraging.cpp)
+ * over the grain-evolution logs of a batch's domains (or of one context, an ensemble of one).
+ * Time slots: t_n = (n + 1) tmax / (nslots - 1), n < nslots, tmax the latest end time of the domains
+ * (postprocess_init + postprocess_initrediscrtimes, :50-80, 510-540).  A grain's volume at t_n is
+ * caHdl::get_interpCellCount (:1304-1365): its final count at or after the end of its run, else
+ * linear between the snapshots around t_n.  Sums run in the reference's order, so FP64 results are
+ * the reference's bits.
+ *   kinetics   rxvol[n] = sum over domains of (cells - interpolated deformed volume) (:546-670);
+ *              boxvol = cells of all domains; X(t_n) = rxvol[n] / boxvol
+ *   texture    vol[n nclass + k] = interpolated volume of the grains of orientation class k, deformed
+ *              and rx (:673-804); grain_class holds every domain's ndefg + nrxg classes in domain
+ *              order, each < nclass <= 32
+ *   grain sizes  every domain's rx grains' final cell counts, in domain order (the final grain-size
+ *              distribution's volumes, :808-905)
+ */
+int  score_rediscr_kinetics(score_ctx* c, uint32_t nslots, double* t_out, double* rxvol_out, double* boxvol_out);
+int  score_batch_rediscr_kinetics(score_batch* b, uint32_t nslots, double* t_out, double* rxvol_out, double* boxvol_out);
+int  score_batch_rediscr_texture(score_batch* b, uint32_t nslots, const uint32_t* grain_class, uint32_t nclass,
+                                 double* t_out, double* vol_out);
+int  score_batch_final_grain_sizes(score_batch* b, uint32_t* rx_cells);
 
 /* FP64 mobility weight P(rxg,defg) on the host, the reference's formula
  * (SCORE_Kernel.cpp:2460-2527, SCORE_Math.cpp:558-622,1067-1130) */

@@ -91,6 +91,16 @@ def _load():
         lib.oracle_done.argtypes = [C.c_void_p, C.c_double]
         lib.oracle_finish.argtypes = [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]
         lib.oracle_destroy.argtypes = [C.c_void_p]
+        lib.oracle_time.restype = C.c_double
+        lib.oracle_time.argtypes = [C.c_void_p]
+        lib.oracle_log_count.restype = C.c_uint32
+        lib.oracle_log_count.argtypes = [C.c_void_p]
+        lib.oracle_log_get.restype = C.c_int
+        lib.oracle_log_get.argtypes = [C.c_void_p, C.c_uint32] + [C.c_void_p] * 6
+        lib.oracle_interp_count.restype = C.c_double
+        lib.oracle_interp_count.argtypes = [C.c_void_p, C.c_uint32, C.c_double]
+        lib.oracle_rediscr_kinetics.argtypes = [C.c_void_p, C.c_uint32, C.c_uint32, C.c_void_p, C.c_void_p, C.c_void_p]
+        lib.oracle_rediscr_macrotexture.argtypes = [C.c_void_p, C.c_uint32, C.c_uint32, C.c_uint32, C.c_void_p, C.c_void_p]
         _lib = lib
     return _lib
 
@@ -155,6 +165,22 @@ class Sim:
         self._lib.oracle_finish(self._h, _p(labels), _p(rc), _p(dc))
         return {"labels": labels, "rxg_counts": rc[: self.nrxg], "defg_counts": dc}
 
+    def time(self) -> float:
+        return self._lib.oracle_time(self._h)
+
+    def grainevo(self, nz: int) -> list[dict]:
+        """Snapshots of the grain-evolution log taken so far: t, X, step, Sv, counts, area [nz, 2]."""
+        out = []
+        G = self.ndefg + self.nrxg
+        for i in range(self._lib.oracle_log_count(self._h)):
+            t, X = C.c_double(), C.c_double()
+            st, sv = C.c_uint32(), C.c_uint32()
+            cnt = np.empty(G, dtype=np.uint32)
+            area = np.empty((nz, 2), dtype=np.uint32)
+            self._lib.oracle_log_get(self._h, i, C.byref(t), C.byref(X), C.byref(st), C.byref(sv), _p(cnt), _p(area))
+            out.append({"t": t.value, "X": X.value, "step": st.value, "Sv": sv.value, "counts": cnt, "area": area})
+        return out
+
     def close(self) -> None:
         if self._h:
             self._lib.oracle_destroy(self._h)
@@ -162,6 +188,50 @@ class Sim:
 
     def __del__(self):
         self.close()
+
+
+class OracleEvo(C.Structure):
+    _fields_ = [("ndefg", C.c_uint32), ("nrxg", C.c_uint32), ("nsnap", C.c_uint32), ("t", C.c_void_p), ("counts", C.c_void_p),
+                ("final_counts", C.c_void_p), ("tsimend", C.c_double), ("nboxvol", C.c_double), ("grain_class", C.c_void_p)]
+
+
+def _evos(domains):
+    """ctypes descriptors of grain-evolution logs: dicts with ndefg, nrxg, t (snapshots), counts
+    [nsnap, G], final [G], tsimend, cells, optionally cls [G]; arrays kept alive with them."""
+    keep, arr = [], (OracleEvo * len(domains))()
+    for k, d in enumerate(domains):
+        t = np.ascontiguousarray(d["t"], dtype=np.float64)
+        cnt = np.ascontiguousarray(d["counts"], dtype=np.uint32)
+        fin = np.ascontiguousarray(d["final"], dtype=np.uint32)
+        cls = None if d.get("cls") is None else np.ascontiguousarray(d["cls"], dtype=np.uint32)
+        keep += [t, cnt, fin, cls]
+        arr[k] = OracleEvo(d["ndefg"], d["nrxg"], len(t), _p(t), _p(cnt), _p(fin), d["tsimend"], float(d["cells"]), _p(cls))
+    return arr, keep
+
+
+def interp_count(domain: dict, gid: int, when: float) -> float:
+    """caHdl::get_interpCellCount restated (SCORE_SolitaryUnitAveraging.cpp:1304-1365)."""
+    arr, keep = _evos([domain])
+    return _load().oracle_interp_count(arr, gid, when)
+
+
+def rediscr_kinetics(domains: list, nslots: int):
+    """postprocess_rediscr_kinetics restated: (t, rx volume per slot, box volume)."""
+    arr, keep = _evos(domains)
+    t = np.empty(nslots, dtype=np.float64)
+    v = np.empty(nslots, dtype=np.float64)
+    box = C.c_double()
+    _load().oracle_rediscr_kinetics(arr, len(domains), nslots, _p(t), _p(v), C.byref(box))
+    return t, v, box.value
+
+
+def rediscr_texture(domains: list, nslots: int, nclass: int):
+    """postprocess_rediscr_macrotexture restated: (t, volume[nslots, nclass])."""
+    arr, keep = _evos(domains)
+    t = np.empty(nslots, dtype=np.float64)
+    v = np.empty((nslots, nclass), dtype=np.float64)
+    _load().oracle_rediscr_macrotexture(arr, len(domains), nslots, nclass, _p(t), _p(v))
+    return t, v
 
 
 def mobility_weight(params, qr, qd) -> float:

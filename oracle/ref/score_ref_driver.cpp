@@ -21,6 +21,16 @@
  *           t, dt, Xcells, Sv, full-cell count, P_max, rho_max at full precision and
  *           the final labels by the reference's clarify rule
  *           (SCORE_Io_Characterization.cpp:925-1000).  Also times the growth phases.
+ *           With SCORE_LOG_AREA=<threshold> set it also takes the reference's on-the-fly
+ *           grain-evolution log where log_OUTPUT_Diehl would (SCORE_OnTheFlyCharacterization.cpp:
+ *           635-650: at the SingleGrainVolOverTime X logpoints, after the master block's
+ *           counts): the reference's own log_grainevo and its RX area profile
+ *           log_rxareaprofile(threshold) (:274-384; the log_rxareaprofile2 that
+ *           log_OUTPUT_Diehl calls indexes an empty vector when rendering is off and
+ *           advances the wrong loop counter, :423-427).  With SCORE_REDISCR="<nslots> <tmax>"
+ *           it then evaluates the reference's caHdl::get_interpCellCount
+ *           (SCORE_SolitaryUnitAveraging.cpp:1304-1365) for every grain at the ensemble's
+ *           rediscretized times (postprocess_initrediscrtimes, :50-80).
  *   asis  : calls the unmodified caHdl::solve_RXGROWTH and records t_end, step_end
  *           and the per-grain cell counts; used to prove `loop` is faithful.
  *   ptab  : dumps P(rxg,defg) from caregionMemHdl::reg_calc_mobilityweight
@@ -36,6 +46,10 @@
 #include <cstring>
 #include <vector>
 #include <string>
+#include <cstdlib>
+
+/* grain-evolution logging of the loop mode (SCORE_LOG_AREA), off when < 0 */
+static long g_log_area = -1;
 
 struct Domain {
     uint32_t nx = 0, ny = 0, nz = 0, ndefg = 0, nrxg = 0;
@@ -223,6 +237,14 @@ static int run_loop(caHdl* ca, std::vector<StepRec>& rec, double phase_s[5], dou
                 if (ca->myRecoveryModel.RecoveryConsider != RECOVERY_NO) ca->update_mydgoptimize_rho();
                 ca->update_mydgoptimize_cnt();
                 ca->update_myrhomax();
+                /* log_OUTPUT_Diehl's grain-evolution branch (SCORE_OnTheFlyCharacterization.cpp:646-650),
+                   bounds test first */
+                if (g_log_area >= 0 && ca->loginfo_grainevo_cnt < ca->output_atthisX.size() &&
+                    ca->Xcells >= ca->output_atthisX[ca->loginfo_grainevo_cnt]) {
+                    ca->ompcrit_clarify_status_infectedcells(RXFRACTION_THRESHOLD);
+                    ca->log_grainevo();
+                    ca->log_rxareaprofile((uint32_t)g_log_area);
+                }
                 StepRec r;
                 memset(&r, 0, sizeof r);
                 r.Sv = ca->Sv; r.nfull = nupd; r.Xcells = ca->Xcells; r.Pmax = ca->myMobilityWeightMax;
@@ -243,6 +265,8 @@ static int run_loop(caHdl* ca, std::vector<StepRec>& rec, double phase_s[5], dou
         #pragma omp master
         { loop_s = omp_get_wtime() - t0loop; }
     }
+    ca->tsimend = ca->t;  /* as solve_RXGROWTH leaves them (SCORE_Kernel.cpp:6752-6753) */
+    ca->stepsimend = ca->step;
     phase_s[0] = tgrow; phase_s[1] = tupd; phase_s[2] = tsync; phase_s[3] = tdefrag;
     phase_s[4] = tgrow + tupd + tsync + tdefrag;
     return 0;
@@ -278,6 +302,7 @@ static bool write_file(const std::string& fn, const void* p, size_t bytes) {
 int main(int argc, char** argv) {
     if (argc < 5) { fprintf(stderr, "usage: %s loop|asis|ptab params.uds domain.scdm outprefix\n", argv[0]); return 2; }
     std::string mode = argv[1], out = argv[4];
+    if (const char* la = getenv("SCORE_LOG_AREA")) g_log_area = atol(la);
     Domain d;
     if (!read_domain(argv[3], d)) { fprintf(stderr, "cannot read domain %s\n", argv[3]); return 2; }
     std::streambuf* keep = std::cout.rdbuf();
@@ -324,5 +349,42 @@ int main(int argc, char** argv) {
     fclose(f);
     bool ok = write_file(out + ".trace", rec.data(), rec.size() * sizeof(StepRec)) &&
               write_file(out + ".labels", lab.data(), lab.size() * 4);
+    if (ok && g_log_area >= 0) {
+        /* grain evolution: per snapshot t, X (f64), step, Sv (u32), counts of every grain (u32, deformed then rx) */
+        FILE* g = fopen((out + ".grainevo").c_str(), "wb");
+        for (size_t i = 0; g && i < ca->mygrainevolution.size(); ++i) {
+            const loginfo_grainevo_ca& e = ca->mygrainevolution[i];
+            const uint32_t hdr[2] = {e.localtstep, e.localSv};
+            fwrite(&e.localtime, 8, 1, g); fwrite(&e.localX, 8, 1, g); fwrite(hdr, 4, 2, g);
+            fwrite(e.localdatabucket, 4, e.nlocaldata, g);
+        }
+        if (g) fclose(g);
+        /* RX area profile: per snapshot t, X (f64), step, 0 (u32), then (rx, deformed) cells per z slice (u32) */
+        FILE* a = fopen((out + ".rxprofile").c_str(), "wb");
+        for (size_t i = 0; a && i < ca->myrxprofile.size(); ++i) {
+            const loginfo_rxareaprofile_ca& e = ca->myrxprofile[i];
+            const uint32_t hdr[2] = {e.localstep, 0u};
+            fwrite(&e.localtime, 8, 1, a); fwrite(&e.localX, 8, 1, a); fwrite(hdr, 4, 2, a);
+            fwrite(e.localdatabucket, 4, 2 * (size_t)d.nz, a);
+        }
+        if (a) fclose(a);
+        ok = g && a;
+    }
+    const char* rd = getenv("SCORE_REDISCR");
+    if (ok && rd) {
+        /* postprocess_initrediscrtimes (SCORE_SolitaryUnitAveraging.cpp:62-80) with tensmin = 0, then
+           get_interpCellCount of every grain at every rediscretized time (doubles, [slot][grain]) */
+        unsigned nslots = 0;
+        double tmax = 0.0;
+        if (sscanf(rd, "%u %lf", &nslots, &tmax) != 2 || nslots < 2) return 5;
+        const double ttmin = 0.0, dt = (tmax - ttmin) / ((double)(nslots - 1));
+        const uint32_t ng = (uint32_t)(ca->mydefgpool.size() + ca->myrxgpool.size());
+        std::vector<double> v((size_t)nslots * ng);
+        for (uint32_t n = 0; n < nslots; ++n) {
+            const double when = ttmin + ((double)(n + 1) * dt);
+            for (uint32_t id = 0; id < ng; ++id) v[(size_t)n * ng + id] = ca->get_interpCellCount(id, when);
+        }
+        ok = write_file(out + ".interp", v.data(), v.size() * 8);
+    }
     return ok ? 0 : 4;
 }

@@ -463,7 +463,67 @@ struct oracle_sim {
     double Xcells, X;
     uint32_t step, it, defrag_cnt, nnuc;
     double dt0, Pmax0;
+    /* grain-evolution log: snapshots taken so far, next logpoint */
+    uint32_t nlog, logcap, log_next;
+    double *log_t, *log_X;
+    uint32_t *log_step, *log_sv, *log_counts, *log_area;
 };
+
+/* labels by the clarify rule (ompcrit_clarify_status_infectedcells, SCORE_Io_Characterization.cpp:925-1000):
+   the grid, with every ACTIVE front cell as its deformed grain below fill 0.5 and its rx grain above */
+static void labels_now(const sim* s, uint32_t* labels) {
+    memcpy(labels, s->grid, s->N * 4);
+    for (int L = 0; L < 2; L++) {
+        const flist* f = &s->f[L];
+        for (uint32_t c = 0; c < f->never; c++) {
+            if (!f->act[c]) continue;
+            uint32_t cell = (uint32_t)f->x[c] + s->nx * ((uint32_t)f->y[c] + s->ny * (uint32_t)f->z[c]);
+            labels[cell] = (f->fill[c] < 0.5) ? f->defg[c] : s->ndefg + f->rxg[c];
+        }
+    }
+}
+
+/* log_OUTPUT_Diehl's grain-evolution branch (SCORE_OnTheFlyCharacterization.cpp:646-650), taken after the
+   master block's counts and before t += dt: log_grainevo (:478-531: t, X, step, 32-bit Sv, every grain's
+   cell count, deformed then rx) and the RX area profile of log_rxareaprofile(threshold) (:274-384: per z
+   slice the cells of the rx grains whose section has at least `threshold` cells, and the rest) */
+static int log_snapshot(oracle_sim* o, uint64_t Sv) {
+    sim* s = &o->S;
+    const uint32_t G = s->ndefg + s->nrxg, nz = s->nz, nxy = s->nxy;
+    if (o->nlog == o->logcap) {
+        uint32_t nc = o->logcap ? 2 * o->logcap : 16;
+        o->log_t = realloc(o->log_t, nc * 8ull); o->log_X = realloc(o->log_X, nc * 8ull);
+        o->log_step = realloc(o->log_step, nc * 4ull); o->log_sv = realloc(o->log_sv, nc * 4ull);
+        o->log_counts = realloc(o->log_counts, (uint64_t)nc * G * 4); o->log_area = realloc(o->log_area, (uint64_t)nc * 2 * nz * 4);
+        if (!o->log_t || !o->log_X || !o->log_step || !o->log_sv || !o->log_counts || !o->log_area) return 0;
+        o->logcap = nc;
+    }
+    const uint32_t k = o->nlog++;
+    o->log_t[k] = s->ph.t; o->log_X[k] = o->X; o->log_step[k] = o->step; o->log_sv[k] = (uint32_t)Sv;
+    uint32_t* cnt = o->log_counts + (uint64_t)k * G;
+    memcpy(cnt, s->defg_cnt, s->ndefg * 4ull);
+    memcpy(cnt + s->ndefg, s->rxg_cnt, s->nrxg * 4ull);
+    uint32_t* lab = malloc(s->N * 4);
+    uint32_t* sec = calloc(s->nrxg ? s->nrxg : 1, 4);
+    if (!lab || !sec) { free(lab); free(sec); return 0; }
+    labels_now(s, lab);
+    uint32_t* area = o->log_area + (uint64_t)k * 2 * nz;
+    const uint32_t thr = s->p->rxarea_threshold;
+    for (uint32_t z = 0; z < nz; z++) {
+        const uint32_t* sl = lab + (uint64_t)z * nxy;
+        for (uint32_t i = 0; i < nxy; i++)
+            if (sl[i] >= s->ndefg && sl[i] < s->ndefg + s->nrxg) sec[sl[i] - s->ndefg]++;
+        uint32_t rx = 0;
+        for (uint32_t r = 0; r < s->nrxg; r++) {
+            if (sec[r] >= thr) rx += sec[r];
+            sec[r] = 0;
+        }
+        area[2 * z] = rx;
+        area[2 * z + 1] = nxy - rx;
+    }
+    free(lab); free(sec);
+    return 1;
+}
 
 oracle_sim* oracle_create(const score_params* p, const uint32_t* grid, const double* defg_q, const double* defg_rho0, uint32_t ndefg,
                           const double* rxg_q, const uint32_t* rxg_site, const double* rxg_tincub, uint32_t nrxg,
@@ -549,6 +609,10 @@ int oracle_advance(oracle_sim* o, double x_target, uint32_t max_steps, oracle_st
         o->X = (o->Xcells / (double)s->N);
         ph->rhomax = rhomax_of(s->rho, s->defg_cnt, s->ndefg);
         double rhomax_step = ph->rhomax, dt_used = ph->dt;
+        if (o->log_next < p->n_logpoints && o->Xcells >= p->logpoint_x[o->log_next] * (double)s->N) {
+            if (!log_snapshot(o, Sv)) { s->status = SCORE_ERR_NOMEM; break; }
+            o->log_next++;
+        }
         ph->t += ph->dt;
         ph_temperature(ph); ph_atomistic(ph); ph_micro(ph); ph_mobilities(ph);
         ph_recovery(ph, s->rho, s->rho0, s->ndefg);
@@ -579,20 +643,28 @@ int oracle_done(const oracle_sim* o, double x_target) {
            (s->ph.t > s->p->tmax) || o->it >= 1000000u;
 }
 
+double oracle_time(const oracle_sim* o) { return o->S.ph.t; }
+
+uint32_t oracle_log_count(const oracle_sim* o) { return o->nlog; }
+
+int oracle_log_get(const oracle_sim* o, uint32_t i, double* t, double* X, uint32_t* step, uint32_t* sv, uint32_t* counts,
+                   uint32_t* area) {
+    const sim* s = &o->S;
+    if (i >= o->nlog) return SCORE_ERR_ARG;
+    const uint32_t G = s->ndefg + s->nrxg;
+    if (t) *t = o->log_t[i];
+    if (X) *X = o->log_X[i];
+    if (step) *step = o->log_step[i];
+    if (sv) *sv = o->log_sv[i];
+    if (counts) memcpy(counts, o->log_counts + (uint64_t)i * G, G * 4ull);
+    if (area) memcpy(area, o->log_area + (uint64_t)i * 2 * s->nz, 2ull * s->nz * 4);
+    return SCORE_OK;
+}
+
 void oracle_finish(const oracle_sim* o, uint32_t* labels, uint32_t* rxg_counts, uint32_t* defg_counts) {
     const sim* s = &o->S;
     /* final labels, ompcrit_clarify_status_infectedcells (SCORE_Io_Characterization.cpp:925-1000) */
-    if (labels) {
-        memcpy(labels, s->grid, s->N * 4);
-        for (int L = 0; L < 2; L++) {
-            const flist* f = &s->f[L];
-            for (uint32_t c = 0; c < f->never; c++) {
-                if (!f->act[c]) continue;
-                uint32_t cell = (uint32_t)f->x[c] + s->nx * ((uint32_t)f->y[c] + s->ny * (uint32_t)f->z[c]);
-                labels[cell] = (f->fill[c] < 0.5) ? f->defg[c] : s->ndefg + f->rxg[c];
-            }
-        }
-    }
+    if (labels) labels_now(s, labels);
     if (rxg_counts) memcpy(rxg_counts, s->rxg_cnt, s->nrxg * 4ull);
     if (defg_counts) memcpy(defg_counts, s->defg_cnt, s->ndefg * 4ull);
 }
@@ -602,7 +674,77 @@ void oracle_destroy(oracle_sim* o) {
     sim* s = &o->S;
     fl_free(&s->f[0]); fl_free(&s->f[1]);
     free(s->grid); free(s->rxg_cnt); free(s->defg_cnt); free(s->rho); free(s->rho0); free(s->pcache); free(o->considered);
+    free(o->log_t); free(o->log_X); free(o->log_step); free(o->log_sv); free(o->log_counts); free(o->log_area);
     free(o);
+}
+
+/* ------------------------------------------------------------------ ensemble post-processing */
+/* caHdl::get_interpCellCount, SCORE_SolitaryUnitAveraging.cpp:1304-1365: the final count at or after the
+   end of the run, else linear between the logged snapshots that frame `when` (the first snapshot
+   before the first log time, the last one after the last); the scan stops at the end of the log */
+double oracle_interp_count(const oracle_evo* e, uint32_t id, double when) {
+    const uint32_t G = e->ndefg + e->nrxg;
+    if (when >= e->tsimend || e->nsnap == 0) return (double)e->final_counts[id];  /* the reference indexes an empty log there */
+    uint32_t i = 0;
+    while (i < e->nsnap && e->t[i] < when) i++;
+    if (i > 0 && i < e->nsnap) {
+        double ti1 = e->t[i - 1];
+        double cnti1 = e->counts[(uint64_t)(i - 1) * G + id];
+        double ti = e->t[i];
+        double cnti = e->counts[(uint64_t)i * G + id];
+        return cnti1 + ((when - ti1) * ((cnti - cnti1) / (ti - ti1)));
+    }
+    if (i == 0) return (double)e->counts[id];
+    return (double)e->counts[(uint64_t)(e->nsnap - 1) * G + id];
+}
+
+/* ensembleHdl::postprocess_init + postprocess_initrediscrtimes (SCORE_SolitaryUnitAveraging.cpp:50-80, 510-540):
+   nslots equidistant times over [0, latest end time], each the end of its interval */
+static double rediscr_times(const oracle_evo* doms, uint32_t ndom, uint32_t nslots, double* t_out) {
+    double tmax = 0.0;
+    for (uint32_t d = 0; d < ndom; d++) if (doms[d].tsimend >= tmax) tmax = doms[d].tsimend;
+    const double ttmin = 0.0, dt = (tmax - ttmin) / ((double)(nslots - 1));
+    for (uint32_t n = 0; n < nslots; n++) t_out[n] = ttmin + ((double)(n + 1) * dt);
+    return tmax;
+}
+
+/* ensembleHdl::postprocess_rediscr_kinetics, SCORE_SolitaryUnitAveraging.cpp:546-670: per time slot the
+   recrystallized volume of the ensemble, sum over domains of (box volume - interpolated deformed volume) */
+void oracle_rediscr_kinetics(const oracle_evo* doms, uint32_t ndom, uint32_t nslots, double* t_out, double* vol_out,
+                             double* boxvol_out) {
+    rediscr_times(doms, ndom, nslots, t_out);
+    double* dv = malloc(nslots * 8ull);
+    double box = 0.0;
+    for (uint32_t n = 0; n < nslots; n++) vol_out[n] = 0.0;
+    for (uint32_t d = 0; d < ndom; d++) {
+        box = box + doms[d].nboxvol;
+        for (uint32_t n = 0; n < nslots; n++) dv[n] = 0.0;
+        for (uint32_t g = 0; g < doms[d].ndefg; g++)
+            for (uint32_t n = 0; n < nslots; n++) dv[n] = dv[n] + oracle_interp_count(&doms[d], g, t_out[n]);
+        for (uint32_t n = 0; n < nslots; n++) vol_out[n] = vol_out[n] + (doms[d].nboxvol - dv[n]);
+    }
+    if (boxvol_out) *boxvol_out = box;
+    free(dv);
+}
+
+/* ensembleHdl::postprocess_rediscr_macrotexture, SCORE_SolitaryUnitAveraging.cpp:673-804: per time slot and
+   orientation class the interpolated volume of the ensemble's grains, deformed then rx, [slot][class] */
+void oracle_rediscr_macrotexture(const oracle_evo* doms, uint32_t ndom, uint32_t nslots, uint32_t nclass, double* t_out,
+                                 double* vol_out) {
+    rediscr_times(doms, ndom, nslots, t_out);
+    const uint64_t M = (uint64_t)nslots * nclass;
+    double* dv = malloc(M * 8);
+    for (uint64_t k = 0; k < M; k++) vol_out[k] = 0.0;
+    for (uint32_t d = 0; d < ndom; d++) {
+        const oracle_evo* e = &doms[d];
+        for (uint64_t k = 0; k < M; k++) dv[k] = 0.0;
+        for (uint32_t g = 0; g < e->ndefg + e->nrxg; g++) {
+            const uint32_t c = e->grain_class[g];
+            for (uint32_t n = 0; n < nslots; n++) dv[(uint64_t)nclass * n + c] += oracle_interp_count(e, g, t_out[n]);
+        }
+        for (uint64_t k = 0; k < M; k++) vol_out[k] += dv[k];
+    }
+    free(dv);
 }
 
 int oracle_run(const score_params* p, const uint32_t* grid, const double* defg_q, const double* defg_rho0, uint32_t ndefg,

@@ -60,6 +60,29 @@ int oracle_advance(oracle_sim* o, double x_target, uint32_t max_steps, oracle_st
 int oracle_done(const oracle_sim* o, double x_target);
 void oracle_finish(const oracle_sim* o, uint32_t* labels, uint32_t* rxg_counts, uint32_t* defg_counts);
 void oracle_destroy(oracle_sim* o);
+double oracle_time(const oracle_sim* o);   /* t after the last step */
+
+/* The grain-evolution log of a run (params n_logpoints / logpoint_x / rxarea_threshold): per snapshot the
+ * time before the logged step, X after it, its step index and 32-bit Sv, every grain's cell count
+ * (ndefg + nrxg, deformed first) and the RX area profile (2 nz: rx cells, the rest, per z slice). */
+uint32_t oracle_log_count(const oracle_sim* o);
+int oracle_log_get(const oracle_sim* o, uint32_t i, double* t, double* X, uint32_t* step, uint32_t* sv, uint32_t* counts,
+                   uint32_t* area);
+
+/* Ensemble post-processing of grain-evolution logs (SCORE_SolitaryUnitAveraging.cpp). */
+typedef struct oracle_evo {
+    uint32_t ndefg, nrxg, nsnap;
+    const double* t;                /* nsnap snapshot times */
+    const uint32_t* counts;         /* nsnap x (ndefg + nrxg) */
+    const uint32_t* final_counts;   /* ndefg + nrxg at the end of the run */
+    double tsimend, nboxvol;        /* end time of the run, cells of the domain */
+    const uint32_t* grain_class;    /* ndefg + nrxg orientation classes (macrotexture), or NULL */
+} oracle_evo;
+double oracle_interp_count(const oracle_evo* e, uint32_t id, double when);
+void oracle_rediscr_kinetics(const oracle_evo* doms, uint32_t ndom, uint32_t nslots, double* t_out, double* vol_out,
+                             double* boxvol_out);
+void oracle_rediscr_macrotexture(const oracle_evo* doms, uint32_t ndom, uint32_t nslots, uint32_t nclass, double* t_out,
+                                 double* vol_out);
 
 /* P(rxg,defg) by the reference's formula, for pinning the table against the reference */
 double oracle_mobility_weight(const score_params* p, const double* qr, const double* qd);

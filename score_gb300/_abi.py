@@ -56,6 +56,7 @@ class Params(C.Structure):
         ("n_zener", _u32), ("zener_time", _d * MAX_TABLE), ("zener_fr", _d * MAX_TABLE),
         ("n_schedule", _u32), ("sched_time", _d * MAX_TABLE), ("sched_temp", _d * MAX_TABLE),
         ("boundary", _i32), ("precision", _i32), ("border_policy", _i32), ("reserved", _i32),
+        ("n_logpoints", _u32), ("logpoint_x", _d * MAX_TABLE), ("rxarea_threshold", _u32), ("reserved2", _u32),
     ]
 
 
@@ -66,6 +67,10 @@ class StepStats(C.Structure):
         ("Pmax", _d), ("rhomax", _d), ("dXstep", _d),
         ("next_never", _u32 * 2), ("n_recycled", _u32 * 2), ("p_misses", _u32), ("reserved", _u32),
     ]
+
+
+class GrainEvoInfo(C.Structure):
+    _fields_ = [("t", _d), ("X", _d), ("step", _u32), ("Sv", _u32)]
 
 
 class Timing(C.Structure):
@@ -133,6 +138,14 @@ SIGNATURES = {
     "score_batch_get_tune": (C.c_int, [_vp, _P(Tune)]),
     "score_batch_set_tune": (C.c_int, [_vp, _P(Tune)]),
     "score_batch_autotune": (C.c_int, [_vp, _d, _u32, _P(Tune)]),
+    "score_grainevo_count": (C.c_int, [_vp, _P(_u32)]),
+    "score_grainevo": (C.c_int, [_vp, _u32, _P(GrainEvoInfo), _vp, _vp]),
+    "score_batch_grainevo_count": (C.c_int, [_vp, _u32, _P(_u32)]),
+    "score_batch_grainevo": (C.c_int, [_vp, _u32, _u32, _P(GrainEvoInfo), _vp, _vp]),
+    "score_rediscr_kinetics": (C.c_int, [_vp, _u32, _vp, _vp, _P(_d)]),
+    "score_batch_rediscr_kinetics": (C.c_int, [_vp, _u32, _vp, _vp, _P(_d)]),
+    "score_batch_rediscr_texture": (C.c_int, [_vp, _u32, _vp, _u32, _vp, _vp]),
+    "score_batch_final_grain_sizes": (C.c_int, [_vp, _vp]),
     "score_mobility_weight": (C.c_int, [_P(Params), _vp, _vp, _P(_d)]),
     "score_mobility_table_noalloc": (C.c_int, [_P(Params), _vp, _u32, _vp, _u32, _vp, _vp, _vp]),
     "score_gen_default": (C.c_int, [_P(GenParams)]),

@@ -231,6 +231,118 @@ __global__ void __launch_bounds__(kBlock) k_defrag_compact(DomainArgs a, int L, 
     }
 }
 
+// ---- on-the-fly characterization: RX area profile (log_rxareaprofile(threshold),
+// SCORE_OnTheFlyCharacterization.cpp:274-384) over a label map, slices [z0, z1) ----
+// section of every rx grain in every slice: hist[(z - z0) nrxg + rxg]; cells of one warp that
+// carry the same label add together (a row of cells mostly belongs to one grain)
+__global__ void k_area_hist(const uint32_t* lab, uint32_t nxy, uint32_t z0, uint32_t z1, uint32_t ndefg, uint32_t nrxg,
+                            uint32_t* hist) {
+    // cells and keys of a chunk fit 32 bits: N < 2^31 and the chunk's slices x nrxg <= N
+    const uint64_t lo = (uint64_t)z0 * nxy;
+    const uint32_t n = (z1 - z0) * nxy, stride = gridDim.x * blockDim.x;
+    const uint32_t end = (n + 31u) & ~31u;  // whole warps, so that every lane takes part in the match
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < end; i += stride) {
+        uint32_t key = 0xFFFFFFFFu;
+        if (i < n) {
+            const uint32_t r = lab[lo + i] - ndefg;  // wraps for deformed ids
+            if (r < nrxg) key = (i / nxy) * nrxg + r;
+        }
+        const uint32_t m = __match_any_sync(0xFFFFFFFFu, key);
+        if (key != 0xFFFFFFFFu && (__ffs(m) - 1) == (int)(threadIdx.x & 31)) atomicAdd(&hist[key], (uint32_t)__popc(m));
+    }
+}
+// one block per slice: cells of the rx grains whose section reaches the threshold, and the rest;
+// clears the slice's histogram for the next use
+__global__ void __launch_bounds__(kBlock) k_area_sum(uint32_t* hist, uint32_t nrxg, uint32_t nxy, uint32_t thr, uint32_t* out) {
+    __shared__ uint32_t s_w[kWarps];
+    uint32_t* h = hist + (uint64_t)blockIdx.x * nrxg;
+    uint32_t rx = 0;
+    for (uint32_t r = threadIdx.x; r < nrxg; r += blockDim.x) {
+        const uint32_t v = h[r];
+        if (v >= thr) rx += v;
+        h[r] = 0;
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) rx += __shfl_xor_sync(0xFFFFFFFFu, rx, o);
+    if ((threadIdx.x & 31) == 0) s_w[threadIdx.x >> 5] = rx;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        uint32_t t = 0;
+        for (int w = 0; w < kWarps; ++w) t += s_w[w];
+        out[2 * blockIdx.x] = t;
+        out[2 * blockIdx.x + 1] = nxy - t;
+    }
+}
+
+// ---- ensemble post-processing (SCORE_SolitaryUnitAveraging.cpp) of the grain-evolution logs ----
+struct EvoDev {
+    const double* t;              // snapshot times
+    const uint32_t* counts;       // nsnap x (ndefg + nrxg)
+    const uint32_t* fin_defg;     // counts at the end of the run
+    const uint32_t* fin_rxg;
+    const uint32_t* cls;          // orientation class of every grain (macrotexture), or null
+    uint32_t ndefg, nrxg, nsnap, pad;
+    double tsimend, nboxvol;
+};
+// caHdl::get_interpCellCount (SCORE_SolitaryUnitAveraging.cpp:1304-1365) for grain `id`, with the
+// snapshot index i of `when` (first snapshot at or after it) found once per time
+__device__ __forceinline__ double interp_count(const EvoDev& e, uint32_t id, double when, uint32_t i) {
+    const uint32_t G = e.ndefg + e.nrxg;
+    if (when >= e.tsimend) return (double)(id < e.ndefg ? e.fin_defg[id] : e.fin_rxg[id - e.ndefg]);
+    if (i > 0 && i < e.nsnap) {
+        const double ti1 = e.t[i - 1], cnti1 = (double)e.counts[(uint64_t)(i - 1) * G + id];
+        const double ti = e.t[i], cnti = (double)e.counts[(uint64_t)i * G + id];
+        return __dadd_rn(cnti1, __dmul_rn(__dsub_rn(when, ti1), __ddiv_rn(__dsub_rn(cnti, cnti1), __dsub_rn(ti, ti1))));
+    }
+    if (i == 0) return (double)e.counts[id];
+    return (double)e.counts[(uint64_t)(e.nsnap - 1) * G + id];
+}
+__device__ __forceinline__ uint32_t snap_index(const EvoDev& e, double when) {
+    uint32_t i = 0;
+    while (i < e.nsnap && e.t[i] < when) ++i;
+    return i;
+}
+// one thread per (domain, time slot): the domain's interpolated deformed volume, summed over its
+// grains in order (postprocess_rediscr_kinetics, :546-600), as box volume minus it
+__global__ void k_rediscr_kinetics(const EvoDev* doms, uint32_t ndom, const double* when, uint32_t nslots, double* per_dom) {
+    const uint32_t k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= ndom * nslots) return;
+    const uint32_t d = k / nslots, n = k - d * nslots;
+    const EvoDev e = doms[d];
+    const double w = when[n];
+    const uint32_t i = snap_index(e, w);
+    double dv = 0.0;
+    for (uint32_t g = 0; g < e.ndefg; ++g) dv = __dadd_rn(dv, interp_count(e, g, w, i));
+    per_dom[k] = __dsub_rn(e.nboxvol, dv);
+}
+// one thread per (domain, time slot): interpolated volume per orientation class, deformed grains then
+// rx grains in order (postprocess_rediscr_macrotexture, :673-747); [domain][slot][class]
+constexpr uint32_t kMaxClasses = 32;
+__global__ void k_rediscr_texture(const EvoDev* doms, uint32_t ndom, const double* when, uint32_t nslots, uint32_t nclass,
+                                  double* per_dom) {
+    const uint32_t k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= ndom * nslots) return;
+    const uint32_t d = k / nslots, n = k - d * nslots;
+    const EvoDev e = doms[d];
+    const double w = when[n];
+    const uint32_t i = snap_index(e, w);
+    double acc[kMaxClasses];
+    for (uint32_t c = 0; c < nclass; ++c) acc[c] = 0.0;
+    for (uint32_t g = 0; g < e.ndefg + e.nrxg; ++g) {
+        const uint32_t c = e.cls[g];
+        acc[c] = __dadd_rn(acc[c], interp_count(e, g, w, i));
+    }
+    for (uint32_t c = 0; c < nclass; ++c) per_dom[(uint64_t)k * nclass + c] = acc[c];
+}
+// ensemble sums over the domains in order, one thread per output value
+__global__ void k_rediscr_ensemble(const double* per_dom, uint32_t ndom, uint32_t m, double* out) {
+    const uint32_t k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= m) return;
+    double v = 0.0;
+    for (uint32_t d = 0; d < ndom; ++d) v = __dadd_rn(v, per_dom[(uint64_t)d * m + k]);
+    out[k] = v;
+}
+
 __global__ void k_first_inactive(const uint8_t* dir, uint32_t lo, uint32_t hi, uint32_t* out) {
     for (uint32_t s = lo + blockIdx.x * blockDim.x + threadIdx.x; s < hi; s += gridDim.x * blockDim.x)
         if (dir[s] == kInactive) atomicMin(out, s);
@@ -317,6 +429,14 @@ struct score_ctx {
     std::vector<double> ans_val;
     uint64_t launches = 0;             // kernels launched outside the step sequence
     std::vector<score_step_stats> trace;  // per-step stats of the last batched run
+    // on-the-fly characterization: the grain-evolution log at the SingleGrainVolOverTime logpoints
+    double t_step = 0.0;               // t at the start of the running step (the log records it)
+    std::vector<double> log_cells;     // logpoint X times N: the reference's output_atthisX
+    uint32_t log_next = 0;             // next logpoint
+    std::vector<score_grainevo_info> log_info;
+    uint32_t* d_log_counts = nullptr;  // log_cap x (ndefg + nrxg) cell counts
+    uint32_t* d_log_area = nullptr;    // log_cap x 2 nz RX area profile
+    uint32_t log_cap = 0;
 
     ~score_ctx() { release_domain(); release_stream(); }
     void release_domain();
@@ -343,7 +463,7 @@ void score_ctx::release_domain() {
                     a.grid, a.claim, a.amask, a.ptab, a.defg_cnt, a.rxg_cnt, a.depleted, a.miss, a.tobm, a.ctcnt, a.fcell,
                     a.f[0].fmask, a.f[0].imask, a.f[0].tcnt, a.f[1].fmask, a.f[1].imask, a.f[1].tcnt,
                     a.f[0].scnt, a.f[1].scnt, a.csct,
-                    d_state, d_pforce, d_u32tmp, d_stage, d_grid_init, d_defg_cnt_init, d_due,
+                    d_state, d_pforce, d_u32tmp, d_stage, d_grid_init, d_defg_cnt_init, d_due, d_log_counts, d_log_area,
                     scratch.fill, scratch.comp, scratch.vel, scratch.defg, scratch.rxg, scratch.xyz, scratch.dir};
     for (void* p : ptrs) if (p) cudaFree(p);
     if (h_pforce) cudaFreeHost(h_pforce);
@@ -354,6 +474,7 @@ void score_ctx::release_domain() {
     scratch = DFront{};
     d_state = nullptr; d_pforce = nullptr; d_u32tmp = nullptr; d_stage = nullptr;
     d_grid_init = nullptr; d_defg_cnt_init = nullptr;
+    d_log_counts = nullptr; d_log_area = nullptr; log_cap = 0;
     stage_cap = 0; scratch_cap = 0;
     loaded = false;
 }
@@ -872,6 +993,10 @@ int reset_state(score_ctx* c) {
     if (e != cudaSuccess) return c->cuda_fail(e, "reset domain");
     c->ans_idx.clear();
     c->ans_val.clear();
+    c->log_info.clear();
+    c->log_next = 0;
+    c->log_cells.resize(std::min<uint32_t>(c->prm.n_logpoints, c->log_cap));
+    for (size_t k = 0; k < c->log_cells.size(); ++k) c->log_cells[k] = c->prm.logpoint_x[k] * (double)c->N;  // log_initialization, :60-62
     memset(&c->h_box->snap, 0, sizeof(DevState));
     c->running = false;
     c->trace.clear();
@@ -920,6 +1045,7 @@ namespace {
 // argument block of this step.
 int pre_step(score_ctx* c, uint32_t* newnuc) {
     Physics& ph = c->ph;
+    c->t_step = ph.t;
     // on-the-fly defragmentation at user X logpoints (SCORE_Kernel.cpp:6625-6630, thresholds in cells)
     const bool defrag = c->prm.defragmentation && c->defrag_cnt < c->prm.n_defrag && c->Xcells >= c->prm.defrag_x[c->defrag_cnt] * (double)c->N;
     // time-dependent nucleation (no-op when site-saturated); on the device unless the host
@@ -964,6 +1090,53 @@ int physics_ahead(score_ctx* c) {
     c->rho_next.resize(c->ndefg);
     for_grains(c, [&](size_t lo, size_t hi) { ph.update_substructure(c->rho_next.data(), c->rho.data(), c->rho0.data(), lo, hi); });
     return upload_physics(c, c->rho_next.data(), c->rho_version + 1);
+}
+
+// log_OUTPUT_Diehl's grain-evolution branch (SCORE_OnTheFlyCharacterization.cpp:646-650), stream-ordered
+// before the next step: every grain's cell count (log_grainevo, :478-531) and the RX area profile of
+// the clarified labels (log_rxareaprofile(threshold), :274-384), on the device; the host keeps the
+// snapshot's time (before t += dt), X, step and 32-bit Sv.
+int log_snapshot(score_ctx* c, uint64_t Sv) {
+    const uint32_t k = (uint32_t)c->log_info.size();
+    if (k >= c->log_cap) return c->fail(SCORE_ERR_CAPACITY, "grain-evolution log full");
+    cudaStream_t st = c->stream;
+    DomainArgs& a = c->a;
+    const size_t G = (size_t)c->ndefg + c->nrxg;
+    uint32_t* cnt = c->d_log_counts + (size_t)k * G;
+    cudaError_t e = cudaMemcpyAsync(cnt, a.defg_cnt, (size_t)c->ndefg * 4, cudaMemcpyDeviceToDevice, st);
+    if (e == cudaSuccess && c->nrxg) e = cudaMemcpyAsync(cnt + c->ndefg, a.rxg_cnt, (size_t)c->nrxg * 4, cudaMemcpyDeviceToDevice, st);
+    // labels by the clarify rule into the attempt-mask array (free between steps)
+    uint32_t* lab = a.amask;
+    if (e == cudaSuccess) e = cudaMemcpyAsync(lab, a.grid, c->N * 4, cudaMemcpyDeviceToDevice, st);
+    if (e != cudaSuccess) return c->cuda_fail(e, "grain-evolution log");
+    for (int L = 0; L < 2; ++L) {
+        const uint32_t n = c->next_never[L];
+        if (n == 0) continue;
+        if (c->fp32) k_labels_front<true><<<blocks_for(n, c->sms), kBlock, 0, st>>>(a, L, n, lab);
+        else k_labels_front<false><<<blocks_for(n, c->sms), kBlock, 0, st>>>(a, L, n, lab);
+        c->launches++;
+    }
+    // per-slice sections of the rx grains, in chunks of slices whose histogram fits the win-mask array
+    uint32_t* out = c->d_log_area + (size_t)k * 2 * c->nz;
+    const uint32_t nxy = c->nx * c->ny, nr = std::max<uint32_t>(c->nrxg, 1);
+    const uint32_t K = (uint32_t)std::max<uint64_t>(1, std::min<uint64_t>(c->nz, c->N / nr));
+    e = cudaMemsetAsync(a.tobm, 0, (size_t)K * nr * 4, st);
+    if (e != cudaSuccess) return c->cuda_fail(e, "RX area profile");
+    for (uint32_t z0 = 0; z0 < c->nz; z0 += K) {
+        const uint32_t z1 = std::min(c->nz, z0 + K);
+        k_area_hist<<<blocks_for((uint64_t)(z1 - z0) * nxy, c->sms, 16), kBlock, 0, st>>>(lab, nxy, z0, z1, c->ndefg, c->nrxg, a.tobm);
+        k_area_sum<<<z1 - z0, kBlock, 0, st>>>(a.tobm, c->nrxg, nxy, c->prm.rxarea_threshold, out + 2 * (size_t)z0);
+        c->launches += 2;
+    }
+    e = cudaGetLastError();
+    if (e != cudaSuccess) return c->cuda_fail(e, "RX area profile");
+    score_grainevo_info info{};
+    info.t = c->t_step;
+    info.X = c->Xcells / (double)c->N;
+    info.step = c->step;
+    info.Sv = (uint32_t)Sv;
+    c->log_info.push_back(info);
+    return SCORE_OK;
 }
 
 // After the step: the mailbox (scalars, weight requests, depleted grains), the host's
@@ -1049,6 +1222,11 @@ int post_step(score_ctx* c, uint32_t newnuc, score_step_stats* out) {
         c->rhomax_version = c->rho_version;
     }
     const double rhomax_step = ph.rhomax;
+    if (c->log_next < c->log_cells.size() && c->Xcells >= c->log_cells[c->log_next]) {
+        const int ls = log_snapshot(c, Sv);
+        if (ls != SCORE_OK) return ls;
+        c->log_next++;
+    }
     if (!c->ahead) {
         const int s = physics_ahead(c);
         if (s != SCORE_OK) return s;
@@ -1508,6 +1686,105 @@ int Engine::set_tune(const score_tune* t) {
     return SCORE_OK;
 }
 
+// ------------------------------------------------------------------ grain-evolution logs
+namespace {
+
+int grainevo_get(score_ctx* c, uint32_t i, score_grainevo_info* info, uint32_t* counts, uint32_t* rxarea) {
+    if (i >= c->log_info.size()) return c->fail(SCORE_ERR_ARG, "no such grain-evolution snapshot");
+    cudaSetDevice(c->device);
+    if (info) *info = c->log_info[i];
+    const size_t G = (size_t)c->ndefg + c->nrxg;
+    cudaError_t e = cudaSuccess;
+    if (counts) e = cudaMemcpyAsync(counts, c->d_log_counts + i * G, G * 4, cudaMemcpyDeviceToHost, c->stream);
+    if (e == cudaSuccess && rxarea)
+        e = cudaMemcpyAsync(rxarea, c->d_log_area + (size_t)i * 2 * c->nz, (size_t)2 * c->nz * 4, cudaMemcpyDeviceToHost, c->stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(c->stream);
+    if (e != cudaSuccess) return c->cuda_fail(e, "read grain-evolution log");
+    return SCORE_OK;
+}
+
+// Ensemble post-processing of the domains' grain-evolution logs on the device: kinetics (cls null)
+// or macrotexture by orientation class.  Writes the time slots and [slot] or [slot][class] sums.
+int rediscr(const std::vector<score_ctx*>& doms, uint32_t nslots, const uint32_t* cls, uint32_t nclass, double* t_out,
+            double* out, double* boxvol_out, std::string& err) {
+    if (doms.empty() || nslots < 2 || !t_out || !out) { err = "bad argument"; return SCORE_ERR_ARG; }
+    if (cls && (nclass == 0 || nclass > kMaxClasses)) { err = "1 to 32 orientation classes"; return SCORE_ERR_ARG; }
+    const int dev = doms[0]->device;
+    double tmax = 0.0, box = 0.0;
+    size_t ntimes = 0, ncls = 0;
+    for (score_ctx* c : doms) {
+        if (!c->loaded || c->device != dev) { err = "every domain must be loaded, on one device"; return SCORE_ERR_STATE; }
+        // get_interpCellCount reads the first snapshot before the first log time: a domain needs one
+        if (c->log_info.empty()) { err = "a domain has no grain-evolution snapshot (no logpoint reached)"; return SCORE_ERR_STATE; }
+        if (c->ph.t >= tmax) tmax = c->ph.t;  // postprocess_init: the latest tsimend
+        box = box + (double)c->N;
+        ntimes += c->log_info.size();
+        ncls += (size_t)c->ndefg + c->nrxg;
+    }
+    // postprocess_initrediscrtimes (REDISCR_TIME_EQUIDISTANT, tensmin 0)
+    const double ttmin = 0.0, dt = (tmax - ttmin) / ((double)(nslots - 1));
+    for (uint32_t n = 0; n < nslots; ++n) t_out[n] = ttmin + ((double)(n + 1) * dt);
+    if (boxvol_out) *boxvol_out = box;
+    cudaSetDevice(dev);
+    for (score_ctx* c : doms) {  // every domain's last run is complete
+        const cudaError_t e = cudaStreamSynchronize(c->stream);
+        if (e != cudaSuccess) { err = cudaGetErrorString(e); return SCORE_ERR_CUDA; }
+    }
+    const uint32_t ndom = (uint32_t)doms.size(), m = cls ? nslots * nclass : nslots;
+    // one device block: domain descriptors, snapshot times, slot times, classes, per-domain and ensemble sums
+    const size_t b_evo = ndom * sizeof(EvoDev), b_t = ntimes * 8, b_w = (size_t)nslots * 8, b_c = cls ? ncls * 4 : 0;
+    const size_t b_pd = (size_t)ndom * m * 8, b_out = (size_t)m * 8;
+    auto up = [](size_t x) { return (x + 255) & ~(size_t)255; };
+    const size_t total = up(b_evo) + up(b_t) + up(b_w) + up(b_c) + up(b_pd) + up(b_out);
+    char* blk = nullptr;
+    cudaError_t e = cudaMalloc((void**)&blk, total);
+    if (e != cudaSuccess) { err = "post-processing buffers"; return SCORE_ERR_NOMEM; }
+    EvoDev* d_evo = (EvoDev*)blk;
+    double* d_t = (double*)(blk + up(b_evo));
+    double* d_w = (double*)((char*)d_t + up(b_t));
+    uint32_t* d_c = (uint32_t*)((char*)d_w + up(b_w));
+    double* d_pd = (double*)((char*)d_c + up(b_c));
+    double* d_out = (double*)((char*)d_pd + up(b_pd));
+    std::vector<EvoDev> evo(ndom);
+    std::vector<double> times;
+    times.reserve(ntimes);
+    size_t toff = 0, coff = 0;
+    for (uint32_t d = 0; d < ndom; ++d) {
+        score_ctx* c = doms[d];
+        EvoDev& v = evo[d];
+        v.t = d_t + toff;
+        v.counts = c->d_log_counts;
+        v.fin_defg = c->a.defg_cnt;
+        v.fin_rxg = c->a.rxg_cnt;
+        v.cls = cls ? d_c + coff : nullptr;
+        v.ndefg = c->ndefg; v.nrxg = c->nrxg; v.nsnap = (uint32_t)c->log_info.size(); v.pad = 0;
+        v.tsimend = c->ph.t; v.nboxvol = (double)c->N;
+        for (const auto& info : c->log_info) times.push_back(info.t);
+        toff += c->log_info.size();
+        coff += (size_t)c->ndefg + c->nrxg;
+    }
+    cudaStream_t st = doms[0]->stream;
+    e = cudaMemcpyAsync(d_evo, evo.data(), b_evo, cudaMemcpyHostToDevice, st);
+    if (e == cudaSuccess && b_t) e = cudaMemcpyAsync(d_t, times.data(), b_t, cudaMemcpyHostToDevice, st);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(d_w, t_out, b_w, cudaMemcpyHostToDevice, st);
+    if (e == cudaSuccess && cls) e = cudaMemcpyAsync(d_c, cls, b_c, cudaMemcpyHostToDevice, st);
+    if (e == cudaSuccess) {
+        const uint32_t nt = ndom * nslots;
+        if (cls) k_rediscr_texture<<<(nt + 127) / 128, 128, 0, st>>>(d_evo, ndom, d_w, nslots, nclass, d_pd);
+        else k_rediscr_kinetics<<<(nt + 127) / 128, 128, 0, st>>>(d_evo, ndom, d_w, nslots, d_pd);
+        k_rediscr_ensemble<<<(m + 127) / 128, 128, 0, st>>>(d_pd, ndom, m, d_out);
+        doms[0]->launches += 2;
+        e = cudaGetLastError();
+    }
+    if (e == cudaSuccess) e = cudaMemcpyAsync(out, d_out, b_out, cudaMemcpyDeviceToHost, st);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+    cudaFree(blk);
+    if (e != cudaSuccess) { err = std::string("post-processing: ") + cudaGetErrorString(e); return SCORE_ERR_CUDA; }
+    return SCORE_OK;
+}
+
+}  // namespace
+
 // ------------------------------------------------------------------ C ABI
 extern "C" {
 
@@ -1647,6 +1924,10 @@ int score_load_domain(score_ctx* c, const uint32_t* grid, const double* defg_qua
         if (e == cudaSuccess) e = cudaMallocHost((void**)&c->h_due, kDueMax * sizeof(NucDue));
         if (e == cudaSuccess) e = dalloc(&c->d_due, kDueMax);
         if (e == cudaSuccess) e = dalloc(&c->d_u32tmp, 64);
+        // at most one grain-evolution snapshot per logpoint
+        c->log_cap = std::min<uint32_t>(p.n_logpoints, SCORE_MAX_TABLE);
+        if (e == cudaSuccess && c->log_cap) e = dalloc(&c->d_log_counts, (size_t)c->log_cap * (ndefg + nrxg));
+        if (e == cudaSuccess && c->log_cap) e = dalloc(&c->d_log_area, (size_t)c->log_cap * 2 * c->nz);
         if (e != cudaSuccess) { c->release_domain(); return c->fail(SCORE_ERR_NOMEM, std::string("device allocation: ") + cudaGetErrorString(e)); }
         a.pforce = c->d_pforce;
         a.st = c->d_state;
@@ -1753,6 +2034,23 @@ int score_grain_counts(score_ctx* c, uint32_t* rxg_counts, uint32_t* defg_counts
     if (e == cudaSuccess) e = cudaStreamSynchronize(c->stream);
     if (e != cudaSuccess) return c->cuda_fail(e, "grain counts");
     return SCORE_OK;
+}
+
+int score_grainevo_count(score_ctx* c, uint32_t* n) {
+    if (!c || !n) return SCORE_ERR_ARG;
+    *n = (uint32_t)c->log_info.size();
+    return SCORE_OK;
+}
+
+int score_grainevo(score_ctx* c, uint32_t i, score_grainevo_info* info, uint32_t* counts, uint32_t* rxarea) {
+    if (!c) return SCORE_ERR_ARG;
+    return grainevo_get(c, i, info, counts, rxarea);
+}
+
+int score_rediscr_kinetics(score_ctx* c, uint32_t nslots, double* t_out, double* rxvol_out, double* boxvol_out) {
+    if (!c) return SCORE_ERR_ARG;
+    const int s = rediscr({c}, nslots, nullptr, 0, t_out, rxvol_out, boxvol_out, c->err);
+    return s;
 }
 
 int score_get_timing(score_ctx* c, score_timing* out) {
@@ -1928,6 +2226,47 @@ int score_batch_grain_counts(score_batch* b, uint32_t d, uint32_t* rxg_counts, u
     if (!b || d >= b->dom.size()) return SCORE_ERR_ARG;
     const int s = score_grain_counts(b->dom[d], rxg_counts, defg_counts);
     return s == SCORE_OK ? s : b->dom_fail(b->dom[d], s);
+}
+
+int score_batch_grainevo_count(score_batch* b, uint32_t d, uint32_t* n) {
+    if (!b || d >= b->dom.size()) return SCORE_ERR_ARG;
+    return score_grainevo_count(b->dom[d], n);
+}
+
+int score_batch_grainevo(score_batch* b, uint32_t d, uint32_t i, score_grainevo_info* info, uint32_t* counts, uint32_t* rxarea) {
+    if (!b || d >= b->dom.size()) return SCORE_ERR_ARG;
+    const int s = grainevo_get(b->dom[d], i, info, counts, rxarea);
+    return s == SCORE_OK ? s : b->dom_fail(b->dom[d], s);
+}
+
+int score_batch_rediscr_kinetics(score_batch* b, uint32_t nslots, double* t_out, double* rxvol_out, double* boxvol_out) {
+    if (!b) return SCORE_ERR_ARG;
+    return rediscr(b->dom, nslots, nullptr, 0, t_out, rxvol_out, boxvol_out, b->err);
+}
+
+int score_batch_rediscr_texture(score_batch* b, uint32_t nslots, const uint32_t* grain_class, uint32_t nclass, double* t_out,
+                                double* vol_out) {
+    if (!b || !grain_class) return SCORE_ERR_ARG;
+    size_t n = 0;
+    for (score_ctx* c : b->dom) n += (size_t)c->ndefg + c->nrxg;
+    for (size_t i = 0; i < n; ++i)
+        if (grain_class[i] >= nclass) return b->fail(SCORE_ERR_ARG, "orientation class out of range");
+    return rediscr(b->dom, nslots, grain_class, nclass, t_out, vol_out, nullptr, b->err);
+}
+
+int score_batch_final_grain_sizes(score_batch* b, uint32_t* rx_cells) {
+    if (!b || !rx_cells) return SCORE_ERR_ARG;
+    size_t off = 0;
+    for (score_ctx* c : b->dom) {
+        if (!c->loaded) return b->fail(SCORE_ERR_STATE, "every domain must be loaded");
+        cudaSetDevice(c->device);
+        cudaError_t e = c->nrxg ? cudaMemcpyAsync(rx_cells + off, c->a.rxg_cnt, (size_t)c->nrxg * 4, cudaMemcpyDeviceToHost, c->stream)
+                                : cudaSuccess;
+        if (e == cudaSuccess) e = cudaStreamSynchronize(c->stream);
+        if (e != cudaSuccess) return b->fail(SCORE_ERR_CUDA, std::string("final grain sizes: ") + cudaGetErrorString(e));
+        off += c->nrxg;
+    }
+    return SCORE_OK;
 }
 
 int score_batch_get_timing(score_batch* b, score_timing* out) {

@@ -405,6 +405,7 @@ void params_default(score_params* p) {
     p->mobility_model = SCORE_MOBILITY_SEBALD_GOTTSTEIN;
     p->boundary = SCORE_BOUNDARY_REFERENCE; p->precision = SCORE_PRECISION_FP64;
     p->border_policy = SCORE_BORDER_REFERENCE_LIMIT;
+    p->rxarea_threshold = 13;  // log_OUTPUT_Diehl's log_rxareaprofile2( 13 ), SCORE_OnTheFlyCharacterization.cpp:649
 }
 
 int uds_read(const char* path, score_params* p, char* errbuf, size_t errlen) {
@@ -526,11 +527,27 @@ int uds_read(const char* path, score_params* p, char* errbuf, size_t errlen) {
         p->n_defrag = (uint32_t)xs.size();
         for (size_t i = 0; i < xs.size(); ++i) p->defrag_x[i] = xs[i];
     }
+    // SingleGrainVolOverTime, init_parameter_additional (SCORE_Kernel.cpp:939-957): column 2 (float), sorted
+    if (read_block(fh, "SingleGrainVolOverTime", b, err)) {
+        if (b.rows.size() > SCORE_MAX_TABLE) { err = "too many SingleGrainVolOverTime logpoints"; ok = false; goto done; }
+        std::vector<double> xs;
+        for (const auto& r : b.rows) {
+            if (b.types.size() < 2 || b.types[1] != 'f') { err = "SingleGrainVolOverTime column 2 must be f"; ok = false; goto done; }
+            double x = (double)r.f[1];
+            if (x < 0.0 || x > 1.0) { err = "invalid logpoint X"; ok = false; goto done; }
+            xs.push_back(x);
+        }
+        std::sort(xs.begin(), xs.end());
+        p->n_logpoints = (uint32_t)xs.size();
+        for (size_t i = 0; i < xs.size(); ++i) p->logpoint_x[i] = xs[i];
+    }
+    err.clear();
     // GB300 build options, optional block "GB300Options" (not part of the reference format)
     if (read_block(fh, "GB300Options", b, err)) {
         if (get_int(b, "Boundary", iv, err)) p->boundary = (int32_t)iv;
         if (get_int(b, "Precision", iv, err)) p->precision = (int32_t)iv;
         if (get_int(b, "BorderPolicy", iv, err)) p->border_policy = (int32_t)iv;
+        if (get_int(b, "RXAreaThreshold", iv, err)) p->rxarea_threshold = (uint32_t)iv;
     }
     err.clear();
 done:

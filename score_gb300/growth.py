@@ -18,7 +18,7 @@ from pathlib import Path
 import numpy as np
 
 from . import _abi
-from ._abi import GenParams, Params, ScoreError, StepStats, Timing, Tune
+from ._abi import GenParams, GrainEvoInfo, Params, ScoreError, StepStats, Timing, Tune
 
 
 def _ptr(a: np.ndarray | None):
@@ -70,6 +70,8 @@ class UdsSpec:
     recache: str = "1.0"
     defragmentation: int = 0
     defrag_x: list = field(default_factory=lambda: ["0.5"])
+    logpoints: list = field(default_factory=lambda: ["1.0"])   # SingleGrainVolOverTime: X of the grain-evolution log
+    area_threshold: int = 13                                   # RX area profile: smallest rx grain section counted
     G0: str = "85.0e9"
     bZeroCelsius: str = "248.5e-12"
     mobility_model: int = 1
@@ -176,10 +178,12 @@ class UdsSpec:
             a(f'"D{i}"\t{x}')
         a("")
         a("|| SingleGrainVolOverTime || *(sf) || Name, X")
-        a('"L0"\t1.0')
+        for i, x in enumerate(self.logpoints):
+            a(f'"L{i}"\t{x}')
         a("")
         a("|| GB300Options || *(ss) || Parameter, Value")
-        for k, v in [("Boundary", str(self.boundary)), ("Precision", str(self.precision)), ("BorderPolicy", str(self.border_policy))]:
+        for k, v in [("Boundary", str(self.boundary)), ("Precision", str(self.precision)), ("BorderPolicy", str(self.border_policy)),
+                     ("RXAreaThreshold", str(self.area_threshold))]:
             a(f'"{k}"\t"{v}"')
         a("")
         return "\n".join(L) + "\n"
@@ -349,6 +353,30 @@ class GrowthMachine:
         self._check(self._lib.score_get_timing(self._ctx, C.byref(t)))
         return t
 
+    def grainevo(self) -> list[tuple[GrainEvoInfo, np.ndarray, np.ndarray]]:
+        """The last run's grain-evolution log (log_grainevo + log_rxareaprofile at the
+        SingleGrainVolOverTime logpoints): per snapshot (info, counts[ndefg + nrxg],
+        rx area profile [nz, 2])."""
+        d = self.domain
+        n = C.c_uint32()
+        self._check(self._lib.score_grainevo_count(self._ctx, C.byref(n)))
+        out = []
+        for i in range(n.value):
+            info = GrainEvoInfo()
+            cnt = np.empty(d.ndefg + d.nrxg, dtype=np.uint32)
+            area = np.empty((d.nz, 2), dtype=np.uint32)
+            self._check(self._lib.score_grainevo(self._ctx, i, C.byref(info), _ptr(cnt), _ptr(area)))
+            out.append((info, cnt, area))
+        return out
+
+    def rediscr_kinetics(self, nslots: int) -> tuple[np.ndarray, np.ndarray, float]:
+        """X(t) of this domain on nslots rediscretized times: (t, rx volume, box volume)."""
+        t = np.empty(nslots, dtype=np.float64)
+        v = np.empty(nslots, dtype=np.float64)
+        box = C.c_double()
+        self._check(self._lib.score_rediscr_kinetics(self._ctx, nslots, _ptr(t), _ptr(v), C.byref(box)))
+        return t, v, box.value
+
     def tune(self) -> Tune:
         t = Tune()
         self._check(self._lib.score_get_tune(self._ctx, C.byref(t)))
@@ -461,6 +489,46 @@ class Batch:
         t = Timing()
         self._check(self._lib.score_batch_get_timing(self._b, C.byref(t)))
         return t
+
+    def grainevo(self, i: int) -> list[tuple[GrainEvoInfo, np.ndarray, np.ndarray]]:
+        """Domain i's grain-evolution log of the last run (see GrowthMachine.grainevo)."""
+        d = self.domains[i]
+        n = C.c_uint32()
+        self._check(self._lib.score_batch_grainevo_count(self._b, i, C.byref(n)))
+        out = []
+        for k in range(n.value):
+            info = GrainEvoInfo()
+            cnt = np.empty(d.ndefg + d.nrxg, dtype=np.uint32)
+            area = np.empty((d.nz, 2), dtype=np.uint32)
+            self._check(self._lib.score_batch_grainevo(self._b, i, k, C.byref(info), _ptr(cnt), _ptr(area)))
+            out.append((info, cnt, area))
+        return out
+
+    def rediscr_kinetics(self, nslots: int) -> tuple[np.ndarray, np.ndarray, float]:
+        """Ensemble recrystallization kinetics on nslots rediscretized times, on the device
+        (postprocess_rediscr_kinetics): (t, rx volume, box volume); X = rx volume / box volume."""
+        t = np.empty(nslots, dtype=np.float64)
+        v = np.empty(nslots, dtype=np.float64)
+        box = C.c_double()
+        self._check(self._lib.score_batch_rediscr_kinetics(self._b, nslots, _ptr(t), _ptr(v), C.byref(box)))
+        return t, v, box.value
+
+    def rediscr_texture(self, nslots: int, grain_class: np.ndarray, nclass: int) -> tuple[np.ndarray, np.ndarray]:
+        """Ensemble volume per orientation class on nslots rediscretized times, on the device
+        (postprocess_rediscr_macrotexture); grain_class: every domain's ndefg + nrxg classes in
+        domain order.  Returns (t, volume[nslots, nclass])."""
+        cls = np.ascontiguousarray(grain_class, dtype=np.uint32)
+        t = np.empty(nslots, dtype=np.float64)
+        v = np.empty((nslots, nclass), dtype=np.float64)
+        self._check(self._lib.score_batch_rediscr_texture(self._b, nslots, _ptr(cls), nclass, _ptr(t), _ptr(v)))
+        return t, v
+
+    def final_grain_sizes(self) -> np.ndarray:
+        """Every domain's rx grains' final cell counts, in domain order."""
+        n = sum(d.nrxg for d in self.domains)
+        out = np.empty(n, dtype=np.uint32)
+        self._check(self._lib.score_batch_final_grain_sizes(self._b, _ptr(out)))
+        return out
 
     def tune(self) -> Tune:
         t = Tune()

@@ -75,3 +75,32 @@ def load_config(name: str, tmp_path: Path):
     g["rxg_counts"] = z["rxg_counts"]
     g["defg_counts"] = z["defg_counts"]
     return p, d, g
+
+
+def load_evolution(tmp_path: Path):
+    """The evolution-ensemble fixture: per domain (params, domain, reference log dict), plus the
+    ensemble's rediscretization (tmax, nslots, nclass, kinetics, texture) made from the reference."""
+    z = np.load(GOLDEN / "evolution_ensemble.npz")
+    doms = []
+    k = 0
+    while f"d{k}_uds" in z:
+        uds = tmp_path / f"evo{k}.uds"
+        uds.write_text(str(z[f"d{k}_uds"]))
+        p = sg.read_uds(uds)
+        nx, ny, nz = (int(v) for v in z[f"d{k}_dims"])
+        d = sg.Domain(nx, ny, nz, z[f"d{k}_grid"].astype(np.uint32).reshape(nz, ny, nx), z[f"d{k}_defg_quat"],
+                      z[f"d{k}_defg_rho0"], z[f"d{k}_rxg_quat"], z[f"d{k}_rxg_site"], z[f"d{k}_rxg_tincub"])
+        g = {a: z[f"d{k}_{a}"] for a in ("t_end", "cls", "snap_t", "snap_X", "snap_step", "snap_Sv", "snap_counts", "areas",
+                                          "interp", "final")}
+        g["t_end"] = float(g["t_end"])
+        doms.append((p, d, g))
+        k += 1
+    ens = {a: z[a] for a in ("kinetics", "texture")}
+    ens.update({"tmax": float(z["tmax"]), "nslots": int(z["nslots"]), "nclass": int(z["nclass"])})
+    return doms, ens
+
+
+def evo_descriptor(d, g) -> dict:
+    """An oracle post-processing descriptor of a domain's reference log."""
+    return {"ndefg": d.ndefg, "nrxg": d.nrxg, "t": g["snap_t"], "counts": g["snap_counts"], "final": g["final"],
+            "tsimend": g["t_end"], "cells": d.ncells, "cls": g["cls"]}

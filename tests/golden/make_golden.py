@@ -54,6 +54,11 @@ CASES = {
                         {"ori_mode": 1, "ncomp": 3, "scatter_deg": 10.0, "rho_mode": 1, "rho_lo": 1e14, "rho_hi": 5e15}),
 }
 PTAB = (40, 80, 111)  # nrxg, ndefg, seed
+# ensemble of the on-the-fly characterization and post-processing fixture: per domain (nx, ny, nz, grains,
+# nuclei, seed); logpoints, RX area threshold, rediscretization slots, orientation classes
+EVO_DOMAINS = [(50, 50, 50, 20, 12, 201), (56, 50, 52, 30, 24, 202), (50, 54, 50, 25, 40, 203)]
+EVO_LOGPOINTS = ["0.0", "0.05", "0.1", "0.2", "0.35", "0.5", "0.65", "0.8", "0.9", "0.95"]
+EVO_AREA, EVO_SLOTS, EVO_CLASSES = 13, 40, 4
 # benchmark configurations: name -> (edge, grains, nuclei, seed)
 CONFIGS = {"config0": (128, 500, 200, 0), "config1": (512, 20000, 50000, 0)}
 
@@ -114,6 +119,84 @@ def make_config(name: str, wd: Path) -> Path:
     return out
 
 
+def read_evo(wd: Path, d: sg.Domain):
+    """Snapshots (t, X, step, Sv, counts) and RX area profiles the harness wrote."""
+    G = d.ndefg + d.nrxg
+    raw = (wd / "out.grainevo").read_bytes()
+    rec = 24 + 4 * G
+    snaps = []
+    for i in range(len(raw) // rec):
+        t, X = np.frombuffer(raw[i * rec:i * rec + 16], dtype=np.float64)
+        st, sv = np.frombuffer(raw[i * rec + 16:i * rec + 24], dtype=np.uint32)
+        snaps.append((t, X, st, sv, np.frombuffer(raw[i * rec + 24:(i + 1) * rec], dtype=np.uint32)))
+    raw = (wd / "out.rxprofile").read_bytes()
+    rec = 24 + 8 * d.nz
+    areas = [np.frombuffer(raw[i * rec + 24:(i + 1) * rec], dtype=np.uint32).reshape(d.nz, 2) for i in range(len(raw) // rec)]
+    return snaps, areas
+
+
+def make_evo(wd: Path) -> Path:
+    """Grain-evolution log, RX area profiles and ensemble post-processing of a 3-domain ensemble, all
+    from the reference: its log_grainevo / log_rxareaprofile at the logpoints and its
+    get_interpCellCount at the rediscretized times; the ensemble sums are formed from those values in
+    the order of postprocess_rediscr_kinetics / postprocess_rediscr_macrotexture."""
+    import os
+    doms, specs = [], []
+    for k, (nx, ny, nz, ng, nn, seed) in enumerate(EVO_DOMAINS):
+        doms.append(sg.generate_domain(nx, ny, nz, ng, nn, seed=seed))
+        specs.append(sg.UdsSpec(nx=nx, ny=ny, nz=nz, logpoints=EVO_LOGPOINTS, area_threshold=EVO_AREA))
+    os.environ["SCORE_LOG_AREA"] = str(EVO_AREA)
+    first = [oracle.run_ref("loop", specs[k].write(wd / f"evo{k}.uds"), d, workdir=wd / f"evo{k}")
+             for k, d in enumerate(doms)]
+    tmax = 0.0
+    for r in first:
+        t_end = float.fromhex(r["t_end"])
+        if t_end >= tmax:
+            tmax = t_end
+    os.environ["SCORE_REDISCR"] = f"{EVO_SLOTS} {tmax!r}"
+    out = {"tmax": np.array(tmax), "nslots": np.array(EVO_SLOTS), "nclass": np.array(EVO_CLASSES),
+           "area_threshold": np.array(EVO_AREA)}
+    rng = np.random.default_rng(7)
+    kin = np.zeros(EVO_SLOTS)
+    tex = np.zeros((EVO_SLOTS, EVO_CLASSES))
+    for k, d in enumerate(doms):
+        r = oracle.run_ref("loop", wd / f"evo{k}.uds", d, workdir=wd / f"evo{k}b")
+        snaps, areas = read_evo(r["workdir"], d)
+        G = d.ndefg + d.nrxg
+        interp = np.fromfile(r["workdir"] / "out.interp", dtype=np.float64).reshape(EVO_SLOTS, G)
+        cls = rng.integers(0, EVO_CLASSES, size=G).astype(np.uint32)
+        # postprocess_rediscr_kinetics (SCORE_SolitaryUnitAveraging.cpp:576-600): sums in grain order
+        for n in range(EVO_SLOTS):
+            dv = 0.0
+            for g in range(d.ndefg):
+                dv = dv + float(interp[n, g])
+            kin[n] = kin[n] + (float(d.ncells) - dv)
+        # postprocess_rediscr_macrotexture (:705-747): deformed then rx grains, per class
+        for n in range(EVO_SLOTS):
+            acc = [0.0] * EVO_CLASSES
+            for g in range(G):
+                acc[cls[g]] += float(interp[n, g])
+            for c in range(EVO_CLASSES):
+                tex[n, c] += acc[c]
+        out.update({f"d{k}_uds": np.array(specs[k].text()), **{f"d{k}_{a}": b for a, b in domain_arrays(d).items()},
+                    f"d{k}_t_end": np.array(float.fromhex(r["t_end"])), f"d{k}_cls": cls,
+                    f"d{k}_snap_t": np.array([x[0] for x in snaps]), f"d{k}_snap_X": np.array([x[1] for x in snaps]),
+                    f"d{k}_snap_step": np.array([x[2] for x in snaps], dtype=np.uint32),
+                    f"d{k}_snap_Sv": np.array([x[3] for x in snaps], dtype=np.uint32),
+                    f"d{k}_snap_counts": np.array([x[4] for x in snaps]), f"d{k}_areas": np.array(areas),
+                    f"d{k}_interp": interp,
+                    f"d{k}_final": np.array([r["defg"].get(i, 0) for i in range(d.ndefg)] + [r["rxg"].get(i, 0) for i in range(d.nrxg)],
+                                            dtype=np.uint32)})
+    del os.environ["SCORE_LOG_AREA"], os.environ["SCORE_REDISCR"]
+    out["kinetics"] = kin
+    out["texture"] = tex
+    path = HERE / "evolution_ensemble.npz"
+    np.savez_compressed(path, **out)
+    print(f"{path.name}: {len(doms)} domains, {[len(read_evo(wd / f'evo{k}b', doms[k])[0]) for k in range(len(doms))]} snapshots, "
+          f"{path.stat().st_size // 1024} KiB")
+    return path
+
+
 def make_ptab(wd: Path) -> Path:
     nrxg, ndefg, seed = PTAB
     d = sg.generate_domain(50, 50, 50, ndefg, nrxg, seed=seed)
@@ -142,6 +225,8 @@ def main() -> None:
                 make_case(name, kw, geo, gkw, wd)
         if not only or "ptab" in only:
             make_ptab(wd)
+        if not only or "evo" in only:
+            make_evo(wd)
         for name in CONFIGS:
             if not only or name in only:
                 make_config(name, wd)

@@ -37,7 +37,7 @@ def test_library_is_the_in_tree_build(built):
 
 def test_status_strings(built):
     lib = _abi.load()
-    assert lib.score_abi_version() == 3
+    assert lib.score_abi_version() == 4
     assert lib.score_status_string(0) == b"ok"
     for code in range(-1, -12, -1):
         s = lib.score_status_string(code)
