@@ -533,6 +533,65 @@ class BatchWorkload:
         self.b.close()
 
 
+LOGPOINTS = ["0.0", "0.1", "0.2", "0.3", "0.4", "0.5", "0.6", "0.7", "0.8", "0.9"]
+
+
+def measure_synthesis(sg, local) -> dict:
+    """Deformed-structure synthesis of the headline domain (512^3, 20,000 Voronoi grains, 50,000 nuclei):
+    the device label fill (score_generate_domain_gpu) against the host generator on every host core,
+    each the whole public call (seeds, fill, orientations, nuclei, grid in a host buffer)."""
+    t0 = time.perf_counter()
+    dh = sg.generate_domain(N_EDGE, N_EDGE, N_EDGE, N_GRAINS, N_NUCLEI, seed=0)
+    host_s = time.perf_counter() - t0
+    sg.generate_domain(64, 64, 64, 100, 10, seed=1, device=local)  # warm-up: module load
+    t0 = time.perf_counter()
+    dd = sg.generate_domain(N_EDGE, N_EDGE, N_EDGE, N_GRAINS, N_NUCLEI, seed=0, device=local)
+    gpu_s = time.perf_counter() - t0
+    same = all(np.array_equal(getattr(dh, f), getattr(dd, f)) for f in ("grid", "defg_quat", "defg_rho0", "rxg_quat", "rxg_site"))
+    return {"workload": "512^3 periodic Voronoi, 20000 grains, 50000 nuclei (the headline domain)",
+            "gpu_s": gpu_s, "host_s": host_s, "host_threads": os.cpu_count(), "gpu_cells_per_s": N_EDGE ** 3 / gpu_s,
+            "identical": bool(same)}
+
+
+def measure_postprocessing(sg, local, doms, shapes, runs: int) -> dict:
+    """On-the-fly characterization and ensemble post-processing on the batched ensemble: the run with
+    the grain-evolution log at 10 logpoints (counts and RX area profile, threshold 13) against the
+    same run without it, then the device post-processing of the 64 logs (1000 rediscretized times:
+    kinetics, and macrotexture over 8 orientation classes), timed through the public API."""
+    out = {}
+    with tempfile.TemporaryDirectory() as td:
+        plog = [sg.read_uds(sg.UdsSpec(nx=nx, ny=ny, nz=nz, logpoints=LOGPOINTS).write(Path(td) / f"{k}.uds"))
+                for k, (nx, ny, nz, *_r) in enumerate(shapes)]
+    with sg.Batch(plog, device=local) as b:
+        for k, d in enumerate(doms):
+            b.load_domain(k, d)
+        ms = 0.0
+        for r in range(1 + runs):
+            b.restart()
+            b.place_nuclei()
+            b.run_until(X_TARGET)
+            if r:
+                ms += b.timing().run_ms
+        nsnap = sum(len(b.grainevo(k)) for k in range(len(doms)))
+        grains = sum(d.ndefg + d.nrxg for d in doms)
+        cls = np.concatenate([np.arange(d.ndefg + d.nrxg, dtype=np.uint32) % 8 for d in doms])
+        tk, tt = [], []
+        for _ in range(5):
+            t0 = time.perf_counter()
+            b.rediscr_kinetics(1000)
+            tk.append(time.perf_counter() - t0)
+            t0 = time.perf_counter()
+            b.rediscr_texture(1000, cls, 8)
+            tt.append(time.perf_counter() - t0)
+    kin, tex = statistics.median(tk), statistics.median(tt)
+    out.update({"logged_run_ms": ms / runs, "snapshots": nsnap,
+                "rediscr_kinetics_ms": 1e3 * kin, "rediscr_texture_ms": 1e3 * tex,
+                "interpolations_per_s_kinetics": 1000 * sum(d.ndefg for d in doms) / kin,
+                "interpolations_per_s_texture": 1000 * grains / tex,
+                "how": "host wall time of the public call (upload of the logs' times and classes, two kernels, download)"})
+    return out
+
+
 def measure_batched(sg, args, local) -> dict:
     """The metric's ratio on the batched ensemble (64 domains, edges uniform in [64, 256]
     per axis, 100-5000 grains, 50-2000 nuclei; domain i from seed i): the batched path in
@@ -566,9 +625,9 @@ def measure_batched(sg, args, local) -> dict:
             labs = [b.labels(k) for k in range(len(doms))]
             xs = [np.array([s.X for s in b.trace(k)]) for k in range(len(doms))]
             launches = b.timing().kernel_launches
-        return sv / (ms / 1e3), labs, xs, launches
+        return sv / (ms / 1e3), labs, xs, ms / runs
 
-    v64, lab64, x64, _ = batch_rate(p64)
+    v64, lab64, x64, ms64 = batch_rate(p64)
     v32, lab32, x32, _ = batch_rate(p32)
     errs = []
     for k, d in enumerate(doms):
@@ -594,6 +653,9 @@ def measure_batched(sg, args, local) -> dict:
     finally:
         for gm in gms:
             gm.close()
+    post = measure_postprocessing(sg, local, doms, shapes, runs)
+    post["unlogged_run_ms"] = ms64
+    out["characterization"] = post
     out.update({
         "fp64_batched_updates_per_s": v64, "fp32_kahan_batched_updates_per_s": v32,
         "plain_fp64_same_domains_updates_per_s": vseq,
@@ -691,6 +753,7 @@ def main():
     if args.workload == "plain" and args.edge == N_EDGE and args.precision == 0 and not args.no_batched:
         batched = measure_batched(sg, args, local)
         batched["ratio_fp32_batched_vs_plain_fp64_512"] = batched["fp32_kahan_batched_updates_per_s"] / value
+        batched["synthesis"] = measure_synthesis(sg, local)
 
     if rank == 0:
         peak, peak_kind = measured_peak_gbs()

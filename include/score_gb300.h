@@ -387,6 +387,15 @@ typedef struct score_gen_params {
 int  score_gen_default(score_gen_params* out);
 int  score_generate_domain(const score_gen_params* g, uint32_t* grid, double* defg_quat, double* defg_rho0,
                            double* rxg_quat, uint32_t* rxg_site, double* rxg_tincub);
+/*
+ * The same domain with the Voronoi label fill on the device: deformed-structure synthesis on the
+ * GPU (the reference synthesizes its deformed structures on the host, src/SCORE_StructureSynthesis.cpp:
+ * cuboid voxelizer :466-529, unit-speed CA tessellation :164-345).  Every output is bit for bit
+ * score_generate_domain's: the nearest-seed search and its FP64 arithmetic are the host's.  The
+ * label grid comes back into the host buffer `grid` (the nuclei placement reads it).
+ */
+int  score_generate_domain_gpu(const score_gen_params* g, uint32_t* grid, double* defg_quat, double* defg_rho0,
+                               double* rxg_quat, uint32_t* rxg_site, double* rxg_tincub, int device);
 
 #ifdef __cplusplus
 }

@@ -150,6 +150,7 @@ SIGNATURES = {
     "score_mobility_table_noalloc": (C.c_int, [_P(Params), _vp, _u32, _vp, _u32, _vp, _vp, _vp]),
     "score_gen_default": (C.c_int, [_P(GenParams)]),
     "score_generate_domain": (C.c_int, [_P(GenParams), _vp, _vp, _vp, _vp, _vp, _vp]),
+    "score_generate_domain_gpu": (C.c_int, [_P(GenParams), _vp, _vp, _vp, _vp, _vp, _vp, C.c_int]),
 }
 
 _lib = None

@@ -18,7 +18,9 @@
 #include <unordered_set>
 #include <vector>
 #include <algorithm>
+#include <functional>
 #include "../../include/score_gb300.h"
+#include "host_generate.h"
 
 namespace {
 
@@ -113,13 +115,7 @@ void det_scatter(Rng& g, const double q[4], double sigma_rad, double out[4]) {
     for (int i = 0; i < 4; ++i) out[i] /= n;
 }
 
-struct Voronoi {
-    uint32_t n[3];
-    double scale[3];                // metric: d^2 = sum ((dx_i)/scale_i)^2
-    std::vector<double> pos;        // 3 per seed
-    uint32_t nb[3];                 // buckets per axis
-    double bw[3];                   // bucket width in cells
-    std::vector<uint32_t> start, items;
+struct Voronoi : score::VoronoiGrid {
 
     void build() {
         const size_t S = pos.size() / 3;
@@ -193,6 +189,26 @@ struct Voronoi {
 
 }  // namespace
 
+namespace score {
+
+// Host fill: every cell's nearest seed, z slabs spread over the host threads.
+int fill_voronoi_host(const VoronoiGrid& vg, uint32_t* grid) {
+    const Voronoi& vo = static_cast<const Voronoi&>(vg);
+    unsigned nth = std::max(1u, std::min(64u, std::thread::hardware_concurrency()));
+    std::vector<std::thread> th;
+    for (unsigned t = 0; t < nth; ++t)
+        th.emplace_back([&, t]() {
+            for (uint32_t z = t; z < vo.n[2]; z += nth)
+                for (uint32_t y = 0; y < vo.n[1]; ++y)
+                    for (uint32_t x = 0; x < vo.n[0]; ++x)
+                        grid[(size_t)x + (size_t)vo.n[0] * (y + (size_t)vo.n[1] * z)] = vo.nearest(x, y, z);
+        });
+    for (auto& t : th) t.join();
+    return SCORE_OK;
+}
+
+}  // namespace score
+
 extern "C" int score_gen_default(score_gen_params* g) {
     if (!g) return SCORE_ERR_ARG;
     memset(g, 0, sizeof *g);
@@ -206,8 +222,10 @@ extern "C" int score_gen_default(score_gen_params* g) {
     return SCORE_OK;
 }
 
-extern "C" int score_generate_domain(const score_gen_params* g, uint32_t* grid, double* defg_quat, double* defg_rho0,
-                                     double* rxg_quat, uint32_t* rxg_site, double* rxg_tincub) {
+namespace score {
+
+int generate_domain_with(const score_gen_params* g, uint32_t* grid, double* defg_quat, double* defg_rho0, double* rxg_quat,
+                         uint32_t* rxg_site, double* rxg_tincub, const std::function<int(const VoronoiGrid&, uint32_t*)>& fill) {
     if (!g || !grid || !defg_quat || !defg_rho0 || !rxg_quat || !rxg_site) return SCORE_ERR_ARG;
     if (g->nx == 0 || g->ny == 0 || g->nz == 0 || g->ngrains == 0) return SCORE_ERR_ARG;
     const uint64_t N = (uint64_t)g->nx * g->ny * g->nz;
@@ -225,16 +243,8 @@ extern "C" int score_generate_domain(const score_gen_params* g, uint32_t* grid, 
         vo.pos[3 * s + 2] = rng.u01() * g->nz;
     }
     vo.build();
-    unsigned nth = std::max(1u, std::min(64u, std::thread::hardware_concurrency()));
-    std::vector<std::thread> th;
-    for (unsigned t = 0; t < nth; ++t)
-        th.emplace_back([&, t]() {
-            for (uint32_t z = t; z < g->nz; z += nth)
-                for (uint32_t y = 0; y < g->ny; ++y)
-                    for (uint32_t x = 0; x < g->nx; ++x)
-                        grid[(size_t)x + (size_t)g->nx * (y + (size_t)g->ny * z)] = vo.nearest(x, y, z);
-        });
-    for (auto& t : th) t.join();
+    const int fs = fill(vo, grid);  // the seed pass is the only RNG use before the fill
+    if (fs != SCORE_OK) return fs;
 
     // 2) grain orientations and dislocation densities
     std::vector<double> comps((size_t)std::max(1u, g->ncomp) * 4);
@@ -281,4 +291,11 @@ extern "C" int score_generate_domain(const score_gen_params* g, uint32_t* grid, 
         }
     }
     return SCORE_OK;
+}
+
+}  // namespace score
+
+extern "C" int score_generate_domain(const score_gen_params* g, uint32_t* grid, double* defg_quat, double* defg_rho0,
+                                     double* rxg_quat, uint32_t* rxg_site, double* rxg_tincub) {
+    return score::generate_domain_with(g, grid, defg_quat, defg_rho0, rxg_quat, rxg_site, rxg_tincub, score::fill_voronoi_host);
 }

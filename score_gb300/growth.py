@@ -235,12 +235,15 @@ class Domain:
         return path
 
 
-def generate_domain(nx: int, ny: int, nz: int, ngrains: int, nnuclei: int, seed: int = 0, **kw) -> Domain:
+def generate_domain(nx: int, ny: int, nz: int, ngrains: int, nnuclei: int, seed: int = 0, device: int | None = None,
+                    **kw) -> Domain:
     """Deterministic synthetic domain (identical bits on x86-64 and aarch64 hosts).
 
     Keyword overrides map onto score_gen_params: rho_mean, rho_sigma, rho_mode,
     rho_lo, rho_hi, aspect (3-tuple), ori_mode, ncomp, scatter_deg, site_mode,
-    gb_fraction, nucleation_rate.
+    gb_fraction, nucleation_rate.  With `device` the Voronoi label fill runs on that
+    GPU (score_generate_domain_gpu): the same bits, the CUDA library instead of the
+    host-only one.
     """
     g = GenParams()
     host_lib().score_gen_default(C.byref(g))
@@ -257,7 +260,10 @@ def generate_domain(nx: int, ny: int, nz: int, ngrains: int, nnuclei: int, seed:
     rq = np.empty((nnuclei, 4), dtype=np.float64)
     site = np.empty(nnuclei, dtype=np.uint32)
     tinc = np.empty(nnuclei, dtype=np.float64)
-    s = host_lib().score_generate_domain(C.byref(g), _ptr(grid), _ptr(dq), _ptr(rho), _ptr(rq), _ptr(site), _ptr(tinc))
+    if device is None:
+        s = host_lib().score_generate_domain(C.byref(g), _ptr(grid), _ptr(dq), _ptr(rho), _ptr(rq), _ptr(site), _ptr(tinc))
+    else:
+        s = lib().score_generate_domain_gpu(C.byref(g), _ptr(grid), _ptr(dq), _ptr(rho), _ptr(rq), _ptr(site), _ptr(tinc), device)
     if s != _abi.OK:
         raise ScoreError(s, "domain generation failed")
     return Domain(nx, ny, nz, grid, dq, rho, rq, site, tinc)
