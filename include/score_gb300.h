@@ -325,6 +325,35 @@ int  score_batch_rediscr_texture(score_batch* b, uint32_t nslots, const uint32_t
                                  double* t_out, double* vol_out);
 int  score_batch_final_grain_sizes(score_batch* b, uint32_t* rx_cells);
 
+/*
+ * Percolation analysis of the recrystallized and infected cells on the device (caHdl::log_PERCOLATION,
+ * src/SCORE_OnTheFlyCharacterization.cpp:777-875, and percAnalyzer, src/SCORE_PercAnalyzer.cpp), between
+ * steps.  Cells with grid value >= ndefg (binarize_partiallyrxed_microstructure, :732-774) form clusters
+ * over the six face neighbours, not periodic; the cell at the origin never joins one (the reference labels
+ * clusters with cell indices and reads label 0 as "not recrystallized").  Clusters are numbered 1..n in
+ * the order of their first cell (compactify, :334-390).
+ *   SCORE_PERC_REFERENCE  the reference's clusters: its Hoshen-Kopelman scan links a cell with all three
+ *                         lower neighbours present to the lower y and z ones only (:218-225), which can
+ *                         split a true cluster (its checkLabeling then reports the split)
+ *   SCORE_PERC_CONNECTED  the true 6-connected clusters
+ * out: count, largest, P_L = largest / N, percolates (a cluster touches both faces of an axis, :500-615)
+ * with the axes in `spans`; sizes: the cluster sizes ascending (determine_clustersize_distr, :617-656),
+ * the first sizes_cap of them, or NULL; labels: every cell's cluster (0 = none), N values, or NULL.
+ * Reference domains are cubes; any box is accepted here.
+ */
+#define SCORE_PERC_REFERENCE 0
+#define SCORE_PERC_CONNECTED 1
+typedef struct score_perc_result {
+    uint32_t n_clusters;
+    uint32_t largest;
+    double PL;
+    int32_t percolates;
+    uint32_t spans;            /* bit 0: along x, 1: y, 2: z */
+} score_perc_result;
+int  score_percolation_analyze(score_ctx* c, int mode, score_perc_result* out, uint32_t* sizes, uint32_t sizes_cap, uint32_t* labels);
+int  score_batch_percolation_analyze(score_batch* b, uint32_t d, int mode, score_perc_result* out, uint32_t* sizes, uint32_t sizes_cap,
+                             uint32_t* labels);
+
 /* FP64 mobility weight P(rxg,defg) on the host, the reference's formula
  * (SCORE_Kernel.cpp:2460-2527, SCORE_Math.cpp:558-622,1067-1130) */
 int  score_mobility_weight(const score_params* p, const double* rxg_q, const double* defg_q, double* P);

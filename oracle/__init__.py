@@ -97,6 +97,9 @@ def _load():
         lib.oracle_log_count.argtypes = [C.c_void_p]
         lib.oracle_log_get.restype = C.c_int
         lib.oracle_log_get.argtypes = [C.c_void_p, C.c_uint32] + [C.c_void_p] * 6
+        lib.oracle_binarize.argtypes = [C.c_void_p, C.c_void_p]
+        lib.oracle_percolation.restype = C.c_int
+        lib.oracle_percolation.argtypes = [C.c_void_p, C.c_uint32, C.c_uint32, C.c_uint32, C.c_int] + [C.c_void_p] * 6
         lib.oracle_interp_count.restype = C.c_double
         lib.oracle_interp_count.argtypes = [C.c_void_p, C.c_uint32, C.c_double]
         lib.oracle_rediscr_kinetics.argtypes = [C.c_void_p, C.c_uint32, C.c_uint32, C.c_void_p, C.c_void_p, C.c_void_p]
@@ -181,6 +184,12 @@ class Sim:
             out.append({"t": t.value, "X": X.value, "step": st.value, "Sv": sv.value, "counts": cnt, "area": area})
         return out
 
+    def binarize(self) -> np.ndarray:
+        """1 for recrystallized and infected cells (grid value >= ndefg), as the reference binarizes."""
+        b = np.empty(self.ncells, dtype=np.uint8)
+        self._lib.oracle_binarize(self._h, _p(b))
+        return b
+
     def close(self) -> None:
         if self._h:
             self._lib.oracle_destroy(self._h)
@@ -232,6 +241,23 @@ def rediscr_texture(domains: list, nslots: int, nclass: int):
     v = np.empty((nslots, nclass), dtype=np.float64)
     _load().oracle_rediscr_macrotexture(arr, len(domains), nslots, nclass, _p(t), _p(v))
     return t, v
+
+
+def percolation(binarized: np.ndarray, nx: int, ny: int, nz: int, reference_scan: bool = False) -> dict:
+    """Clusters of the 1-cells (6-connected, not periodic): the reference's sequential Hoshen-Kopelman
+    scan (reference_scan) or the true components; labels in order of first appearance, counts,
+    largest, spanning axes and the ascending sizes (SCORE_PercAnalyzer.cpp)."""
+    b = np.ascontiguousarray(binarized, dtype=np.uint8).ravel()
+    N = nx * ny * nz
+    labels = np.empty(N, dtype=np.uint32)
+    sizes = np.empty(N // 2 + 2, dtype=np.uint32)
+    n, big, perc, spans = C.c_uint32(), C.c_uint32(), C.c_int(), C.c_uint32()
+    s = _load().oracle_percolation(_p(b), nx, ny, nz, int(reference_scan), _p(labels), C.byref(n), C.byref(big), C.byref(perc),
+                                   C.byref(spans), _p(sizes))
+    if s != 0:
+        raise MemoryError("oracle_percolation")
+    return {"labels": labels, "n_clusters": n.value, "largest": big.value, "percolates": bool(perc.value),
+            "spans": spans.value, "sizes": sizes[: n.value].copy()}
 
 
 def mobility_weight(params, qr, qd) -> float:

@@ -31,6 +31,11 @@
  *           it then evaluates the reference's caHdl::get_interpCellCount
  *           (SCORE_SolitaryUnitAveraging.cpp:1304-1365) for every grain at the ensemble's
  *           rediscretized times (postprocess_initrediscrtimes, :50-80).
+ *           With SCORE_PERC=1 it ends with the reference's percolation analysis of the final
+ *           state (log_PERCOLATION, SCORE_OnTheFlyCharacterization.cpp:777-875: the binarized
+ *           structure of binarize_partiallyrxed_microstructure, then percAnalyzer's
+ *           Hoshen-Kopelman labeling, compactify, checkLabeling, percolates and the sorted
+ *           cluster-size distribution, SCORE_PercAnalyzer.cpp:118-665).
  *   asis  : calls the unmodified caHdl::solve_RXGROWTH and records t_end, step_end
  *           and the per-grain cell counts; used to prove `loop` is faithful.
  *   ptab  : dumps P(rxg,defg) from caregionMemHdl::reg_calc_mobilityweight
@@ -47,6 +52,7 @@
 #include <vector>
 #include <string>
 #include <cstdlib>
+#include <sstream>
 
 /* grain-evolution logging of the loop mode (SCORE_LOG_AREA), off when < 0 */
 static long g_log_area = -1;
@@ -369,6 +375,36 @@ int main(int argc, char** argv) {
         }
         if (a) fclose(a);
         ok = g && a;
+    }
+    if (ok && getenv("SCORE_PERC") && d.nx == d.ny && d.nx == d.nz) {
+        /* percolation record: n clusters, largest cluster, percolates, checkLabeling failed (u32), the sorted cluster sizes (u32),
+           then the binarized structure (one byte per cell) */
+        std::vector<bool>* bin = new std::vector<bool>;
+        ca->binarize_partiallyrxed_microstructure(bin);
+        std::vector<uint8_t> bytes(bin->size());
+        for (size_t i = 0; i < bin->size(); ++i) bytes[i] = (*bin)[i] ? 1 : 0;
+        percAnalyzer* hk = new percAnalyzer;
+        hk->initialize(bin, d.nx);
+        delete bin;
+        std::cout.rdbuf(sink.rdbuf());
+        hk->hoshen_kopelman();
+        hk->compactify();
+        std::ostringstream cerr_text;  /* checkLabeling reports a cell whose neighbour carries another label on cerr */
+        std::streambuf* keep_err = std::cerr.rdbuf(cerr_text.rdbuf());
+        hk->checkLabeling();
+        std::cerr.rdbuf(keep_err);
+        const bool perc = hk->percolates();
+        hk->determine_clustersize_distr();
+        std::cout.rdbuf(keep);
+        const uint32_t split = cerr_text.str().find("failed assertion") != std::string::npos ? 1u : 0u;
+        const uint32_t hdr[4] = {hk->getNCluster(), hk->getClusterSize(), perc ? 1u : 0u, split};
+        std::vector<uint32_t> dist(hdr[0]);
+        if (hdr[0]) hk->handover_distribution(dist.data());
+        delete hk;
+        FILE* f = fopen((out + ".perc").c_str(), "wb");
+        ok = f && fwrite(hdr, 4, 4, f) == 4 && fwrite(dist.data(), 4, dist.size(), f) == dist.size() &&
+             fwrite(bytes.data(), 1, bytes.size(), f) == bytes.size();
+        if (f) fclose(f);
     }
     const char* rd = getenv("SCORE_REDISCR");
     if (ok && rd) {

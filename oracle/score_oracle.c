@@ -758,3 +758,111 @@ int oracle_run(const score_params* p, const uint32_t* grid, const double* defg_q
     oracle_destroy(o);
     return status;
 }
+
+/* ------------------------------------------------------------------ percolation */
+/* caHdl::binarize_partiallyrxed_microstructure, SCORE_OnTheFlyCharacterization.cpp:732-774: recrystallized
+   and currently infected cells (grid value >= ndefg) are 1 */
+void oracle_binarize(const oracle_sim* o, uint8_t* bin) {
+    const sim* s = &o->S;
+    for (uint64_t i = 0; i < s->N; i++) bin[i] = s->grid[i] >= s->ndefg ? 1 : 0;
+}
+
+static uint32_t uf_root(uint32_t* id, uint32_t p) {  /* UF::find_root with path compression, SCORE_PercAnalyzer.h:133-143 */
+    uint32_t root = p;
+    while (root != id[root]) root = id[root];
+    while (p != root) { uint32_t q = id[p]; id[p] = root; p = q; }
+    return root;
+}
+static uint32_t uf_merge(uint32_t* id, uint32_t* sz, uint32_t x, uint32_t y) {  /* UF::merge, :146-160 */
+    uint32_t i = uf_root(id, x), j = uf_root(id, y);
+    if (i == j) return i;
+    if (sz[i] < sz[j]) { id[i] = j; sz[j] += sz[i]; return j; }
+    id[j] = i; sz[i] += sz[j];
+    return i;
+}
+static int cmp_u32(const void* a, const void* b) {
+    uint32_t x = *(const uint32_t*)a, y = *(const uint32_t*)b;
+    return (x > y) - (x < y);
+}
+
+/* Clusters of the 1-cells, 6-connected, not periodic, in the reference's terms (percAnalyzer,
+   SCORE_PercAnalyzer.cpp): labels 1..n in the order of each cluster's first cell (compactify, :334-390),
+   0 outside every cluster; percolates when a cluster touches both faces of one axis (percolates,
+   :500-615); sizes ascending (determine_clustersize_distr, :617-656).
+   reference_scan = 1 runs the reference's sequential Hoshen-Kopelman scan itself (hk3d_core_nonperiodic,
+   :161-226, with its union-find): labels are cell indices and 0 means "not recrystallized", so the
+   origin cell never joins a cluster, and a cell whose three lower neighbours are all labelled merges only
+   the lower two (:218-225), which can leave one true cluster split in two.
+   reference_scan = 0 computes the true 6-connected clusters, the origin cell left out as the reference
+   leaves it out. */
+int oracle_percolation(const uint8_t* bin, uint32_t nx, uint32_t ny, uint32_t nz, int reference_scan, uint32_t* labels,
+                       uint32_t* n_clusters, uint32_t* largest, int* percolates, uint32_t* spans, uint32_t* sizes) {
+    const uint64_t N = (uint64_t)nx * ny * nz, nxy = (uint64_t)nx * ny;
+    uint32_t* id = malloc(N * 4);
+    uint32_t* uf = malloc(N * 4);
+    uint32_t* sz = malloc(N * 4);
+    if (!id || !uf || !sz) { free(id); free(uf); free(sz); return SCORE_ERR_NOMEM; }
+    for (uint64_t i = 0; i < N; i++) { id[i] = bin[i] ? 1u : 0u; uf[i] = (uint32_t)i; sz[i] = 1; }
+    for (uint32_t z = 0; z < nz; z++)
+        for (uint32_t y = 0; y < ny; y++)
+            for (uint32_t x = 0; x < nx; x++) {
+                const uint64_t c = x + nx * ((uint64_t)y + (uint64_t)ny * z);
+                if (id[c] != 1) continue;  /* only the cells still marked 1 (unlabelled) */
+                uint32_t front = z == 0 ? 0 : id[c - nxy], bottom = y == 0 ? 0 : id[c - nx], left = x == 0 ? 0 : id[c - 1];
+                if (reference_scan) {
+                    int bl = left > 0, bb = bottom > 0, bf = front > 0;
+                    if (!bl && !bb && !bf) id[c] = (uint32_t)c;
+                    else if (bl && !bb && !bf) id[c] = left;
+                    else if (!bl && bb && !bf) id[c] = bottom;
+                    else if (!bl && !bb && bf) id[c] = front;
+                    else if (bl && bb && !bf) id[c] = uf_merge(uf, sz, left, bottom);
+                    else if (bl && !bb && bf) id[c] = uf_merge(uf, sz, left, front);
+                    else if (!bl && bb && bf) id[c] = uf_merge(uf, sz, bottom, front);
+                    else id[c] = uf_merge(uf, sz, bottom, front);
+                } else {
+                    if (c == 0) { id[c] = 0; continue; }
+                    uint32_t lab = (uint32_t)c;
+                    if (left) lab = uf_merge(uf, sz, lab, left);
+                    if (bottom) lab = uf_merge(uf, sz, lab, bottom);
+                    if (front) lab = uf_merge(uf, sz, lab, front);
+                    id[c] = lab;
+                }
+            }
+    /* compactify: new labels in the order of first appearance of each root */
+    uint32_t* newkey = uf;  /* reuse as root -> new label map after resolving every root */
+    uint32_t* root = sz;
+    for (uint64_t i = 0; i < N; i++) root[i] = id[i] > 0 ? uf_root(uf, id[i]) : 0xFFFFFFFFu;
+    for (uint64_t i = 0; i < N; i++) newkey[i] = 0;
+    uint32_t n = 0;
+    for (uint64_t i = 0; i < N; i++) {
+        if (root[i] == 0xFFFFFFFFu) { labels[i] = 0; continue; }
+        if (newkey[root[i]] == 0) newkey[root[i]] = ++n;
+        labels[i] = newkey[root[i]];
+    }
+    free(id); free(uf); free(sz);
+    /* sizes, faces */
+    uint32_t* cnt = calloc(n + 1, 4);
+    uint8_t* face = calloc(n + 1, 1);
+    if (!cnt || !face) { free(cnt); free(face); return SCORE_ERR_NOMEM; }
+    for (uint32_t z = 0; z < nz; z++)
+        for (uint32_t y = 0; y < ny; y++)
+            for (uint32_t x = 0; x < nx; x++) {
+                const uint32_t l = labels[x + nx * ((uint64_t)y + (uint64_t)ny * z)];
+                if (!l) continue;
+                cnt[l]++;
+                face[l] |= (x == 0 ? 1 : 0) | (x == nx - 1 ? 2 : 0) | (y == 0 ? 4 : 0) | (y == ny - 1 ? 8 : 0) |
+                           (z == 0 ? 16 : 0) | (z == nz - 1 ? 32 : 0);
+            }
+    uint32_t big = 0, sp = 0;
+    for (uint32_t l = 1; l <= n; l++) {
+        if (cnt[l] > big) big = cnt[l];
+        if ((face[l] & 3) == 3) sp |= 1;
+        if ((face[l] & 12) == 12) sp |= 2;
+        if ((face[l] & 48) == 48) sp |= 4;
+    }
+    if (sizes) { memcpy(sizes, cnt + 1, n * 4ull); qsort(sizes, n, 4, cmp_u32); }
+    *n_clusters = n; *largest = big; *percolates = sp != 0; *spans = sp;
+    free(cnt); free(face);
+    return SCORE_OK;
+}
+

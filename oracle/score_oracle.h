@@ -84,6 +84,13 @@ void oracle_rediscr_kinetics(const oracle_evo* doms, uint32_t ndom, uint32_t nsl
 void oracle_rediscr_macrotexture(const oracle_evo* doms, uint32_t ndom, uint32_t nslots, uint32_t nclass, double* t_out,
                                  double* vol_out);
 
+/* Percolation of the recrystallized and infected cells (SCORE_PercAnalyzer.cpp, log_PERCOLATION):
+ * binarize (grid value >= ndefg), then clusters (see score_oracle.c) with labels (N, 0 = none), their
+ * count, the largest, the spanning axes (bit 0 x, 1 y, 2 z) and the sizes ascending. */
+void oracle_binarize(const oracle_sim* o, uint8_t* bin);
+int oracle_percolation(const uint8_t* bin, uint32_t nx, uint32_t ny, uint32_t nz, int reference_scan, uint32_t* labels,
+                       uint32_t* n_clusters, uint32_t* largest, int* percolates, uint32_t* spans, uint32_t* sizes);
+
 /* P(rxg,defg) by the reference's formula, for pinning the table against the reference */
 double oracle_mobility_weight(const score_params* p, const double* qr, const double* qd);
 

@@ -73,6 +73,10 @@ class GrainEvoInfo(C.Structure):
     _fields_ = [("t", _d), ("X", _d), ("step", _u32), ("Sv", _u32)]
 
 
+class Percolation(C.Structure):
+    _fields_ = [("n_clusters", _u32), ("largest", _u32), ("PL", _d), ("percolates", _i32), ("spans", _u32)]
+
+
 class Timing(C.Structure):
     _fields_ = [
         ("total_ms", _d), ("grow_ms", _d), ("claim_ms", _d), ("commit_ms", _d), ("host_ms", _d),
@@ -146,6 +150,8 @@ SIGNATURES = {
     "score_batch_rediscr_kinetics": (C.c_int, [_vp, _u32, _vp, _vp, _P(_d)]),
     "score_batch_rediscr_texture": (C.c_int, [_vp, _u32, _vp, _u32, _vp, _vp]),
     "score_batch_final_grain_sizes": (C.c_int, [_vp, _vp]),
+    "score_percolation_analyze": (C.c_int, [_vp, C.c_int, _P(Percolation), _vp, _u32, _vp]),
+    "score_batch_percolation_analyze": (C.c_int, [_vp, _u32, C.c_int, _P(Percolation), _vp, _u32, _vp]),
     "score_mobility_weight": (C.c_int, [_P(Params), _vp, _vp, _P(_d)]),
     "score_mobility_table_noalloc": (C.c_int, [_P(Params), _vp, _u32, _vp, _u32, _vp, _vp, _vp]),
     "score_gen_default": (C.c_int, [_P(GenParams)]),

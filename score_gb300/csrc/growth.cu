@@ -34,6 +34,7 @@
 #include "device_common.cuh"
 #include "growth_kernels.cuh"
 #include "host_model.h"
+#include "percolation.h"
 
 using namespace score;
 
@@ -2053,6 +2054,13 @@ int score_rediscr_kinetics(score_ctx* c, uint32_t nslots, double* t_out, double*
     return s;
 }
 
+int score_percolation_analyze(score_ctx* c, int mode, score_perc_result* out, uint32_t* sizes, uint32_t sizes_cap, uint32_t* labels) {
+    if (!c) return SCORE_ERR_ARG;
+    if (!c->loaded) return c->fail(SCORE_ERR_STATE, "no domain loaded");
+    cudaSetDevice(c->device);
+    return percolation_analyze(c->a.grid, c->nx, c->ny, c->nz, c->ndefg, mode, c->stream, c->sms, out, sizes, sizes_cap, labels, c->err);
+}
+
 int score_get_timing(score_ctx* c, score_timing* out) {
     if (!c || !out) return SCORE_ERR_ARG;
     *out = c->eng->tm;
@@ -2267,6 +2275,13 @@ int score_batch_final_grain_sizes(score_batch* b, uint32_t* rx_cells) {
         off += c->nrxg;
     }
     return SCORE_OK;
+}
+
+int score_batch_percolation_analyze(score_batch* b, uint32_t d, int mode, score_perc_result* out, uint32_t* sizes, uint32_t sizes_cap,
+                            uint32_t* labels) {
+    if (!b || d >= b->dom.size()) return SCORE_ERR_ARG;
+    const int s = score_percolation_analyze(b->dom[d], mode, out, sizes, sizes_cap, labels);
+    return s == SCORE_OK ? s : b->dom_fail(b->dom[d], s);
 }
 
 int score_batch_get_timing(score_batch* b, score_timing* out) {

@@ -18,7 +18,7 @@ from pathlib import Path
 import numpy as np
 
 from . import _abi
-from ._abi import GenParams, GrainEvoInfo, Params, ScoreError, StepStats, Timing, Tune
+from ._abi import GenParams, GrainEvoInfo, Params, Percolation, ScoreError, StepStats, Timing, Tune
 
 
 def _ptr(a: np.ndarray | None):
@@ -282,6 +282,18 @@ def stats_dict(s: StepStats) -> dict:
     return {k: (list(getattr(s, k)) if k in ("next_never", "n_recycled") else getattr(s, k)) for k, _ in StepStats._fields_}
 
 
+def _percolation(d: Domain, call, connected: bool, labels: bool) -> dict:
+    r = Percolation()
+    sizes = np.empty(d.ncells // 2 + 2, dtype=np.uint32)
+    lab = np.empty((d.nz, d.ny, d.nx), dtype=np.uint32) if labels else None
+    call(1 if connected else 0, C.byref(r), _ptr(sizes), sizes.size, _ptr(lab))
+    out = {"n_clusters": r.n_clusters, "largest": r.largest, "PL": r.PL, "percolates": bool(r.percolates), "spans": r.spans,
+           "sizes": sizes[: r.n_clusters].copy()}
+    if labels:
+        out["labels"] = lab
+    return out
+
+
 # ---------------------------------------------------------------- growth machine
 class GrowthMachine:
     """One domain on one GPU (caHdl + its region fronts, SCORE_Kernel.h:1008-1584)."""
@@ -374,6 +386,12 @@ class GrowthMachine:
             self._check(self._lib.score_grainevo(self._ctx, i, C.byref(info), _ptr(cnt), _ptr(area)))
             out.append((info, cnt, area))
         return out
+
+    def percolation(self, connected: bool = False, labels: bool = False) -> dict:
+        """Clusters of the recrystallized and infected cells now (log_PERCOLATION): the reference's
+        clusters, or the true 6-connected ones; count, largest, P_L, percolates, spans, sorted sizes,
+        optionally every cell's label."""
+        return _percolation(self.domain, lambda *a: self._check(self._lib.score_percolation_analyze(self._ctx, *a)), connected, labels)
 
     def rediscr_kinetics(self, nslots: int) -> tuple[np.ndarray, np.ndarray, float]:
         """X(t) of this domain on nslots rediscretized times: (t, rx volume, box volume)."""
@@ -528,6 +546,11 @@ class Batch:
         v = np.empty((nslots, nclass), dtype=np.float64)
         self._check(self._lib.score_batch_rediscr_texture(self._b, nslots, _ptr(cls), nclass, _ptr(t), _ptr(v)))
         return t, v
+
+    def percolation(self, i: int, connected: bool = False, labels: bool = False) -> dict:
+        """Domain i's clusters now (see GrowthMachine.percolation)."""
+        return _percolation(self.domains[i], lambda *a: self._check(self._lib.score_batch_percolation_analyze(self._b, i, *a)), connected,
+                            labels)
 
     def final_grain_sizes(self) -> np.ndarray:
         """Every domain's rx grains' final cell counts, in domain order."""

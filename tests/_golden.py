@@ -104,3 +104,16 @@ def evo_descriptor(d, g) -> dict:
     """An oracle post-processing descriptor of a domain's reference log."""
     return {"ndefg": d.ndefg, "nrxg": d.nrxg, "t": g["snap_t"], "counts": g["snap_counts"], "final": g["final"],
             "tsimend": g["t_end"], "cells": d.ncells, "cls": g["cls"]}
+
+
+def load_percolation():
+    """The reference's percolation analyses: per (domain, X) the .uds, the binarized structure,
+    (n clusters, largest, percolates, checkLabeling failed) and the ascending cluster sizes."""
+    z = np.load(GOLDEN / "percolation.npz")
+    out = []
+    for c in z["cases"]:
+        for k in range(len(z["xs"])):
+            key = f"{c}_{k}"
+            out.append({"name": str(c), "x": str(z["xs"][k]), "uds": str(z[f"{key}_uds"]), "hdr": z[f"{key}_hdr"],
+                        "sizes": z[f"{key}_sizes"], "bin": np.unpackbits(z[f"{key}_bin"])})
+    return out

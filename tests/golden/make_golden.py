@@ -59,6 +59,9 @@ PTAB = (40, 80, 111)  # nrxg, ndefg, seed
 EVO_DOMAINS = [(50, 50, 50, 20, 12, 201), (56, 50, 52, 30, 24, 202), (50, 54, 50, 25, 40, 203)]
 EVO_LOGPOINTS = ["0.0", "0.05", "0.1", "0.2", "0.35", "0.5", "0.65", "0.8", "0.9", "0.95"]
 EVO_AREA, EVO_SLOTS, EVO_CLASSES = 13, 40, 4
+# percolation fixture: cubic growth fixtures stopped at these X, analysed by the reference
+PERC_CASES = ["base", "many_nuclei_small_cache", "texture_bimodal", "rollett_holm"]
+PERC_X = ["0.01", "0.05", "0.15", "0.3", "0.6", "0.99"]
 # benchmark configurations: name -> (edge, grains, nuclei, seed)
 CONFIGS = {"config0": (128, 500, 200, 0), "config1": (512, 20000, 50000, 0)}
 
@@ -197,6 +200,38 @@ def make_evo(wd: Path) -> Path:
     return path
 
 
+def make_perc(wd: Path) -> Path:
+    """The reference's percolation analysis (log_PERCOLATION: binarize, Hoshen-Kopelman, compactify,
+    checkLabeling, percolates, cluster-size distribution) of growth fixtures stopped at several X."""
+    import os
+    out = {}
+    os.environ["SCORE_PERC"] = "1"
+    for name in PERC_CASES:
+        z = np.load(HERE / f"growth_{name}.npz")
+        nx, ny, nz = (int(v) for v in z["dims"])
+        d = sg.Domain(nx, ny, nz, z["grid"].astype(np.uint32).reshape(nz, ny, nx), z["defg_quat"], z["defg_rho0"],
+                      z["rxg_quat"], z["rxg_site"], z["rxg_tincub"])
+        base = str(z["uds"])
+        for k, xm in enumerate(PERC_X):
+            uds = wd / f"perc_{name}_{k}.uds"
+            uds.write_text(base.replace('"XMAX"\t"0.99"', f'"XMAX"\t"{xm}"'))
+            r = oracle.run_ref("loop", uds, d, workdir=wd / f"perc_{name}_{k}")
+            raw = (r["workdir"] / "out.perc").read_bytes()
+            n, big, perc, split = (int(v) for v in np.frombuffer(raw[:16], dtype=np.uint32))
+            key = f"{name}_{k}"
+            out[f"{key}_uds"] = np.array(uds.read_text())
+            out[f"{key}_hdr"] = np.array([n, big, perc, split], dtype=np.uint32)
+            out[f"{key}_sizes"] = np.frombuffer(raw[16:16 + 4 * n], dtype=np.uint32)
+            out[f"{key}_bin"] = np.packbits(np.frombuffer(raw[16 + 4 * n:], dtype=np.uint8))
+    del os.environ["SCORE_PERC"]
+    out["cases"] = np.array(PERC_CASES)
+    out["xs"] = np.array(PERC_X)
+    path = HERE / "percolation.npz"
+    np.savez_compressed(path, **out)
+    print(f"{path.name}: {len(PERC_CASES)} domains x {len(PERC_X)} X, {path.stat().st_size // 1024} KiB")
+    return path
+
+
 def make_ptab(wd: Path) -> Path:
     nrxg, ndefg, seed = PTAB
     d = sg.generate_domain(50, 50, 50, ndefg, nrxg, seed=seed)
@@ -227,6 +262,8 @@ def main() -> None:
             make_ptab(wd)
         if not only or "evo" in only:
             make_evo(wd)
+        if not only or "perc" in only:
+            make_perc(wd)
         for name in CONFIGS:
             if not only or name in only:
                 make_config(name, wd)
