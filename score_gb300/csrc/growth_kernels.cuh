@@ -658,8 +658,6 @@ __global__ void __launch_bounds__(kBlock) k_grow_lists(int base, int ndom) {
         const uint32_t reccap = fr.reccap;
 #pragma unroll
         for (int h = 0; h < WPL; ++h) {
-            // word 32h + j covers slots base + 32 (32h + j) .. + 31; lane j of the loop below
-            // owns bit `lane` of word 32h + j
             uint32_t cf = __popc(fw[h]), ci = __popc(iw[h]);
             uint32_t xf = cf, xi = ci;
 #pragma unroll
@@ -667,15 +665,26 @@ __global__ void __launch_bounds__(kBlock) k_grow_lists(int base, int ndom) {
                 const uint32_t p = __shfl_up_sync(0xFFFFFFFFu, xf, o), q = __shfl_up_sync(0xFFFFFFFFu, xi, o);
                 if (lane >= o) { xf += p; xi += q; }
             }
-            const uint32_t ef = rf + xf - cf, ei = ri + xi - ci;  // exclusive rank of the word's first bit
-            for (int j = 0; j < 32; ++j) {
-                const uint32_t wf = __shfl_sync(0xFFFFFFFFu, fw[h], j), wi = __shfl_sync(0xFFFFFFFFu, iw[h], j);
-                const uint32_t bf = __shfl_sync(0xFFFFFFFFu, ef, j), bi = __shfl_sync(0xFFFFFFFFu, ei, j);
-                const uint32_t slot = tile * S::kTile + 32u * (uint32_t)(32 * h + j) + (uint32_t)lane;
-                if ((wf >> lane) & 1u) fr.full[bf + __popc(wf & lt)] = slot;
-                if ((wi >> lane) & 1u) {
-                    const uint32_t r = bi + __popc(wi & lt);
-                    if (r < reccap) fr.recyc[r] = slot;
+            // lane j owns word 32h + j of the tile: slots tile kTile + 32 (32h + j) + bit
+            const uint32_t wslot = tile * S::kTile + 32u * (uint32_t)(32 * h + lane);
+            // full slots are a few per cent of the slots: each lane writes its word's, in bit order
+            uint32_t r = rf + xf - cf;
+            for (uint32_t m = fw[h]; m; m &= m - 1u) fr.full[r++] = wslot + (uint32_t)(__ffs(m) - 1);
+            // INACTIVE slots only up to the recycle cap (SCORE_Kernel.cpp:4133-4180); the rest are not listed.
+            // Dense words go through the warp in word order so that the stores coalesce.
+            uint32_t q0 = ri + xi - ci;
+            if (__any_sync(0xFFFFFFFFu, q0 < reccap && ci)) {
+                if (__ballot_sync(0xFFFFFFFFu, ci > 8u)) {
+                    for (int j = 0; j < 32; ++j) {
+                        const uint32_t wi = __shfl_sync(0xFFFFFFFFu, iw[h], j), bi = __shfl_sync(0xFFFFFFFFu, q0, j);
+                        if (bi >= reccap || !wi) continue;  // uniform over the warp
+                        if ((wi >> lane) & 1u) {
+                            const uint32_t rr = bi + __popc(wi & lt);
+                            if (rr < reccap) fr.recyc[rr] = tile * S::kTile + 32u * (uint32_t)(32 * h + j) + (uint32_t)lane;
+                        }
+                    }
+                } else {
+                    for (uint32_t m = iw[h]; m && q0 < reccap; m &= m - 1u) fr.recyc[q0++] = wslot + (uint32_t)(__ffs(m) - 1);
                 }
             }
             rf += __shfl_sync(0xFFFFFFFFu, xf, 31);

@@ -12,7 +12,7 @@
 // SCORE_PERC_CONNECTED links all present lower neighbours: the true 6-connected clusters.
 //
 // Kernels: init (parent = self for 1-cells), link (lock-free union: the larger root is attached to
-// the smaller with atomicCAS, path halving in find), flatten, then the compaction of
+// the smaller with atomicCAS, path halving in find), flatten (read-only walks), then the compaction of
 // compactify (:334-390): clusters numbered in the order of their first cell, which is the root (the
 // smallest index of a cluster) order, by a count / scan / assign pass; then per-cluster sizes and face
 // bits for percolates (:500-615) and the size distribution (:617-656, sorted on the host).
@@ -76,9 +76,18 @@ __global__ void k_perc_link(const uint32_t* grid, uint32_t nx, uint32_t ny, uint
     }
 }
 
+// Every cell's root.  The walk only reads: path halving here could overwrite the root another
+// thread just stored for its own cell with an older ancestor, and the labels read parent as the root.
+// Concurrent stores of other cells' roots only shorten the paths walked.
 __global__ void k_perc_flatten(uint32_t* parent, uint64_t N, uint32_t* err) {
-    for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < N; i += (uint64_t)gridDim.x * blockDim.x)
-        if (parent[i] != kNone) parent[i] = find_root(parent, (uint32_t)i, err);
+    for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < N; i += (uint64_t)gridDim.x * blockDim.x) {
+        uint32_t x = parent[i];
+        if (x == kNone) continue;
+        uint32_t k = 0;
+        for (uint32_t p = parent[x]; p != x && k < kFindLimit; p = parent[x], ++k) x = p;
+        if (k == kFindLimit) atomicOr(err, 1u);
+        parent[i] = x;
+    }
 }
 
 // roots per tile of kPercTile cells (a root is a cell that is its own parent)
