@@ -41,6 +41,7 @@ struct DevState {
     uint32_t ntagged;           // new cells whose P waits for the host (tagged)
     uint32_t ndepleted;         // deformed grains whose last cell recrystallized
     uint32_t nnuc;              // nuclei placed on the device before this step's grow
+    uint32_t commit_done;       // commit blocks finished (the last one closes the step)
     unsigned long long sv[2];   // ACTIVE slots updated
     unsigned long long pmax_bits;  // max over new non-negative P (ordered bits)
     double dv[2];               // sum of fill increments

@@ -138,6 +138,10 @@ __global__ void __launch_bounds__(kDueMax) k_place_due(DomainArgs a, const NucDu
     }
 }
 
+__global__ void k_clear_ptab(unsigned long long* ptab, const unsigned long long* idx, uint32_t n) {
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) ptab[idx[i]] = kPtabEmpty;
+}
+
 __global__ void k_fill_ptab(unsigned long long* ptab, const unsigned long long* idx, const double* val, uint32_t n) {
     for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
         ptab[idx[i]] = (unsigned long long)__double_as_longlong(val[i]);
@@ -152,7 +156,27 @@ __global__ void k_labels_front(DomainArgs a, int L, uint32_t n, uint32_t* lab) {
         bool rx;
         if (!FP32) rx = !(((const double*)f.fill)[s] < 0.5);
         else rx = !((((const float*)f.fill)[s] - f.comp[s]) < 0.5f);
-        lab[f.xyz[s]] = rx ? a.ndefg + f.rxg[s] : f.defg[s];
+        int x, y, z;
+        decode(a, f.xyz[s], x, y, z);
+        lab[linear_of(a, x, y, z)] = rx ? a.ndefg + f.rxg[s] : f.defg[s];
+    }
+}
+
+// the grid between the linear order of the C interface and the device's bricks (gindex); the
+// padding words of odd extents hold kPadCell, which no attempt can claim
+constexpr uint32_t kPadCell = 0xFFFFFFFFu;
+__global__ void k_brick(DomainArgs a, const uint32_t* lin, uint32_t* g) {
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < a.ncells; i += gridDim.x * blockDim.x) {
+        int x, y, z;
+        decode(a, i, x, y, z);
+        g[i] = (x < (int)a.nx && y < (int)a.ny && z < (int)a.nz) ? lin[linear_of(a, x, y, z)] : kPadCell;
+    }
+}
+__global__ void k_unbrick(DomainArgs a, const uint32_t* g, uint32_t* lin) {
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < a.ncells; i += gridDim.x * blockDim.x) {
+        int x, y, z;
+        decode(a, i, x, y, z);
+        if (x < (int)a.nx && y < (int)a.ny && z < (int)a.nz) lin[linear_of(a, x, y, z)] = g[i];
     }
 }
 
@@ -377,11 +401,13 @@ struct score_ctx {
 
     uint32_t nx = 0, ny = 0, nz = 0;
     uint64_t N = 0;
+    uint64_t ncells = 0;               // grid words on the device (2x2x2 bricks over the extents rounded up to even)
     uint32_t ndefg = 0, nrxg = 0;
     bool loaded = false, fp32 = false, failed = false;
     int refresh = 0;                   // next step: 1 full refresh from P, 2 from cached mobilities
     std::vector<double> defg_q, rxg_q, rho0, rho, tincub;
-    std::vector<uint32_t> site;
+    std::vector<uint32_t> site;        // nucleus sites, linear index (x + nx (y + ny z))
+    std::vector<uint32_t> gsite;       // the same sites as grid words (brick index)
     std::vector<uint32_t> site_defg;   // deformed grain of each nucleus site in the loaded grid
     std::vector<uint8_t> placed;
     std::vector<uint32_t> nuc_order;   // rxg ids sorted by (tincub, id)
@@ -438,6 +464,10 @@ struct score_ctx {
     uint32_t* d_log_counts = nullptr;  // log_cap x (ndefg + nrxg) cell counts
     uint32_t* d_log_area = nullptr;    // log_cap x 2 nz RX area profile
     uint32_t log_cap = 0;
+    // P-table entries the runs since the last reset wrote (requests, nuclei): a reset clears these
+    // instead of the whole table, unless the table is fresh or was loaded from the caller
+    std::vector<unsigned long long> ptab_touched;
+    bool ptab_dirty_all = true;
 
     ~score_ctx() { release_domain(); release_stream(); }
     void release_domain();
@@ -492,7 +522,7 @@ struct TuneCfg {
     int fill_bpsm = 16;     // k_grow_fill blocks per SM
     int claim_bpsm = 2;     // k_claim blocks per SM (autotuner's choice on the 512^3 workload)
     int commit_bpsm = 8;    // k_resolve / k_commit blocks per SM (same)
-    int spec_pct = 30;      // fill data loaded with the infector byte up to this INACTIVE share [%]
+    int spec_pct = 30;      // every slot's data loaded with its infector byte up to this INACTIVE share [%]
     int timing_every = 8;   // phase events on every k-th step of a run (0 never): each event costs
                             // microseconds of device time, so the steps in between run without
     bool operator==(const TuneCfg& o) const {
@@ -618,12 +648,14 @@ struct Engine {
     bool use_graph = true;
     bool capturing = false;
     bool events = false;               // the sequence being launched records the phase events
-    bool r2 = false;                   // ... and every stepping domain refreshes from cached mobilities
+    int fill_mode = kFillAny;          // ... and the grow mode of every stepping domain (kFillAny: per domain)
     // the step without / with phase events, with the general / the refresh-only grow kernel
-    cudaGraphExec_t gexec[4] = {nullptr, nullptr, nullptr, nullptr};
-    TuneCfg gcfg[4];
-    int gndom[4] = {-1, -1, -1, -1};
-    bool gfp32[4] = {false, false, false, false};
+    // the step graphs: with or without phase events, times the fill mode (0..3 or per domain)
+    static constexpr int kGraphs = 10;
+    cudaGraphExec_t gexec[kGraphs] = {};
+    TuneCfg gcfg[kGraphs];
+    int gndom[kGraphs] = {-1, -1, -1, -1, -1, -1, -1, -1, -1, -1};
+    bool gfp32[kGraphs] = {};
     uint64_t run_steps = 0;            // steps since the run started (phase sampling)
     // 0 start, 1 end of fill, 2 end of lists, 3 end of claim, 4 end of step, 5/6 run span
     cudaEvent_t ev[7] = {nullptr, nullptr, nullptr, nullptr, nullptr, nullptr, nullptr};
@@ -662,7 +694,7 @@ struct Engine {
         return e == cudaSuccess ? SCORE_OK : SCORE_ERR_CUDA;
     }
     void drop_graph() {
-        for (int k = 0; k < 4; ++k) {
+        for (int k = 0; k < kGraphs; ++k) {
             if (gexec[k]) cudaGraphExecDestroy(gexec[k]);
             gexec[k] = nullptr;
             gndom[k] = -1;
@@ -685,7 +717,7 @@ struct Engine {
     }
     int fail(int code, const std::string& m) { err = m; return code; }
     void launch_sequence(int n);
-    cudaError_t enqueue_step(int n, bool timed, bool refresh_only);
+    cudaError_t enqueue_step(int n, bool timed, int mode);
     int step(bool timed);
     void balance_weights();
     int run_until(double x_target, uint32_t max_steps, uint32_t* steps_done);
@@ -829,7 +861,8 @@ int place_nuclei_upto(score_ctx* c, double tnow, uint32_t* nplaced, bool on_devi
             const uint32_t z = s / nxy, y = (s - z * nxy) / nx, x = s - z * nxy - y * nx;
             const bool inside = x > 0 && x < nx - 1 && y > 0 && y < ny - 1 && z > 0 && z < c->nz - 1;
             c->placed[r] = 1;
-            c->h_due[i] = NucDue{s, r, g, inside ? 0u : 1u, weight_of(c, r, g)};
+            c->h_due[i] = NucDue{c->gsite[r], r, g, inside ? 0u : 1u, weight_of(c, r, g)};
+            c->ptab_touched.push_back((unsigned long long)r * c->ndefg + g);
         }
         const cudaError_t e = cudaMemcpyAsync(c->d_due, c->h_due, (size_t)n * sizeof(NucDue), cudaMemcpyHostToDevice, c->stream);
         if (e != cudaSuccess) return c->cuda_fail(e, "upload due nuclei");
@@ -839,12 +872,12 @@ int place_nuclei_upto(score_ctx* c, double tnow, uint32_t* nplaced, bool on_devi
         c->launches++;
         return SCORE_OK;
     }
-    std::vector<uint32_t> sites(n), gval(n);
-    for (uint32_t i = 0; i < n; ++i) sites[i] = c->site[cand[i]];
+    std::vector<uint32_t> sites(n), gsites(n), gval(n);
+    for (uint32_t i = 0; i < n; ++i) { sites[i] = c->site[cand[i]]; gsites[i] = c->gsite[cand[i]]; }
     if (!c->stage((size_t)n * 8)) return c->fail(SCORE_ERR_NOMEM, "staging buffer");
     uint32_t* d_idx = (uint32_t*)c->d_stage;
     uint32_t* d_out = d_idx + n;
-    cudaError_t e = cudaMemcpyAsync(d_idx, sites.data(), (size_t)n * 4, cudaMemcpyHostToDevice, c->stream);
+    cudaError_t e = cudaMemcpyAsync(d_idx, gsites.data(), (size_t)n * 4, cudaMemcpyHostToDevice, c->stream);
     if (e != cudaSuccess) return c->cuda_fail(e, "upload nucleus sites");
     k_gather_u32<<<blocks_for(n, c->sms), kBlock, 0, c->stream>>>(c->a.grid, d_idx, n, d_out);
     c->launches++;
@@ -873,12 +906,13 @@ int place_nuclei_upto(score_ctx* c, double tnow, uint32_t* nplaced, bool on_devi
             return c->fail(SCORE_ERR_BORDER_CAPACITY, "Border list exceeded 2(xy+xz+yz) slots while placing nuclei");
         c->next_never[L]++;
         NucRec q{};
-        q.list = (uint32_t)L; q.slot = slot; q.site = s; q.rxg = r; q.defg = g;
+        q.list = (uint32_t)L; q.slot = slot; q.site = gsites[i]; q.rxg = r; q.defg = g;
         q.P = weight_of(c, r, g);
         if (q.P >= c->ph.Pmax) c->ph.Pmax = q.P;  // reg_myMobilityWeightMax, then the master's max
         recs.push_back(q);
         taken.insert(s);
         pidx.push_back((unsigned long long)r * c->ndefg + g);
+        c->ptab_touched.push_back(pidx.back());
         pval.push_back(q.P);
         c->n_nuclei++;
         if (nplaced) (*nplaced)++;
@@ -978,14 +1012,32 @@ int defragment(score_ctx* c, int L) {
 // (SCORE_Kernel.cpp:6513-6530): rho max, T, G/b, mobilities, dt0.
 int reset_state(score_ctx* c) {
     DomainArgs& a = c->a;
-    const uint64_t N = c->N;
+    const uint64_t W = c->ncells;
     cudaStream_t st = c->stream;
-    cudaError_t e = cudaMemcpyAsync(a.grid, c->d_grid_init, N * 4, cudaMemcpyDeviceToDevice, st);
-    if (e == cudaSuccess) e = cudaMemsetAsync(a.claim, 0xFF, N * 4, st);
-    for (int L = 0; L < 2 && e == cudaSuccess; ++L)
+    cudaError_t e = cudaMemcpyAsync(a.grid, c->d_grid_init, W * 4, cudaMemcpyDeviceToDevice, st);
+    if (e == cudaSuccess) e = cudaMemsetAsync(a.claim, 0xFF, W * 4, st);
+    for (int L = 0; L < 2 && e == cudaSuccess; ++L) {
         e = cudaMemsetAsync(a.f[L].dir, kInactive, std::max<size_t>(c->high_water[L], 1), st);
-    if (e == cudaSuccess && c->user_ptab.empty())
-        e = cudaMemsetAsync(a.ptab, 0xFF, std::max<size_t>((size_t)c->nrxg * c->ndefg, 1) * 8, st);
+    }
+    if (e == cudaSuccess && c->user_ptab.empty()) {
+        // every entry unknown again: the whole table after allocation or a caller's table, else only the
+        // entries the last runs wrote (a 512^3 run writes about 0.03 % of its 8 GB table)
+        const size_t total = std::max<size_t>((size_t)c->nrxg * c->ndefg, 1);
+        const size_t nt = c->ptab_touched.size();
+        if (c->failed) c->ptab_dirty_all = true;  // a step that failed may have tagged entries it never reported
+        if (c->ptab_dirty_all || nt > total / 64 || !c->stage(nt * 8)) {
+            e = cudaMemsetAsync(a.ptab, 0xFF, total * 8, st);
+        } else if (nt) {
+            e = cudaMemcpyAsync(c->d_stage, c->ptab_touched.data(), nt * 8, cudaMemcpyHostToDevice, st);
+            if (e == cudaSuccess) {
+                k_clear_ptab<<<blocks_for(nt, c->sms), kBlock, 0, st>>>(a.ptab, (const unsigned long long*)c->d_stage, (uint32_t)nt);
+                c->launches++;
+                e = cudaGetLastError();
+            }
+        }
+        c->ptab_touched.clear();
+        c->ptab_dirty_all = false;
+    }
     if (e == cudaSuccess) e = cudaMemcpyAsync(a.defg_cnt, c->d_defg_cnt_init, (size_t)c->ndefg * 4, cudaMemcpyDeviceToDevice, st);
     if (e == cudaSuccess) e = cudaMemsetAsync(a.rxg_cnt, 0, std::max<size_t>(c->nrxg, 1) * 4, st);
     if (e == cudaSuccess) e = cudaMemsetAsync(c->d_state, 0, sizeof(DevState), st);
@@ -1108,7 +1160,11 @@ int log_snapshot(score_ctx* c, uint64_t Sv) {
     if (e == cudaSuccess && c->nrxg) e = cudaMemcpyAsync(cnt + c->ndefg, a.rxg_cnt, (size_t)c->nrxg * 4, cudaMemcpyDeviceToDevice, st);
     // labels by the clarify rule into the attempt-mask array (free between steps)
     uint32_t* lab = a.amask;
-    if (e == cudaSuccess) e = cudaMemcpyAsync(lab, a.grid, c->N * 4, cudaMemcpyDeviceToDevice, st);
+    if (e == cudaSuccess) {
+        k_unbrick<<<blocks_for(c->ncells, c->sms, 16), kBlock, 0, st>>>(a, a.grid, lab);
+        c->launches++;
+        e = cudaGetLastError();
+    }
     if (e != cudaSuccess) return c->cuda_fail(e, "grain-evolution log");
     for (int L = 0; L < 2; ++L) {
         const uint32_t n = c->next_never[L];
@@ -1186,6 +1242,8 @@ int post_step(score_ctx* c, uint32_t newnuc, score_step_stats* out) {
         c->ans_idx.clear();
         c->ans_val.clear();
     }
+    for (unsigned long long x : c->ans_idx)
+        if (x != kMissVoid) c->ptab_touched.push_back(x);
     // deformed grains that ran out of cells this step (synchronize_mydefpool_counts)
     if (hs.ndepleted > 0) {
         const uint32_t nd = std::min(hs.ndepleted, c->ndefg);
@@ -1268,12 +1326,18 @@ inline void record(const Engine& E, int k) {
 template <bool FP32, int ITEMS>
 void launch_grow(const Engine& E, int n) {
     const uint32_t g = (uint32_t)(E.sms * E.cfg.fill_bpsm);
-    if (E.r2) {
-        if (n == 1) k_grow_fill<FP32, ITEMS, true, true><<<g, kBlock, 0, E.stream>>>(E.base, n);
-        else k_grow_fill<FP32, ITEMS, false, true><<<g, kBlock, 0, E.stream>>>(E.base, n);
+    if (n == 1) {
+        switch (E.fill_mode) {
+            case 0: k_grow_fill<FP32, ITEMS, true, 0><<<g, kBlock, 0, E.stream>>>(E.base, n); break;
+            case 1: k_grow_fill<FP32, ITEMS, true, 1><<<g, kBlock, 0, E.stream>>>(E.base, n); break;
+            case 2: k_grow_fill<FP32, ITEMS, true, 2><<<g, kBlock, 0, E.stream>>>(E.base, n); break;
+            case 3: k_grow_fill<FP32, ITEMS, true, 3><<<g, kBlock, 0, E.stream>>>(E.base, n); break;
+            default: k_grow_fill<FP32, ITEMS, true, kFillAny><<<g, kBlock, 0, E.stream>>>(E.base, n); break;
+        }
+    } else if (E.fill_mode == 2) {
+        k_grow_fill<FP32, ITEMS, false, 2><<<g, kBlock, 0, E.stream>>>(E.base, n);
     } else {
-        if (n == 1) k_grow_fill<FP32, ITEMS, true, false><<<g, kBlock, 0, E.stream>>>(E.base, n);
-        else k_grow_fill<FP32, ITEMS, false, false><<<g, kBlock, 0, E.stream>>>(E.base, n);
+        k_grow_fill<FP32, ITEMS, false, kFillAny><<<g, kBlock, 0, E.stream>>>(E.base, n);
     }
     record(E, 1);
     k_grow_lists<ITEMS><<<(uint32_t)E.sms * 8, kBlock, 0, E.stream>>>(E.base, n);
@@ -1292,18 +1356,20 @@ void launch_sequence_t(const Engine& E, int n) {
     if (n == 1) k_claim<true><<<S * (uint32_t)E.cfg.claim_bpsm, kBlock, 0, st>>>(d, n);
     else k_claim<false><<<S * (uint32_t)E.cfg.claim_bpsm, kBlock, 0, st>>>(d, n);
     record(E, 3);
+    const uint32_t gt = (uint32_t)(kBlock * E.cfg.items);
     if (n == 1) {
         k_resolve<true><<<S * (uint32_t)E.cfg.commit_bpsm, kBlock, 0, st>>>(d, n);
-        k_commit<FP32, true><<<S * (uint32_t)E.cfg.commit_bpsm, kBlock, 0, st>>>(d, n);
+        k_commit<FP32, true><<<S * (uint32_t)E.cfg.commit_bpsm, kBlock, 0, st>>>(d, n, gt);  // ends the step too
     } else {
         k_resolve<false><<<S * (uint32_t)E.cfg.commit_bpsm, kBlock, 0, st>>>(d, n);
-        k_commit<FP32, false><<<S * (uint32_t)E.cfg.commit_bpsm, kBlock, 0, st>>>(d, n);
+        k_commit<FP32, false><<<S * (uint32_t)E.cfg.commit_bpsm, kBlock, 0, st>>>(d, n, gt);
+        k_step_end<<<(uint32_t)n, kBlock, 0, st>>>(d, n, gt);
     }
-    k_step_end<<<(uint32_t)n, kBlock, 0, st>>>(d, n, (uint32_t)(kBlock * E.cfg.items));
     record(E, 4);
 }
 
-constexpr int kStepKernels = 6;  // fill, lists, claim, resolve, commit, step end
+// kernels per step: fill, lists, claim, resolve, commit, and for batches a separate step end
+inline int step_kernels(int n) { return n == 1 ? 5 : 6; }
 
 }  // namespace
 
@@ -1313,7 +1379,7 @@ void Engine::launch_sequence(int n) {
 }
 
 // the argument copy and the kernels of one step, as a graph replay or direct launches
-cudaError_t Engine::enqueue_step(int n, bool timed, bool refresh_only) {
+cudaError_t Engine::enqueue_step(int n, bool timed, int mode) {
     // the argument blocks only change when dt, the physics or a domain's state changes
     cudaError_t e = cudaSuccess;
     if (args_dirty || memcmp(h_args, h_args_dev.data(), (size_t)n * sizeof(DomainArgs)) != 0) {
@@ -1323,13 +1389,13 @@ cudaError_t Engine::enqueue_step(int n, bool timed, bool refresh_only) {
     }
     if (e != cudaSuccess) return e;
     events = timed;
-    r2 = refresh_only;
+    fill_mode = mode;
     if (!use_graph) {
         launch_sequence(n);
-        launches += kStepKernels;
+        launches += step_kernels(n);
         return cudaGetLastError();
     }
-    const int k = (timed ? 1 : 0) + (refresh_only ? 2 : 0);
+    const int k = (timed ? 1 : 0) + 2 * (mode == kFillAny ? 4 : mode);
     if (!gexec[k] || gndom[k] != n || !(gcfg[k] == cfg) || gfp32[k] != fp32) {
         if (gexec[k]) cudaGraphExecDestroy(gexec[k]);
         gexec[k] = nullptr;
@@ -1346,7 +1412,7 @@ cudaError_t Engine::enqueue_step(int n, bool timed, bool refresh_only) {
         if (e != cudaSuccess) { gexec[k] = nullptr; return e; }
         gndom[k] = n; gcfg[k] = cfg; gfp32[k] = fp32;
     }
-    launches += kStepKernels;
+    launches += step_kernels(n);
     return cudaGraphLaunch(gexec[k], stream);
 }
 
@@ -1446,9 +1512,16 @@ int Engine::step(bool timed) {
     if (nrun == 0) return SCORE_OK;
     const auto pre_t1 = std::chrono::steady_clock::now();
     tm.pre_ms += std::chrono::duration<double, std::milli>(pre_t1 - host_t0).count();
-    bool r2all = true;  // every stepping domain refreshes from its cached mobilities
-    for (int i = 0; i < n; ++i) if (dom[i]->running && h_args[i].refresh != 2) r2all = false;
-    cudaError_t e = enqueue_step(n, timed, r2all);
+    // the grow mode every stepping domain shares (a kernel specialised to it), or per domain
+    int mode = -2;
+    for (int i = 0; i < n; ++i) {
+        if (!dom[i]->running) continue;
+        const DomainArgs& a = h_args[i];
+        const int m = a.refresh == 2 ? 2 : a.refresh == 1 ? 1 : (a.spec && !a.dt_changed) ? 3 : 0;
+        mode = (mode == -2 || mode == m) ? m : kFillAny;
+    }
+    if (n > 1 && mode != 2) mode = kFillAny;  // batches: the refresh-only kernel, or the per-domain one
+    cudaError_t e = enqueue_step(n, timed, mode);
     ++run_steps;
     // while the GPU steps: each domain's outcome-independent physics for the next step
     std::vector<int> status(n, SCORE_OK);
@@ -1562,6 +1635,7 @@ int check_params(const score_params* p, int device) {
     if (p->nx < 3 || p->ny < 3 || p->nz < 3) return SCORE_ERR_ARG;
     const uint64_t N = (uint64_t)p->nx * p->ny * p->nz;
     if (N >= 0x7FFFFFFFull) return SCORE_ERR_ARG;  // slot counters and ranks are 32-bit with headroom
+    if (8ull * ((p->nx + 1) / 2) * ((p->ny + 1) / 2) * ((p->nz + 1) / 2) >= 0x7FFFFFFFull) return SCORE_ERR_ARG;  // grid words
     if (p->n_schedule < 1) return SCORE_ERR_ARG;
     int ndev = 0;
     if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) { cudaGetLastError(); return SCORE_ERR_NOT_BUILT; }
@@ -1575,6 +1649,7 @@ int make_ctx(const score_params* p, Engine* eng, bool own, score_ctx** out) {
     c->prm = *p;
     c->device = eng->device;
     c->nx = p->nx; c->ny = p->ny; c->nz = p->nz; c->N = (uint64_t)p->nx * p->ny * p->nz;
+    c->ncells = 8ull * ((p->nx + 1) / 2) * ((p->ny + 1) / 2) * ((p->nz + 1) / 2);
     c->fp32 = p->precision == SCORE_PRECISION_FP32_KAHAN;
     c->eng = eng;
     c->own_eng = own;
@@ -1846,6 +1921,14 @@ int score_load_domain(score_ctx* c, const uint32_t* grid, const double* defg_qua
     c->rxg_q.assign(rxg_quat, rxg_quat + 4 * (size_t)nrxg);
     c->rho0.assign(defg_rho0, defg_rho0 + ndefg);
     c->site.assign(rxg_site, rxg_site + nrxg);
+    {
+        const uint32_t gbx = (c->nx + 1) / 2, gby = (c->ny + 1) / 2, nxy = c->nx * c->ny;
+        c->gsite.resize(nrxg);
+        for (uint32_t r = 0; r < nrxg; ++r) {
+            const uint32_t s = rxg_site[r], z = s / nxy, y = (s - z * nxy) / c->nx, x = s - z * nxy - y * c->nx;
+            c->gsite[r] = gindex(gbx, gby, x, y, z);
+        }
+    }
     c->site_defg.resize(nrxg);
     for (uint32_t r = 0; r < nrxg; ++r) c->site_defg[r] = grid[rxg_site[r]];
     c->tincub.assign(nrxg, 0.0);
@@ -1858,17 +1941,17 @@ int score_load_domain(score_ctx* c, const uint32_t* grid, const double* defg_qua
     std::stable_sort(c->nuc_order.begin(), c->nuc_order.end(), [&](uint32_t x, uint32_t y) { return c->tincub[x] < c->tincub[y]; });
     c->user_ptab.clear();
     if (ptable) c->user_ptab.assign(ptable, ptable + (size_t)nrxg * ndefg);
+    if (ptable || !reuse) c->ptab_dirty_all = true;  // a later reset without a caller's table clears it all
 
     const score_params& p = c->prm;
     DomainArgs& a = c->a;
     const size_t ptab_words = (size_t)nrxg * ndefg;
     cudaError_t e = cudaSuccess;
     if (!reuse) {
-        a.nx = c->nx; a.ny = c->ny; a.nz = c->nz; a.nxy = c->nx * c->ny;
-        a.dnx = make_fastdiv(c->nx); a.dnxy = make_fastdiv(c->nx * c->ny);
-        a.ncells = (uint32_t)N;
-        for (int d = 0; d < 26; ++d)
-            a.noff[d] = kStencilDx[d] + (int32_t)c->nx * kStencilDy[d] + (int32_t)(c->nx * c->ny) * kStencilDz[d];
+        a.nx = c->nx; a.ny = c->ny; a.nz = c->nz;
+        a.gbx = (c->nx + 1) / 2; a.gby = (c->ny + 1) / 2; a.gbxy = a.gbx * a.gby;
+        a.dgbx = make_fastdiv(a.gbx); a.dgbxy = make_fastdiv(a.gbxy);
+        a.ncells = (uint32_t)c->ncells;
         a.ndefg = ndefg; a.nrxg = nrxg;
         a.border_ref_cap = 2 * ((c->nx * c->ny) + (c->nx * c->nz) + (c->ny * c->nz));
         a.border_policy = p.border_policy; a.boundary = p.boundary; a.mobility_model = p.mobility_model;
@@ -1905,9 +1988,9 @@ int score_load_domain(score_ctx* c, const uint32_t* grid, const double* defg_qua
         }
         c->csct_words = 2 * ((N / kBlock + 2) / kSuper + 2);
         a.misscap = (uint32_t)std::min<uint64_t>(N, 1ull << 25);
-        if (e == cudaSuccess) e = dalloc(&a.grid, N);
-        if (e == cudaSuccess) e = dalloc(&c->d_grid_init, N);
-        if (e == cudaSuccess) e = dalloc(&a.claim, N);
+        if (e == cudaSuccess) e = dalloc(&a.grid, c->ncells);
+        if (e == cudaSuccess) e = dalloc(&c->d_grid_init, c->ncells);
+        if (e == cudaSuccess) e = dalloc(&a.claim, c->ncells);
         if (e == cudaSuccess) e = dalloc(&a.amask, N);
         if (e == cudaSuccess) e = dalloc(&a.tobm, N);
         if (e == cudaSuccess) e = dalloc(&a.fcell, N);
@@ -1938,15 +2021,17 @@ int score_load_domain(score_ctx* c, const uint32_t* grid, const double* defg_qua
         c->high_water[0] = std::max(c->high_water[0], c->next_never[0]);
         c->high_water[1] = std::max(c->high_water[1], c->next_never[1]);
     }
-    e = cudaMemcpyAsync(c->d_grid_init, grid, N * 4, cudaMemcpyHostToDevice, c->stream);
+    // the linear grid goes through the claim array (reset before the first step) into bricks
+    e = cudaMemcpyAsync(a.claim, grid, N * 4, cudaMemcpyHostToDevice, c->stream);
     if (e == cudaSuccess && ptable) e = cudaMemcpyAsync(a.ptab, ptable, ptab_words * 8, cudaMemcpyHostToDevice, c->stream);
     if (e == cudaSuccess) e = cudaMemsetAsync(c->d_defg_cnt_init, 0, (size_t)ndefg * 4, c->stream);
     if (e == cudaSuccess) e = cudaMemsetAsync(c->d_state, 0, sizeof(DevState), c->stream);
     if (e != cudaSuccess) return c->cuda_fail(e, "load domain");
     // per-grain cell counts (solve_REPLACE_CA_STRUCTURE, SCORE_Kernel.cpp:6394-6400)
-    k_count_defg<<<blocks_for(N, c->sms, 16), kBlock, 0, c->stream>>>(c->d_grid_init, N, ndefg, c->d_defg_cnt_init,
+    k_count_defg<<<blocks_for(N, c->sms, 16), kBlock, 0, c->stream>>>(a.claim, N, ndefg, c->d_defg_cnt_init,
                                                                       (uint32_t*)((char*)c->d_state + offsetof(DevState, err)));
-    c->launches++;
+    k_brick<<<blocks_for(c->ncells, c->sms, 16), kBlock, 0, c->stream>>>(a, a.claim, c->d_grid_init);
+    c->launches += 2;
     c->defg_cnt_init_host.assign(ndefg, 0);
     e = cudaMemcpyAsync(c->defg_cnt_init_host.data(), c->d_defg_cnt_init, (size_t)ndefg * 4, cudaMemcpyDeviceToHost, c->stream);
     if (e == cudaSuccess) e = cudaMemcpyAsync(c->h_state, c->d_state, sizeof(DevState), cudaMemcpyDeviceToHost, c->stream);
@@ -2011,7 +2096,9 @@ int score_export_labels(score_ctx* c, uint32_t* labels) {
     if (!c->loaded) return c->fail(SCORE_ERR_STATE, "no domain loaded");
     cudaSetDevice(c->device);
     uint32_t* d_lab = c->a.amask;  // N words, free between steps
-    cudaError_t e = cudaMemcpyAsync(d_lab, c->a.grid, c->N * 4, cudaMemcpyDeviceToDevice, c->stream);
+    k_unbrick<<<blocks_for(c->ncells, c->sms, 16), kBlock, 0, c->stream>>>(c->a, c->a.grid, d_lab);
+    c->launches++;
+    cudaError_t e = cudaGetLastError();
     for (int L = 0; L < 2 && e == cudaSuccess; ++L) {
         const uint32_t n = c->next_never[L];
         if (n == 0) continue;
@@ -2058,7 +2145,12 @@ int score_percolation_analyze(score_ctx* c, int mode, score_perc_result* out, ui
     if (!c) return SCORE_ERR_ARG;
     if (!c->loaded) return c->fail(SCORE_ERR_STATE, "no domain loaded");
     cudaSetDevice(c->device);
-    return percolation_analyze(c->a.grid, c->nx, c->ny, c->nz, c->ndefg, mode, c->stream, c->sms, out, sizes, sizes_cap, labels, c->err);
+    // the analysis reads the grid in linear order: a copy in the attempt-mask array (free between steps)
+    k_unbrick<<<blocks_for(c->ncells, c->sms, 16), kBlock, 0, c->stream>>>(c->a, c->a.grid, c->a.amask);
+    c->launches++;
+    const cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) return c->cuda_fail(e, "percolation grid");
+    return percolation_analyze(c->a.amask, c->nx, c->ny, c->nz, c->ndefg, mode, c->stream, c->sms, out, sizes, sizes_cap, labels, c->err);
 }
 
 int score_get_timing(score_ctx* c, score_timing* out) {

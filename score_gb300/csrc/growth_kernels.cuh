@@ -85,11 +85,11 @@ struct HostBox;
 struct DomainArgs {
     DFront f[2];
     DevState* st;
-    uint32_t* grid;
-    uint32_t* claim;
+    uint32_t* grid;             // grain id per cell, in 2x2x2 bricks (gindex)
+    uint32_t* claim;            // lowest attempt ordinal per cell this step, same layout
     uint32_t* amask;            // per full cell: attempts made (bit d), then attempts won
     uint32_t* tobm;             // per full cell: won attempts that go to the Border list
-    uint32_t* fcell;            // per full cell: its cell index (written by k_claim)
+    uint32_t* fcell;            // per full cell: its cell (brick index, written by k_claim)
     uint32_t* ctcnt;            // per commit tile: (Inside, Border) win counts
     uint32_t* csct;             // per supertile of kSuper commit tiles: the same counts (zero between steps)
     unsigned long long* ptab;   // nrxg x ndefg mobility weights as bits (kPtabEmpty = unknown)
@@ -99,10 +99,10 @@ struct DomainArgs {
     uint32_t* depleted;
     unsigned long long* miss;   // table indices the host must fill
     uint32_t misscap;
-    uint32_t nx, ny, nz, nxy;
-    uint32_t ncells;
-    int32_t noff[26];           // linear offset of neighbour d of an interior cell
-    FastDiv dnx, dnxy;
+    uint32_t nx, ny, nz;
+    uint32_t gbx, gby, gbxy;    // bricks along x, along y, per brick layer
+    uint32_t ncells;            // grid words: 8 per brick, the domain padded to even extents
+    FastDiv dgbx, dgbxy;
     uint32_t ndefg, nrxg;
     uint32_t border_ref_cap;
     int32_t border_policy, boundary, mobility_model;
@@ -116,16 +116,36 @@ struct DomainArgs {
     HostBox* box;               // device view of the domain's mailbox
     double mLAGB, mHAGB, mGS, mRH, dt, cinv;
     float dtc32;
-    int32_t spec;               // few INACTIVE slots: k_grow_fill loads every slot's fill data with its
-                                // infector byte instead of after it (no effect on results)
+    int32_t spec;               // few INACTIVE slots last step: k_grow_fill loads every slot's data with its
+                                // infector byte instead of only the ACTIVE slots' (no effect on results)
     double pc_fac;              // 1/sqrt(2) as the host computes it (the disorientation of d_grimmer)
 };
 
+// Cells on the device are named by their grid word: the grid is stored in bricks of 2x2x2 cells
+// (8 consecutive words, x fastest inside the brick), bricks in x, then y, then z order, so that
+// the 3x3x3 neighbourhood of any cell lies in 8 bricks, one 32-byte sector each.  Front slots,
+// full-cell positions and nucleus sites hold this brick index; the linear index x + nx (y + ny z)
+// of the C interface is converted at the boundary (load, labels).
+__host__ __device__ __forceinline__ uint32_t gindex(uint32_t gbx, uint32_t gby, uint32_t x, uint32_t y, uint32_t z) {
+    return ((((z >> 1) * gby + (y >> 1)) * gbx + (x >> 1)) << 3) | ((z & 1u) << 2) | ((y & 1u) << 1) | (x & 1u);
+}
+__device__ __forceinline__ uint32_t gindex(const DomainArgs& a, uint32_t x, uint32_t y, uint32_t z) {
+    return gindex(a.gbx, a.gby, x, y, z);
+}
+
 __device__ __forceinline__ void decode(const DomainArgs& a, uint32_t cell, int& x, int& y, int& z) {
-    const uint32_t zz = fdiv(cell, a.dnxy);
-    const uint32_t r = cell - zz * a.nxy;
-    const uint32_t yy = fdiv(r, a.dnx);
-    x = (int)(r - yy * a.nx); y = (int)yy; z = (int)zz;
+    const uint32_t b = cell >> 3;
+    const uint32_t bz = fdiv(b, a.dgbxy);
+    const uint32_t r = b - bz * a.gbxy;
+    const uint32_t by = fdiv(r, a.dgbx);
+    x = (int)(2u * (r - by * a.gbx) + (cell & 1u));
+    y = (int)(2u * by + ((cell >> 1) & 1u));
+    z = (int)(2u * bz + ((cell >> 2) & 1u));
+}
+
+// linear index of the C interface
+__device__ __forceinline__ uint32_t linear_of(const DomainArgs& a, int x, int y, int z) {
+    return (uint32_t)x + a.nx * ((uint32_t)y + a.ny * (uint32_t)z);
 }
 
 // Target of attempt d from (x,y,z) of a cell of list L.  Inside cells are strictly
@@ -149,7 +169,7 @@ __device__ __forceinline__ bool target_of(const DomainArgs& a, int L, int x, int
         return false;
     }
     interior = tx > 0 && tx < (int)a.nx - 1 && ty > 0 && ty < (int)a.ny - 1 && tz > 0 && tz < (int)a.nz - 1;
-    t = (uint32_t)tx + a.nx * ((uint32_t)ty + a.ny * (uint32_t)tz);
+    t = gindex(a, (uint32_t)tx, (uint32_t)ty, (uint32_t)tz);
     return true;
 }
 
@@ -300,13 +320,12 @@ __device__ __forceinline__ void tile_prefix(const uint32_t* cnt, const uint32_t*
 //   k_grow_lists  one warp per tile: the tile's exclusive prefix from the supertile
 //                 and tile counts, then the FullRX list and the capped recycle list in
 //                 slot order; the warp of a list's last tile stores the list totals.
-// REFRESH 1: recompute vel of every active slot from the P table and the current
-// physics (after T changed the mobilities); REFRESH 2: from the cell's cached mobility
-// (only rho or the drag changed the driving force), no table gather; REFRESH 3: as 0 with
-// dt unchanged, the slot's cached increment and fill loaded together with its infector
-// byte, for every slot below the high-water mark (one memory round trip instead of two,
-// at the price of reading the fill data of INACTIVE slots too); REFRESH 4: REFRESH 2 with
-// the same early loads (cached mobility, grain and fill).
+// REFRESH 1: recompute vel of every active slot from the P table and the current physics
+// (after T changed the mobilities); REFRESH 2: from the cell's cached mobility (only rho or the
+// drag changed the driving force), no table gather; REFRESH 0: the cached increment (or vel when
+// dt changed or the increment is stale); REFRESH 3: as 0 with dt unchanged when the last step's
+// list had few holes: every slot's data is loaded with its infector byte, whether ACTIVE or not
+// (one memory round trip instead of two).
 // A cell created last step whose weight the host computed: P = answer `tag`; the table
 // entry (tagged until now) gets the value for later lookups.
 __device__ __forceinline__ double answered_velocity(const DomainArgs& a, const DFront& fr, uint32_t slot, uint8_t dir,
@@ -319,226 +338,20 @@ __device__ __forceinline__ double answered_velocity(const DomainArgs& a, const D
     return velocity_from_mobility(a, mo, fr.defg[slot], dir & kCodeMask);
 }
 
-// returns the thread's ACTIVE slots (the Sv share)
-template <bool FP32, int REFRESH, int ITEMS>
-__device__ __forceinline__ uint32_t grow_tile(const DomainArgs& a, int L, uint32_t tile, uint32_t n) {
+// The full and INACTIVE masks of a warp's ITEMS x 32 slots of grow tile `tile` (slot of item k and
+// lane: base + 32 k), the warp's two counts and its share of the supertile's counts.
+template <int ITEMS>
+__device__ __forceinline__ void tile_masks(const DFront& fr, uint32_t tile, uint32_t base, uint32_t n, uint32_t act, uint32_t fullbits) {
     using S = GrowShape<ITEMS>;
-    const DFront& fr = a.f[L];
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    // each warp owns 32 * ITEMS consecutive slots of the tile: no block barrier, warps run apart
-    const uint32_t base = tile * S::kTile + (uint32_t)warp * 32u * ITEMS + (uint32_t)lane;
-    uint32_t sv = 0;
-    uint8_t d[ITEMS];
-#pragma unroll
-    for (int k = 0; k < ITEMS; ++k) {
-        const uint32_t slot = base + (uint32_t)(k * 32);
-        d[k] = slot < n ? fr.dir[slot] : kInactive;
-    }
-    bool full[ITEMS];
-    if (!FP32) {
-        double w[ITEMS], fill[ITEMS];  // w: cached inc, or vel when the increment is stale
-        if (REFRESH == 3) {
-#pragma unroll
-            for (int k = 0; k < ITEMS; ++k) {
-                const uint32_t slot = base + (uint32_t)(k * 32);
-                w[k] = -1.0; fill[k] = 0.0;
-                if (slot < n) {
-                    w[k] = fr.inc[slot];
-                    fill[k] = ((const double*)fr.fill)[slot];
-                }
-            }
-#pragma unroll
-            for (int k = 0; k < ITEMS; ++k) {
-                const uint32_t slot = base + (uint32_t)(k * 32);
-                if (d[k] != kInactive && (d[k] & kStale)) {
-                    if (d[k] & kPend) {
-                        w[k] = answered_velocity(a, fr, slot, d[k], ((const unsigned long long*)fr.vel)[slot]);
-                        ((double*)fr.vel)[slot] = w[k];
-                    } else {
-                        w[k] = ((const double*)fr.vel)[slot];
-                    }
-                }
-            }
-        } else if (REFRESH == 4) {
-            // in two halves of the items: the early loads of all of them do not fit the registers
-            constexpr int H = ITEMS / 2;
-#pragma unroll
-            for (int h = 0; h < 2; ++h) {
-                double mo[H];
-                uint32_t g[H];
-#pragma unroll
-                for (int j = 0; j < H; ++j) {
-                    const int k = h * H + j;
-                    const uint32_t slot = base + (uint32_t)(k * 32);
-                    w[k] = -1.0; fill[k] = 0.0; mo[j] = 0.0; g[j] = 0;
-                    if (slot < n) {
-                        mo[j] = fr.mob[slot];
-                        g[j] = fr.defg[slot];
-                        fill[k] = ((const double*)fr.fill)[slot];
-                    }
-                }
-#pragma unroll
-                for (int j = 0; j < H; ++j) {
-                    const int k = h * H + j;
-                    const uint32_t slot = base + (uint32_t)(k * 32);
-                    if (d[k] != kInactive) {
-                        if (d[k] & kPend) w[k] = answered_velocity(a, fr, slot, d[k], ((const unsigned long long*)fr.vel)[slot]);
-                        else w[k] = velocity_from_mobility(a, mo[j], g[j], d[k] & kCodeMask);
-                        ((double*)fr.vel)[slot] = w[k];
-                    }
-                }
-            }
-        } else {
-#pragma unroll
-        for (int k = 0; k < ITEMS; ++k) {
-            const uint32_t slot = base + (uint32_t)(k * 32);
-            w[k] = -1.0; fill[k] = 0.0;
-            if (d[k] != kInactive) {
-                if (d[k] & kPend) {
-                    w[k] = answered_velocity(a, fr, slot, d[k], ((const unsigned long long*)fr.vel)[slot]);
-                    ((double*)fr.vel)[slot] = w[k];
-                } else if (REFRESH == 1) {
-                    const uint32_t g = fr.defg[slot];
-                    const double P = __longlong_as_double((long long)a.ptab[(unsigned long long)fr.rxg[slot] * a.ndefg + g]);
-                    const double mo = mobility(a, P);
-                    fr.mob[slot] = mo;
-                    w[k] = velocity_from_mobility(a, mo, g, d[k] & kCodeMask);
-                    ((double*)fr.vel)[slot] = w[k];
-                } else if (REFRESH == 2) {
-                    w[k] = velocity_from_mobility(a, fr.mob[slot], fr.defg[slot], d[k] & kCodeMask);
-                    ((double*)fr.vel)[slot] = w[k];
-                } else if (a.dt_changed || (d[k] & kStale)) {
-                    w[k] = ((const double*)fr.vel)[slot];
-                } else {
-                    w[k] = fr.inc[slot];
-                }
-                fill[k] = ((const double*)fr.fill)[slot];
-            }
-        }
-        }
-#pragma unroll
-        for (int k = 0; k < ITEMS; ++k) {
-            full[k] = false;
-            if (d[k] != kInactive) {
-                ++sv;
-                const uint32_t slot = base + (uint32_t)(k * 32);
-                double inc = w[k];
-                if (REFRESH == 1 || REFRESH == 2 || REFRESH == 4 || (REFRESH == 0 && a.dt_changed) || (d[k] & kStale)) {
-                    if (__double_as_longlong(w[k]) >= 0) inc = __dmul_rn(__dmul_rn(w[k], a.dt), a.cinv);
-                    fr.inc[slot] = inc;
-                    if (d[k] & kStale) fr.dir[slot] = d[k] & kCodeMask;
-                }
-                if (__double_as_longlong(inc) >= 0) {  // sign bit clear: driving force present
-                    const double f = __dadd_rn(fill[k], inc);
-                    ((double*)fr.fill)[slot] = f;
-                    full[k] = __double_as_longlong(f) >= 0x3FF0000000000000ll;  // f >= 1.0, f never negative
-                }
-            }
-        }
-    } else {
-        float vel[ITEMS], fill[ITEMS], comp[ITEMS];
-        if (REFRESH == 3) {
-#pragma unroll
-            for (int k = 0; k < ITEMS; ++k) {
-                const uint32_t slot = base + (uint32_t)(k * 32);
-                vel[k] = -1.0f; fill[k] = 0.0f; comp[k] = 0.0f;
-                if (slot < n) {
-                    vel[k] = ((const float*)fr.vel)[slot];
-                    fill[k] = ((const float*)fr.fill)[slot];
-                    comp[k] = fr.comp[slot];
-                }
-            }
-#pragma unroll
-            for (int k = 0; k < ITEMS; ++k) {
-                const uint32_t slot = base + (uint32_t)(k * 32);
-                if (d[k] != kInactive && (d[k] & kPend)) {
-                    vel[k] = (float)answered_velocity(a, fr, slot, d[k], ((const uint32_t*)fr.vel)[slot]);
-                    ((float*)fr.vel)[slot] = vel[k];
-                }
-            }
-        } else if (REFRESH == 4) {
-            constexpr int H = ITEMS / 2;
-#pragma unroll
-            for (int h = 0; h < 2; ++h) {
-                double mo[H];
-                uint32_t g[H];
-#pragma unroll
-                for (int j = 0; j < H; ++j) {
-                    const int k = h * H + j;
-                    const uint32_t slot = base + (uint32_t)(k * 32);
-                    vel[k] = -1.0f; fill[k] = 0.0f; comp[k] = 0.0f; mo[j] = 0.0; g[j] = 0;
-                    if (slot < n) {
-                        mo[j] = fr.mob[slot];
-                        g[j] = fr.defg[slot];
-                        fill[k] = ((const float*)fr.fill)[slot];
-                        comp[k] = fr.comp[slot];
-                    }
-                }
-#pragma unroll
-                for (int j = 0; j < H; ++j) {
-                    const int k = h * H + j;
-                    const uint32_t slot = base + (uint32_t)(k * 32);
-                    if (d[k] != kInactive) {
-                        if (d[k] & kPend) vel[k] = (float)answered_velocity(a, fr, slot, d[k], ((const uint32_t*)fr.vel)[slot]);
-                        else vel[k] = (float)velocity_from_mobility(a, mo[j], g[j], d[k] & kCodeMask);
-                        ((float*)fr.vel)[slot] = vel[k];
-                    }
-                }
-            }
-        } else {
-#pragma unroll
-        for (int k = 0; k < ITEMS; ++k) {
-            const uint32_t slot = base + (uint32_t)(k * 32);
-            vel[k] = -1.0f; fill[k] = 0.0f; comp[k] = 0.0f;
-            if (d[k] != kInactive) {
-                if (d[k] & kPend) {
-                    vel[k] = (float)answered_velocity(a, fr, slot, d[k], ((const uint32_t*)fr.vel)[slot]);
-                    ((float*)fr.vel)[slot] = vel[k];
-                } else if (REFRESH == 1) {
-                    const uint32_t g = fr.defg[slot];
-                    const double P = __longlong_as_double((long long)a.ptab[(unsigned long long)fr.rxg[slot] * a.ndefg + g]);
-                    const double mo = mobility(a, P);
-                    fr.mob[slot] = mo;
-                    vel[k] = (float)velocity_from_mobility(a, mo, g, d[k] & kCodeMask);
-                    ((float*)fr.vel)[slot] = vel[k];
-                } else if (REFRESH == 2) {
-                    vel[k] = (float)velocity_from_mobility(a, fr.mob[slot], fr.defg[slot], d[k] & kCodeMask);
-                    ((float*)fr.vel)[slot] = vel[k];
-                } else {
-                    vel[k] = ((const float*)fr.vel)[slot];
-                }
-                fill[k] = ((const float*)fr.fill)[slot];
-                comp[k] = fr.comp[slot];
-            }
-        }
-        }
-#pragma unroll
-        for (int k = 0; k < ITEMS; ++k) {
-            full[k] = false;
-            if (d[k] != kInactive) {
-                ++sv;
-                const uint32_t slot = base + (uint32_t)(k * 32);
-                if (d[k] & kStale) fr.dir[slot] = d[k] & kCodeMask;
-                if (vel[k] >= 0.0f) {
-                    // Kahan-compensated accumulation of the fill
-                    const float inc = vel[k] * a.dtc32;
-                    const float y = inc - comp[k];
-                    const float t = fill[k] + y;
-                    const float c = (t - fill[k]) - y;
-                    ((float*)fr.fill)[slot] = t;
-                    fr.comp[slot] = c;
-                    full[k] = (t - c) >= 1.0f;
-                }
-            }
-        }
-    }
+    const uint32_t word0 = tile * S::kWords + (uint32_t)(warp * ITEMS);  // item k's mask word
     uint32_t cf = 0, ci = 0;
 #pragma unroll
     for (int k = 0; k < ITEMS; ++k) {
-        const uint32_t fm = __ballot_sync(0xFFFFFFFFu, full[k]);
-        const uint32_t im = __ballot_sync(0xFFFFFFFFu, d[k] == kInactive && base + (uint32_t)(k * 32) < n);
+        const uint32_t fm = __ballot_sync(0xFFFFFFFFu, (fullbits >> k) & 1u);
+        const uint32_t im = __ballot_sync(0xFFFFFFFFu, !((act >> k) & 1u) && base + (uint32_t)(k * 32) < n);
         if (lane == 0) {
-            const uint32_t word = tile * S::kWords + (uint32_t)(warp * ITEMS + k);  // slots 32 word .. 32 word + 31
+            const uint32_t word = word0 + (uint32_t)k;  // slots 32 word .. 32 word + 31
             fr.fmask[word] = fm;
             fr.imask[word] = im;
         }
@@ -552,6 +365,254 @@ __device__ __forceinline__ uint32_t grow_tile(const DomainArgs& a, int L, uint32
         if (cf) atomicAdd(&fr.scnt[2 * (tile / kSuper)], cf);
         if (ci) atomicAdd(&fr.scnt[2 * (tile / kSuper) + 1], ci);
     }
+}
+
+// returns the thread's ACTIVE slots (the Sv share)
+template <bool FP32, int REFRESH, int ITEMS>
+__device__ __forceinline__ uint32_t grow_tile(const DomainArgs& a, int L, uint32_t tile, uint32_t n) {
+    using S = GrowShape<ITEMS>;
+    const DFront& fr = a.f[L];
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    // each warp owns 32 * ITEMS consecutive slots of the tile: no block barrier, warps run apart
+    const uint32_t base = tile * S::kTile + (uint32_t)warp * 32u * ITEMS + (uint32_t)lane;
+    uint32_t sv = 0, act = 0;  // act bit k: item k's slot is ACTIVE
+    uint8_t d[ITEMS];
+#pragma unroll
+    for (int k = 0; k < ITEMS; ++k) {
+        const uint32_t slot = base + (uint32_t)(k * 32);
+        d[k] = slot < n ? fr.dir[slot] : kInactive;
+        if (d[k] != kInactive) act |= 1u << k;
+    }
+    uint32_t fullbits = 0;  // bit k: item k's cell is full
+    if (!FP32 && REFRESH == 3) {
+        double w[ITEMS], fill[ITEMS];
+#pragma unroll
+        for (int k = 0; k < ITEMS; ++k) {
+            const uint32_t slot = base + (uint32_t)(k * 32);
+            w[k] = -1.0; fill[k] = 0.0;
+            if (slot < n) {
+                w[k] = fr.inc[slot];
+                fill[k] = ((const double*)fr.fill)[slot];
+            }
+        }
+#pragma unroll
+        for (int k = 0; k < ITEMS; ++k) {
+            const uint32_t slot = base + (uint32_t)(k * 32);
+            if (((act >> k) & 1u) && (d[k] & kStale)) {
+                if (d[k] & kPend) {
+                    w[k] = answered_velocity(a, fr, slot, d[k], ((const unsigned long long*)fr.vel)[slot]);
+                    ((double*)fr.vel)[slot] = w[k];
+                } else {
+                    w[k] = ((const double*)fr.vel)[slot];
+                }
+            }
+        }
+#pragma unroll
+        for (int k = 0; k < ITEMS; ++k) {
+            if (!((act >> k) & 1u)) continue;
+            ++sv;
+            const uint32_t slot = base + (uint32_t)(k * 32);
+            double inc = w[k];
+            if (d[k] & kStale) {
+                if (__double_as_longlong(w[k]) >= 0) inc = __dmul_rn(__dmul_rn(w[k], a.dt), a.cinv);
+                fr.inc[slot] = inc;
+                fr.dir[slot] = d[k] & kCodeMask;
+            }
+            if (__double_as_longlong(inc) >= 0) {
+                const double f = __dadd_rn(fill[k], inc);
+                ((double*)fr.fill)[slot] = f;
+                if (__double_as_longlong(f) >= 0x3FF0000000000000ll) fullbits |= 1u << k;
+            }
+        }
+    } else if (!FP32) {
+        // in two halves of the items, each loaded, brought to its velocity factor and updated before
+        // the next: the loads of one half stay in flight together and nothing spills
+        constexpr int H = ITEMS / 2;
+#pragma unroll
+        for (int h = 0; h < 2; ++h) {
+            double w[H], fill[H];  // w: cached inc, or vel when the increment is stale
+            if (REFRESH == 0) {
+#pragma unroll
+                for (int j = 0; j < H; ++j) {
+                    const int k = h * H + j;
+                    const uint32_t slot = base + (uint32_t)(k * 32);
+                    w[j] = -1.0; fill[j] = 0.0;
+                    if ((act >> k) & 1u) {
+                        w[j] = a.dt_changed ? ((const double*)fr.vel)[slot] : fr.inc[slot];
+                        fill[j] = ((const double*)fr.fill)[slot];
+                    }
+                }
+#pragma unroll
+                for (int j = 0; j < H; ++j) {
+                    const int k = h * H + j;
+                    const uint32_t slot = base + (uint32_t)(k * 32);
+                    if (((act >> k) & 1u) && (d[k] & kStale)) {  // nuclei, cells answered by the host: no increment yet
+                        if (d[k] & kPend) {
+                            w[j] = answered_velocity(a, fr, slot, d[k], ((const unsigned long long*)fr.vel)[slot]);
+                            ((double*)fr.vel)[slot] = w[j];
+                        } else if (!a.dt_changed) {
+                            w[j] = ((const double*)fr.vel)[slot];
+                        }
+                    }
+                }
+            } else if (REFRESH == 2) {
+                double mo[H];
+                uint32_t g[H];
+#pragma unroll
+                for (int j = 0; j < H; ++j) {
+                    const int k = h * H + j;
+                    const uint32_t slot = base + (uint32_t)(k * 32);
+                    w[j] = -1.0; fill[j] = 0.0; mo[j] = 0.0; g[j] = 0;
+                    if ((act >> k) & 1u) {
+                        mo[j] = fr.mob[slot];
+                        g[j] = fr.defg[slot];
+                        fill[j] = ((const double*)fr.fill)[slot];
+                    }
+                }
+#pragma unroll
+                for (int j = 0; j < H; ++j) {
+                    const int k = h * H + j;
+                    const uint32_t slot = base + (uint32_t)(k * 32);
+                    if ((act >> k) & 1u) {
+                        if (d[k] & kPend) w[j] = answered_velocity(a, fr, slot, d[k], ((const unsigned long long*)fr.vel)[slot]);
+                        else w[j] = velocity_from_mobility(a, mo[j], g[j], d[k] & kCodeMask);
+                        ((double*)fr.vel)[slot] = w[j];
+                    }
+                }
+            } else {
+#pragma unroll
+                for (int j = 0; j < H; ++j) {
+                    const int k = h * H + j;
+                    const uint32_t slot = base + (uint32_t)(k * 32);
+                    w[j] = -1.0; fill[j] = 0.0;
+                    if ((act >> k) & 1u) {
+                        if (d[k] & kPend) {
+                            w[j] = answered_velocity(a, fr, slot, d[k], ((const unsigned long long*)fr.vel)[slot]);
+                        } else {
+                            const uint32_t g = fr.defg[slot];
+                            const double P = __longlong_as_double((long long)a.ptab[(unsigned long long)fr.rxg[slot] * a.ndefg + g]);
+                            const double mo = mobility(a, P);
+                            fr.mob[slot] = mo;
+                            w[j] = velocity_from_mobility(a, mo, g, d[k] & kCodeMask);
+                        }
+                        ((double*)fr.vel)[slot] = w[j];
+                        fill[j] = ((const double*)fr.fill)[slot];
+                    }
+                }
+            }
+#pragma unroll
+            for (int j = 0; j < H; ++j) {
+                const int k = h * H + j;
+                if (!((act >> k) & 1u)) continue;
+                ++sv;
+                const uint32_t slot = base + (uint32_t)(k * 32);
+                double inc = w[j];
+                if (REFRESH != 0 || a.dt_changed || (d[k] & kStale)) {
+                    if (__double_as_longlong(w[j]) >= 0) inc = __dmul_rn(__dmul_rn(w[j], a.dt), a.cinv);
+                    fr.inc[slot] = inc;
+                    if (d[k] & kStale) fr.dir[slot] = d[k] & kCodeMask;
+                }
+                if (__double_as_longlong(inc) >= 0) {  // sign bit clear: driving force present
+                    const double f = __dadd_rn(fill[j], inc);
+                    ((double*)fr.fill)[slot] = f;
+                    if (__double_as_longlong(f) >= 0x3FF0000000000000ll) fullbits |= 1u << k;  // f >= 1.0, never negative
+                }
+            }
+        }
+    } else {
+        constexpr int H = ITEMS / 2;  // two halves, as the FP64 fill
+#pragma unroll
+        for (int h = 0; h < 2; ++h) {
+            float vel[H], fill[H], comp[H];
+            if (REFRESH == 0 || REFRESH == 3) {
+#pragma unroll
+                for (int j = 0; j < H; ++j) {
+                    const int k = h * H + j;
+                    const uint32_t slot = base + (uint32_t)(k * 32);
+                    vel[j] = -1.0f; fill[j] = 0.0f; comp[j] = 0.0f;
+                    if (REFRESH == 3 ? slot < n : ((act >> k) & 1u)) {
+                        vel[j] = ((const float*)fr.vel)[slot];
+                        fill[j] = ((const float*)fr.fill)[slot];
+                        comp[j] = fr.comp[slot];
+                    }
+                }
+#pragma unroll
+                for (int j = 0; j < H; ++j) {
+                    const int k = h * H + j;
+                    const uint32_t slot = base + (uint32_t)(k * 32);
+                    if (((act >> k) & 1u) && (d[k] & kPend)) {
+                        vel[j] = (float)answered_velocity(a, fr, slot, d[k], ((const uint32_t*)fr.vel)[slot]);
+                        ((float*)fr.vel)[slot] = vel[j];
+                    }
+                }
+            } else if (REFRESH == 2) {
+                double mo[H];
+                uint32_t g[H];
+#pragma unroll
+                for (int j = 0; j < H; ++j) {
+                    const int k = h * H + j;
+                    const uint32_t slot = base + (uint32_t)(k * 32);
+                    vel[j] = -1.0f; fill[j] = 0.0f; comp[j] = 0.0f; mo[j] = 0.0; g[j] = 0;
+                    if ((act >> k) & 1u) {
+                        mo[j] = fr.mob[slot];
+                        g[j] = fr.defg[slot];
+                        fill[j] = ((const float*)fr.fill)[slot];
+                        comp[j] = fr.comp[slot];
+                    }
+                }
+#pragma unroll
+                for (int j = 0; j < H; ++j) {
+                    const int k = h * H + j;
+                    const uint32_t slot = base + (uint32_t)(k * 32);
+                    if ((act >> k) & 1u) {
+                        if (d[k] & kPend) vel[j] = (float)answered_velocity(a, fr, slot, d[k], ((const uint32_t*)fr.vel)[slot]);
+                        else vel[j] = (float)velocity_from_mobility(a, mo[j], g[j], d[k] & kCodeMask);
+                        ((float*)fr.vel)[slot] = vel[j];
+                    }
+                }
+            } else {
+#pragma unroll
+                for (int j = 0; j < H; ++j) {
+                    const int k = h * H + j;
+                    const uint32_t slot = base + (uint32_t)(k * 32);
+                    vel[j] = -1.0f; fill[j] = 0.0f; comp[j] = 0.0f;
+                    if ((act >> k) & 1u) {
+                        if (d[k] & kPend) {
+                            vel[j] = (float)answered_velocity(a, fr, slot, d[k], ((const uint32_t*)fr.vel)[slot]);
+                        } else {
+                            const uint32_t g = fr.defg[slot];
+                            const double P = __longlong_as_double((long long)a.ptab[(unsigned long long)fr.rxg[slot] * a.ndefg + g]);
+                            const double mo = mobility(a, P);
+                            fr.mob[slot] = mo;
+                            vel[j] = (float)velocity_from_mobility(a, mo, g, d[k] & kCodeMask);
+                        }
+                        ((float*)fr.vel)[slot] = vel[j];
+                        fill[j] = ((const float*)fr.fill)[slot];
+                        comp[j] = fr.comp[slot];
+                    }
+                }
+            }
+#pragma unroll
+            for (int j = 0; j < H; ++j) {
+                const int k = h * H + j;
+                if (!((act >> k) & 1u)) continue;
+                ++sv;
+                const uint32_t slot = base + (uint32_t)(k * 32);
+                if (d[k] & kStale) fr.dir[slot] = d[k] & kCodeMask;
+                if (vel[j] >= 0.0f) {
+                    // Kahan-compensated accumulation of the fill
+                    const float inc = vel[j] * a.dtc32;
+                    const float y = inc - comp[j];
+                    const float t = fill[j] + y;
+                    const float c = (t - fill[j]) - y;
+                    ((float*)fr.fill)[slot] = t;
+                    fr.comp[slot] = c;
+                    if ((t - c) >= 1.0f) fullbits |= 1u << k;
+                }
+            }
+        }
+    }
+    tile_masks<ITEMS>(fr, tile, base, n, act, fullbits);
     return sv;
 }
 
@@ -567,9 +628,23 @@ __device__ __forceinline__ uint32_t list_slots(const DomainArgs& a, int L) { ret
 
 // ONE: a single domain (the plain path): its argument block sits at a launch-uniform
 // slot and the two lists are walked in turn, so every argument read is uniform.
-// R2: every stepping domain refreshes from cached mobilities (REFRESH 2, recovery); a
-// kernel of its own, so that its register-hungry early loads cost the other modes nothing.
-template <bool FP32, int ITEMS, bool ONE, bool R2>
+// MODE: the grow mode every stepping domain uses this step (0, 1, 2, 3 as grow_tile's REFRESH), or
+// kFillAny to decide per domain.  The host knows a single domain's mode before the launch, and a
+// kernel specialised to one mode holds only that mode's loads in its registers.
+constexpr int kFillAny = -1;
+
+template <bool FP32, int ITEMS, int MODE>
+__device__ __forceinline__ uint32_t grow_tile_mode(const DomainArgs& a, int L, uint32_t tile, uint32_t n) {
+    if (MODE == kFillAny) {
+        if (a.refresh == 2) return grow_tile<FP32, 2, ITEMS>(a, L, tile, n);
+        if (a.refresh == 1) return grow_tile<FP32, 1, ITEMS>(a, L, tile, n);
+        if (a.spec && !a.dt_changed) return grow_tile<FP32, 3, ITEMS>(a, L, tile, n);
+        return grow_tile<FP32, 0, ITEMS>(a, L, tile, n);
+    }
+    return grow_tile<FP32, MODE == kFillAny ? 0 : MODE, ITEMS>(a, L, tile, n);
+}
+
+template <bool FP32, int ITEMS, bool ONE, int MODE>
 __global__ void __launch_bounds__(kBlock, ITEMS >= 16 ? 2 : 4) k_grow_fill(int base, int ndom) {
     using S = GrowShape<ITEMS>;
     __shared__ uint32_t s_pre[kMaxSegs + 1];
@@ -581,21 +656,7 @@ __global__ void __launch_bounds__(kBlock, ITEMS >= 16 ? 2 : 4) k_grow_fill(int b
             const uint32_t n = a.st->next_never[L];
             const uint32_t ntiles = (n + S::kTile - 1) / S::kTile;
             uint32_t sv = 0;
-            if (R2) {
-                if (a.spec) {
-                    for (uint32_t tile = blockIdx.x; tile < ntiles; tile += gridDim.x) sv += grow_tile<FP32, 4, ITEMS>(a, L, tile, n);
-                } else {
-                    for (uint32_t tile = blockIdx.x; tile < ntiles; tile += gridDim.x) sv += grow_tile<FP32, 2, ITEMS>(a, L, tile, n);
-                }
-            } else if (a.refresh == 1) {
-                for (uint32_t tile = blockIdx.x; tile < ntiles; tile += gridDim.x) sv += grow_tile<FP32, 1, ITEMS>(a, L, tile, n);
-            } else if (a.refresh == 2) {
-                for (uint32_t tile = blockIdx.x; tile < ntiles; tile += gridDim.x) sv += grow_tile<FP32, 2, ITEMS>(a, L, tile, n);
-            } else if (a.spec && !a.dt_changed) {
-                for (uint32_t tile = blockIdx.x; tile < ntiles; tile += gridDim.x) sv += grow_tile<FP32, 3, ITEMS>(a, L, tile, n);
-            } else {
-                for (uint32_t tile = blockIdx.x; tile < ntiles; tile += gridDim.x) sv += grow_tile<FP32, 0, ITEMS>(a, L, tile, n);
-            }
+            for (uint32_t tile = blockIdx.x; tile < ntiles; tile += gridDim.x) sv += grow_tile_mode<FP32, ITEMS, MODE>(a, L, tile, n);
             flush_sv(a, L, sv);
         }
         return;
@@ -616,14 +677,7 @@ __global__ void __launch_bounds__(kBlock, ITEMS >= 16 ? 2 : 4) k_grow_fill(int b
         const DomainArgs& a = c_args[base + (s >> 1)];
         const int L = s & 1;
         const uint32_t tile = u - s_pre[s];
-        const uint32_t n = a.st->next_never[L];
-        if (R2) {
-            if (a.spec) sv += grow_tile<FP32, 4, ITEMS>(a, L, tile, n);
-            else sv += grow_tile<FP32, 2, ITEMS>(a, L, tile, n);
-        } else if (a.refresh == 1) sv += grow_tile<FP32, 1, ITEMS>(a, L, tile, n);
-        else if (a.refresh == 2) sv += grow_tile<FP32, 2, ITEMS>(a, L, tile, n);
-        else if (a.spec && !a.dt_changed) sv += grow_tile<FP32, 3, ITEMS>(a, L, tile, n);
-        else sv += grow_tile<FP32, 0, ITEMS>(a, L, tile, n);
+        sv += grow_tile_mode<FP32, ITEMS, MODE>(a, L, tile, a.st->next_never[L]);
     }
     if (cur >= 0) flush_sv(c_args[base + (cur >> 1)], cur & 1, sv);
 }
@@ -754,24 +808,16 @@ __device__ __forceinline__ void scan_pairs_block(uint32_t* cnt, uint32_t ntiles,
 }
 
 // ------------------------------------------------------------------ K2 claim
-// Attempts LO..HI-1 of one full cell: the grid loads are all issued before the atomics
-// (claims are a min, so the order of the atomics does not matter).  Inside cells are
-// strictly interior (every list insertion checks it), so their targets are the cell
-// index plus a fixed offset; Border cells wrap through target_of.
-template <int LO, int HI, bool INSIDE>
-__device__ __forceinline__ uint32_t claim_plane(const DomainArgs& a, uint32_t cell, int x, int y, int z, uint32_t f) {
+// Attempts LO..HI-1 of one Border cell: the grid loads are all issued before the atomics
+// (claims are a min, so the order of the atomics does not matter); targets wrap through target_of.
+template <int LO, int HI>
+__device__ __forceinline__ uint32_t claim_plane(const DomainArgs& a, int x, int y, int z, uint32_t f) {
     uint32_t tg[HI - LO], gv[HI - LO];
 #pragma unroll
     for (int k = 0; k < HI - LO; ++k) {
         gv[k] = 0xFFFFFFFFu;
-        if (INSIDE) {
-            tg[k] = cell + (uint32_t)a.noff[LO + k];
-            if (tg[k] < a.ncells) gv[k] = a.grid[tg[k]];  // not __ldg: stays behind the previous plane's atomics
-            else atomicOr(&a.st->err, kErrBounds);
-        } else {
-            bool inter;
-            if (target_of(a, 1, x, y, z, LO + k, tg[k], inter)) gv[k] = a.grid[tg[k]];
-        }
+        bool inter;
+        if (target_of(a, 1, x, y, z, LO + k, tg[k], inter)) gv[k] = a.grid[tg[k]];
     }
     uint32_t mask = 0;
 #pragma unroll
@@ -817,19 +863,22 @@ __global__ void __launch_bounds__(kBlock, 2) k_claim(int base, int ndom) {
         const uint32_t F0 = a.st->nfull[0];
         uint32_t mask;
         if (f < F0) {
-            // an Inside cell: all 26 grid reads in flight before the first claim
+            // an Inside cell (strictly interior, every list insertion checks it): its neighbourhood
+            // spans 8 bricks; all 26 grid reads in flight before the first claim
             const uint32_t cell = a.f[0].xyz[a.f[0].full[f]];
             a.fcell[f] = cell;
+            int x, y, z;
+            decode(a, cell, x, y, z);
             uint32_t gv[26];
 #pragma unroll
             for (int d = 0; d < 26; ++d) {
-                const uint32_t t = cell + (uint32_t)a.noff[d];
+                const uint32_t t = gindex(a, (uint32_t)(x + c_dx[d]), (uint32_t)(y + c_dy[d]), (uint32_t)(z + c_dz[d]));
                 gv[d] = t < a.ncells ? a.grid[t] : 0xFFFFFFFFu;
             }
             mask = 0;
 #pragma unroll
             for (int d = 0; d < 26; ++d) {
-                const uint32_t t = cell + (uint32_t)a.noff[d];
+                const uint32_t t = gindex(a, (uint32_t)(x + c_dx[d]), (uint32_t)(y + c_dy[d]), (uint32_t)(z + c_dz[d]));
                 if (t >= a.ncells) atomicOr(&a.st->err, kErrBounds);
                 else if (gv[d] < a.ndefg) {
                     atomicMin(&a.claim[t], f * 26u + (uint32_t)d);
@@ -841,9 +890,9 @@ __global__ void __launch_bounds__(kBlock, 2) k_claim(int base, int ndom) {
             a.fcell[f] = cell;
             int x, y, z;
             decode(a, cell, x, y, z);
-            mask = claim_plane<0, 8, false>(a, cell, x, y, z, f);
-            mask |= claim_plane<8, 17, false>(a, cell, x, y, z, f);
-            mask |= claim_plane<17, 26, false>(a, cell, x, y, z, f);
+            mask = claim_plane<0, 8>(a, x, y, z, f);
+            mask |= claim_plane<8, 17>(a, x, y, z, f);
+            mask |= claim_plane<17, 26>(a, x, y, z, f);
         }
         a.amask[f] = mask;
     }
@@ -915,6 +964,59 @@ __device__ __forceinline__ bool lookup_p(const DomainArgs& a, uint32_t rxg, uint
     if ((bits >> 48) == (kPtabTag >> 48)) { tag = (uint32_t)bits; return false; }
     P = __longlong_as_double((long long)bits);
     return true;
+}
+
+// ------------------------------------------------------------------ K4 step end
+// Host mailbox in pinned, device-mapped memory: k_step_end writes the step's scalars,
+// the mobility-weight requests and the depleted grains straight into host memory, so
+// the host needs one stream synchronization per step and no copies.
+constexpr uint32_t kBoxMiss = 16384;
+constexpr uint32_t kBoxDep = 16384;
+struct HostBox {
+    DevState snap;
+    unsigned long long miss[kBoxMiss];
+    uint32_t depleted[kBoxDep];
+};
+
+// The end of a domain's step, by one block: advances the high-water marks, posts the step to the
+// domain's mailbox, clears the supertile counters the step used and the per-step fields.  The
+// step's scalars, requests and depleted grains are read through L2 (__ldcg): in the commit's last
+// block they were written by other blocks of the same launch.
+__device__ __forceinline__ void step_end_block(const DomainArgs& a, uint32_t grow_tile) {
+    DevState* st = a.st;
+    HostBox* box = a.box;
+    __shared__ uint32_t s_nm, s_nd, s_sup[3];
+    __shared__ unsigned long long s_state[(sizeof(DevState) + 7) / 8];  // the step's scalars, read once through L2
+    for (uint32_t i = threadIdx.x; i < sizeof(DevState) / 8; i += blockDim.x) s_state[i] = __ldcg((const unsigned long long*)st + i);
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        DevState& v = *(DevState*)s_state;
+        const uint32_t F = v.nfull[0] + v.nfull[1];
+        for (int L = 0; L < 2; ++L) s_sup[L] = ((v.next_never[L] + grow_tile - 1) / grow_tile + kSuper - 1) / kSuper;
+        s_sup[2] = ((F + kBlock - 1) / kBlock + kSuper - 1) / kSuper;
+        const uint32_t cap[2] = {a.f[0].cap, a.f[1].cap};
+        for (int D = 0; D < 2; ++D) {
+            if (v.nwin[D] > v.nrec[D]) v.next_never[D] += v.nwin[D] - v.nrec[D];
+            if (v.next_never[D] > cap[D]) { v.next_never[D] = cap[D]; v.err |= kErrCapacity; }
+        }
+        st->next_never[0] = v.next_never[0];
+        st->next_never[1] = v.next_never[1];
+        st->err = v.err;
+        box->snap = v;
+        s_nm = min(min(v.nmiss, a.misscap), kBoxMiss);
+        s_nd = min(min(v.ndepleted, a.ndefg), kBoxDep);
+    }
+    __syncthreads();
+    for (uint32_t i = threadIdx.x; i < s_nm; i += blockDim.x) box->miss[i] = __ldcg(&a.miss[i]);
+    for (uint32_t i = threadIdx.x; i < s_nd; i += blockDim.x) box->depleted[i] = __ldcg(&a.depleted[i]);
+    for (uint32_t i = threadIdx.x; i < 2 * s_sup[0]; i += blockDim.x) a.f[0].scnt[i] = 0u;
+    for (uint32_t i = threadIdx.x; i < 2 * s_sup[1]; i += blockDim.x) a.f[1].scnt[i] = 0u;
+    for (uint32_t i = threadIdx.x; i < 2 * s_sup[2]; i += blockDim.x) a.csct[i] = 0u;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        char* p = (char*)st + kStepFieldsOffset;
+        for (size_t i = 0; i < sizeof(DevState) - kStepFieldsOffset; ++i) p[i] = 0;
+    }
 }
 
 // ------------------------------------------------------------------ K3 commit (+ finalize)
@@ -1009,7 +1111,7 @@ __device__ __forceinline__ void flush_new(const DomainArgs& a, double pmax, uint
 }
 
 template <bool FP32, bool ONE>
-__global__ void __launch_bounds__(kBlock, 3) k_commit(int base, int ndom) {
+__global__ void __launch_bounds__(kBlock, ONE ? 4 : 3) k_commit(int base, int ndom, uint32_t grow_tile) {
     __shared__ uint32_t s_pre[kMaxSegs + 1];
     __shared__ uint32_t s_a[kWarps], s_b[kWarps], s_w[kWarps], s_base[2];
     // per full cell of the tile: win masks, first ranks, cell (| Border list << 31), grain, overshoot
@@ -1178,52 +1280,26 @@ __global__ void __launch_bounds__(kBlock, 3) k_commit(int base, int ndom) {
         __syncthreads();
     }
     if (cur >= 0) flush_new(c_args[base + cur], pmax, ntag);
+    if (ONE) {
+        // a single domain's step ends in the last block to finish (no separate launch)
+        const DomainArgs& a = c_args[base];
+        if (!a.active) return;
+        __shared__ bool s_last;
+        __threadfence();  // this block's stores before its count
+        __syncthreads();
+        if (threadIdx.x == 0) s_last = atomicAdd(&a.st->commit_done, 1u) == gridDim.x - 1;
+        __syncthreads();
+        if (!s_last) return;
+        __threadfence();
+        step_end_block(a, grow_tile);
+    }
 }
 
-// ------------------------------------------------------------------ K4 step end
-// Host mailbox in pinned, device-mapped memory: k_step_end writes the step's scalars,
-// the mobility-weight requests and the depleted grains straight into host memory, so
-// the host needs one stream synchronization per step and no copies.
-constexpr uint32_t kBoxMiss = 16384;
-constexpr uint32_t kBoxDep = 16384;
-struct HostBox {
-    DevState snap;
-    unsigned long long miss[kBoxMiss];
-    uint32_t depleted[kBoxDep];
-};
-
-// One block per domain: advances the high-water marks, posts the step to the domain's
-// mailbox, clears the supertile counters the step used and the per-step fields.
+// One block per domain (batches; a single domain closes its step in the commit's last block).
 __global__ void __launch_bounds__(kBlock) k_step_end(int base, int ndom, uint32_t grow_tile) {
     const DomainArgs& a = c_args[base + (blockIdx.x)];
     if (!a.active) return;
-    DevState* st = a.st;
-    HostBox* box = a.box;
-    __shared__ uint32_t s_nm, s_nd, s_sup[3];
-    if (threadIdx.x == 0) {
-        const uint32_t F = st->nfull[0] + st->nfull[1];
-        for (int L = 0; L < 2; ++L) s_sup[L] = ((st->next_never[L] + grow_tile - 1) / grow_tile + kSuper - 1) / kSuper;
-        s_sup[2] = ((F + kBlock - 1) / kBlock + kSuper - 1) / kSuper;
-        const uint32_t cap[2] = {a.f[0].cap, a.f[1].cap};
-        for (int D = 0; D < 2; ++D) {
-            if (st->nwin[D] > st->nrec[D]) st->next_never[D] += st->nwin[D] - st->nrec[D];
-            if (st->next_never[D] > cap[D]) { st->next_never[D] = cap[D]; st->err |= kErrCapacity; }
-        }
-        box->snap = *st;
-        s_nm = min(min(st->nmiss, a.misscap), kBoxMiss);
-        s_nd = min(min(st->ndepleted, a.ndefg), kBoxDep);
-    }
-    __syncthreads();
-    for (uint32_t i = threadIdx.x; i < s_nm; i += blockDim.x) box->miss[i] = a.miss[i];
-    for (uint32_t i = threadIdx.x; i < s_nd; i += blockDim.x) box->depleted[i] = a.depleted[i];
-    for (uint32_t i = threadIdx.x; i < 2 * s_sup[0]; i += blockDim.x) a.f[0].scnt[i] = 0u;
-    for (uint32_t i = threadIdx.x; i < 2 * s_sup[1]; i += blockDim.x) a.f[1].scnt[i] = 0u;
-    for (uint32_t i = threadIdx.x; i < 2 * s_sup[2]; i += blockDim.x) a.csct[i] = 0u;
-    __syncthreads();
-    if (threadIdx.x == 0) {
-        char* p = (char*)st + kStepFieldsOffset;
-        for (size_t i = 0; i < sizeof(DevState) - kStepFieldsOffset; ++i) p[i] = 0;
-    }
+    step_end_block(a, grow_tile);
 }
 
 }  // namespace score
