@@ -522,7 +522,7 @@ struct TuneCfg {
     int fill_bpsm = 16;     // k_grow_fill blocks per SM
     int claim_bpsm = 2;     // k_claim blocks per SM (autotuner's choice on the 512^3 workload)
     int commit_bpsm = 8;    // k_resolve / k_commit blocks per SM (same)
-    int spec_pct = 30;      // every slot's data loaded with its infector byte up to this INACTIVE share [%]
+    int spec_pct = 60;      // every slot's data loaded with its infector byte up to this INACTIVE share [%]
     int timing_every = 8;   // phase events on every k-th step of a run (0 never): each event costs
                             // microseconds of device time, so the steps in between run without
     bool operator==(const TuneCfg& o) const {
@@ -735,7 +735,7 @@ void for_grains(score_ctx* c, Body body) {
     const size_t n = c->ndefg;
     Engine& E = *c->eng;
     if (n < 8192 || E.dom.size() != 1) { body(0, n); return; }
-    E.workers(7);
+    E.workers(15);
     constexpr int kChunks = 16;
     E.pool->run(kChunks, [&](int k) { body(n * (size_t)k / kChunks, n * (size_t)(k + 1) / kChunks); });
 }
@@ -818,8 +818,8 @@ void resolve_weights(score_ctx* c, const std::vector<unsigned long long>& idx, s
     size_t n = idx.size();
     Engine& E = *c->eng;
     if (n >= 16 && E.dom.size() == 1) {  // one domain: the engine's workers (a batch runs its domains in parallel)
-        E.workers(7);
-        const int chunks = (int)std::min<size_t>(32, n / 8);
+        E.workers(15);
+        const int chunks = (int)std::min<size_t>(64, n / 8);
         E.pool->run(chunks, [&](int k) { work(n * (size_t)k / chunks, n * (size_t)(k + 1) / chunks); });
         return;
     }
@@ -1326,7 +1326,9 @@ inline void record(const Engine& E, int k) {
 template <bool FP32, int ITEMS>
 void launch_grow(const Engine& E, int n) {
     const uint32_t g = (uint32_t)(E.sms * E.cfg.fill_bpsm);
-    if (n == 1) {
+    if (n == 1 && !FP32 && E.fill_mode == 3 && ITEMS <= 8) {  // 16 items spill in the pipelined kernel
+        k_grow_fill_pf<ITEMS><<<g, kBlock, 0, E.stream>>>(E.base);
+    } else if (n == 1) {
         switch (E.fill_mode) {
             case 0: k_grow_fill<FP32, ITEMS, true, 0><<<g, kBlock, 0, E.stream>>>(E.base, n); break;
             case 1: k_grow_fill<FP32, ITEMS, true, 1><<<g, kBlock, 0, E.stream>>>(E.base, n); break;

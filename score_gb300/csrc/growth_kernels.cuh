@@ -682,6 +682,91 @@ __global__ void __launch_bounds__(kBlock, ITEMS >= 16 ? 2 : 4) k_grow_fill(int b
     if (cur >= 0) flush_sv(c_args[base + (cur >> 1)], cur & 1, sv);
 }
 
+// The FP64 fill of a single domain in grow mode 3 (dt unchanged, few holes), software-pipelined:
+// a thread's loads for its next tile (infector bytes, increments, fills) are issued before the
+// current tile's additions, so that one tile's FP64 adds and stores overlap the next tile's memory
+// round trip.  The tiles of both lists form one sequence (list 0's, then list 1's).  Arithmetic,
+// stores and masks are grow_tile's in mode 3.
+template <int ITEMS>
+struct Mode3Regs {
+    uint8_t d[ITEMS];
+    double w[ITEMS], f[ITEMS];
+};
+
+template <int ITEMS>
+__device__ __forceinline__ void mode3_load(const DomainArgs& a, uint32_t u, uint32_t t0, uint32_t n0, uint32_t n1, Mode3Regs<ITEMS>& r) {
+    using S = GrowShape<ITEMS>;
+    const int L = u >= t0 ? 1 : 0;
+    const DFront& fr = a.f[L];
+    const uint32_t n = L ? n1 : n0;
+    const uint32_t base = (L ? u - t0 : u) * S::kTile + (uint32_t)(threadIdx.x >> 5) * 32u * ITEMS + (threadIdx.x & 31u);
+#pragma unroll
+    for (int k = 0; k < ITEMS; ++k) {
+        const uint32_t slot = base + (uint32_t)(k * 32);
+        r.d[k] = kInactive; r.w[k] = -1.0; r.f[k] = 0.0;
+        if (slot < n) {
+            r.d[k] = fr.dir[slot];
+            r.w[k] = fr.inc[slot];
+            r.f[k] = ((const double*)fr.fill)[slot];
+        }
+    }
+}
+
+template <int ITEMS>
+__global__ void __launch_bounds__(kBlock, ITEMS >= 8 ? 2 : 3) k_grow_fill_pf(int base) {
+    using S = GrowShape<ITEMS>;
+    const DomainArgs& a = c_args[base];
+    if (!a.active) return;
+    const uint32_t n0 = a.st->next_never[0], n1 = a.st->next_never[1];
+    const uint32_t t0 = (n0 + S::kTile - 1) / S::kTile, total = t0 + (n1 + S::kTile - 1) / S::kTile;
+    uint32_t sv0 = 0, sv1 = 0;  // ACTIVE slots per list
+    uint32_t u = blockIdx.x;
+    Mode3Regs<ITEMS> cur;
+    if (u < total) mode3_load<ITEMS>(a, u, t0, n0, n1, cur);
+    while (u < total) {
+        const uint32_t un = u + gridDim.x;
+        Mode3Regs<ITEMS> nxt;
+        if (un < total) mode3_load<ITEMS>(a, un, t0, n0, n1, nxt);  // in flight during this tile's work
+        const int L = u >= t0 ? 1 : 0;
+        const DFront& fr = a.f[L];
+        const uint32_t n = L ? n1 : n0, tile = L ? u - t0 : u;
+        const uint32_t base_slot = tile * S::kTile + (uint32_t)(threadIdx.x >> 5) * 32u * ITEMS + (threadIdx.x & 31u);
+        uint32_t act = 0, fullbits = 0;
+#pragma unroll
+        for (int k = 0; k < ITEMS; ++k) {
+            if (cur.d[k] == kInactive) continue;
+            act |= 1u << k;
+            if (!(cur.d[k] & kStale)) continue;  // nuclei, cells answered by the host: no increment yet
+            const uint32_t slot = base_slot + (uint32_t)(k * 32);
+            double w;
+            if (cur.d[k] & kPend) {
+                w = answered_velocity(a, fr, slot, cur.d[k], ((const unsigned long long*)fr.vel)[slot]);
+                ((double*)fr.vel)[slot] = w;
+            } else {
+                w = ((const double*)fr.vel)[slot];
+            }
+            cur.w[k] = __double_as_longlong(w) >= 0 ? __dmul_rn(__dmul_rn(w, a.dt), a.cinv) : w;
+            fr.inc[slot] = cur.w[k];
+            fr.dir[slot] = cur.d[k] & kCodeMask;
+        }
+#pragma unroll
+        for (int k = 0; k < ITEMS; ++k) {
+            // sign bit clear: driving force present
+            if (!((act >> k) & 1u) || __double_as_longlong(cur.w[k]) < 0) continue;
+            const double f = __dadd_rn(cur.f[k], cur.w[k]);
+            ((double*)fr.fill)[base_slot + (uint32_t)(k * 32)] = f;
+            if (__double_as_longlong(f) >= 0x3FF0000000000000ll) fullbits |= 1u << k;  // f >= 1.0
+        }
+        if (L) sv1 += (uint32_t)__popc(act);
+        else sv0 += (uint32_t)__popc(act);
+        tile_masks<ITEMS>(fr, tile, base_slot, n, act, fullbits);
+        u = un;
+        if (u < total) cur = nxt;
+    }
+    flush_sv(a, 0, sv0);
+    flush_sv(a, 1, sv1);
+}
+
 // one warp per grow tile
 template <int ITEMS>
 __global__ void __launch_bounds__(kBlock) k_grow_lists(int base, int ndom) {
@@ -1285,9 +1370,13 @@ __global__ void __launch_bounds__(kBlock, ONE ? 4 : 3) k_commit(int base, int nd
         const DomainArgs& a = c_args[base];
         if (!a.active) return;
         __shared__ bool s_last;
-        __threadfence();  // this block's stores before its count
+        // the block's stores before its count: the barrier orders them before thread 0's fence, which
+        // is cumulative (one fence per block instead of one per thread)
         __syncthreads();
-        if (threadIdx.x == 0) s_last = atomicAdd(&a.st->commit_done, 1u) == gridDim.x - 1;
+        if (threadIdx.x == 0) {
+            __threadfence();
+            s_last = atomicAdd(&a.st->commit_done, 1u) == gridDim.x - 1;
+        }
         __syncthreads();
         if (!s_last) return;
         __threadfence();
