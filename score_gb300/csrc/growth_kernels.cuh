@@ -180,10 +180,12 @@ __device__ __forceinline__ double mobility(const DomainArgs& a, double P) {
     return __dadd_rn(__dmul_rn(P, a.mGS), __dmul_rn(__dsub_rn(1.0, P), a.mHAGB));
 }
 // velocity factor (m p) f_geo, or -1 when the driving force is not above 5e-16
-__device__ __forceinline__ double velocity_from_mobility(const DomainArgs& a, double m, uint32_t defg, int code) {
-    const double p = a.pforce[defg];
+__device__ __forceinline__ double velocity_from_force(double m, double p, int code) {
     if (!(p > 5.0e-16)) return -1.0;
     return __dmul_rn(__dmul_rn(m, p), c_sf[code]);
+}
+__device__ __forceinline__ double velocity_from_mobility(const DomainArgs& a, double m, uint32_t defg, int code) {
+    return velocity_from_force(m, a.pforce[defg], code);
 }
 __device__ __forceinline__ double velocity_factor(const DomainArgs& a, double P, uint32_t defg, int code) {
     return velocity_from_mobility(a, mobility(a, P), defg, code);
@@ -1033,7 +1035,9 @@ __device__ __forceinline__ double d_disori(const DomainArgs& A, const double p[4
 __device__ __forceinline__ bool lookup_p(const DomainArgs& a, uint32_t rxg, uint32_t defg, double& P, uint32_t& tag) {
     const unsigned long long idx = (unsigned long long)rxg * a.ndefg + defg;
     unsigned long long* e = &a.ptab[idx];
-    unsigned long long bits = *(volatile unsigned long long*)e;
+    // a plain (L1-cached) load: within a launch an entry only goes from EMPTY to a tag, and a stale
+    // EMPTY is settled by the compare-and-swap below
+    unsigned long long bits = *e;
     if (bits == kPtabEmpty) {
         const uint32_t m = atomicAdd(&a.st->nmiss, 1u);
         if (m >= a.misscap) { atomicOr(&a.st->err, kErrMissCap); tag = 0; return false; }
@@ -1291,12 +1295,13 @@ __global__ void __launch_bounds__(kBlock, ONE ? 4 : 3) k_commit(int base, int nd
             uint32_t tgt;
             bool inter;
             target_of(a, Ls, x, y, z, d, tgt, inter);
+            const uint32_t gt = a.grid[tgt];  // in flight together with the slot's load
             const DFront& dst = a.f[D];
             const uint32_t nrec = a.st->nrec[D];
             const uint32_t ns = r < nrec ? dst.recyc[r] : a.st->next_never[D] + (r - nrec);
             if (ns >= dst.cap) { atomicOr(&a.st->err, kErrCapacity); continue; }
             if (D == 1 && a.border_policy == 0 && r >= nrec && ns >= a.border_ref_cap) atomicOr(&a.st->err, kErrBorderRef);
-            const uint32_t gt = a.grid[tgt];
+            const double pf = a.pforce[gt];  // in flight together with the weight's load
             const int cls = c_cls[d];
             if (!FP32) {
                 const double fac = cls == 1 ? 0.0682 : (cls == 2 ? 0.0542 : 0.0484);
@@ -1318,7 +1323,7 @@ __global__ void __launch_bounds__(kBlock, ONE ? 4 : 3) k_commit(int base, int nd
             if (lookup_p(a, rs, gt, P, tag)) {
                 const double mo = mobility(a, P);
                 dst.mob[ns] = mo;
-                const double v = velocity_from_mobility(a, mo, gt, c_code[d]);
+                const double v = velocity_from_force(mo, pf, c_code[d]);
                 if (!FP32) {
                     // the increment with this step's dt: valid next step unless dt changes, when
                     // k_grow_fill recomputes every increment from vel anyway
