@@ -288,23 +288,24 @@ constexpr uint32_t kSuper = 64;  // tiles per supertile of the two-level tile pr
 
 // Exclusive prefix of tile `tile` of a (cnt: count pairs, `per` entries per tile;
 // sup: per-supertile pairs) count array, computed by one warp; every lane returns both.
+template <int U = 4>
 __device__ __forceinline__ void tile_prefix(const uint32_t* cnt, const uint32_t* sup, uint32_t tile, uint32_t& pa, uint32_t& pb,
                                             uint32_t per = 1) {
     // the supertile sums [0, s) then the count pairs [s kSuper per, tile per), as one
-    // index range of 8-byte loads with four in flight per lane before any add waits
+    // index range of 8-byte loads with U in flight per lane before any add waits
     const uint32_t s = tile / kSuper, lo = s * kSuper * per, n = s + (tile * per - lo);
     const uint2* ps = (const uint2*)sup;
     const uint2* pc = (const uint2*)cnt + lo - s;
     uint32_t a = 0, b = 0;
-    for (uint32_t i = threadIdx.x & 31; i < n; i += 128) {
-        uint2 x[4];
+    for (uint32_t i = threadIdx.x & 31; i < n; i += 32 * U) {
+        uint2 x[U];
 #pragma unroll
-        for (int k = 0; k < 4; ++k) {
+        for (int k = 0; k < U; ++k) {
             const uint32_t j = i + 32u * k;
             x[k] = j < n ? (j < s ? ps[j] : pc[j]) : make_uint2(0u, 0u);
         }
 #pragma unroll
-        for (int k = 0; k < 4; ++k) { a += x[k].x; b += x[k].y; }
+        for (int k = 0; k < U; ++k) { a += x[k].x; b += x[k].y; }
     }
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) {
@@ -789,7 +790,8 @@ __global__ void __launch_bounds__(kBlock) k_grow_lists(int base, int ndom) {
         const DFront& fr = a.f[L];
         const uint32_t tile = u - s_pre[s];
         uint32_t rf, ri;
-        tile_prefix(fr.tcnt, fr.scnt, tile, rf, ri, kWarps);  // the fill wrote one count pair per warp
+        // the fill wrote one count pair per warp: up to kSuper x kWarps pairs, all loads in flight at once
+        tile_prefix<8>(fr.tcnt, fr.scnt, tile, rf, ri, kWarps);
         uint32_t fw[WPL], iw[WPL];
 #pragma unroll
         for (int h = 0; h < WPL; ++h) {
@@ -1240,11 +1242,16 @@ __global__ void __launch_bounds__(kBlock, ONE ? 4 : 3) k_commit(int base, int nd
         // the full cell's own data, loaded while the scans complete
         const int L = f >= F0 ? 1 : 0;
         uint32_t slot = 0, cell = 0, rsrc = 0, gsrc = 0;
+        double over = 0.0;  // the full cell's overshoot, for the cells it infects
         if (f < F) {
             slot = a.f[L].full[L ? f - F0 : f];
             cell = a.fcell[f];
             rsrc = a.f[L].rxg[slot];
             gsrc = a.f[L].defg[slot];
+            if (win) {  // loaded with the grain ids, one round trip
+                if (!FP32) over = __dsub_rn(((const double*)a.f[L].fill)[slot], 1.0);
+                else over = (double)((((const float*)a.f[L].fill)[slot] - 1.0f) - a.f[L].comp[slot]);
+            }
         }
         __syncthreads();
         uint32_t rA = s_base[0] + iA - cA, rB = s_base[1] + iB - cB, oW = iW - cW;
@@ -1266,10 +1273,7 @@ __global__ void __launch_bounds__(kBlock, ONE ? 4 : 3) k_commit(int base, int nd
         s_rB[threadIdx.x] = rB;
         s_cell[threadIdx.x] = cell | ((uint32_t)L << 31);
         s_rsrc[threadIdx.x] = rsrc;
-        if (win) {
-            if (!FP32) s_over[threadIdx.x] = __dsub_rn(((const double*)a.f[L].fill)[slot], 1.0);
-            else s_over[threadIdx.x] = (double)((((const float*)a.f[L].fill)[slot] - 1.0f) - a.f[L].comp[slot]);
-        }
+        if (win) s_over[threadIdx.x] = over;
         __syncthreads();
         // every win of the tile by all threads: win k belongs to the full cell t with
         // s_off[t] <= k < s_off[t + 1]; its direction is the (k - s_off[t])-th set bit and
