@@ -81,3 +81,23 @@ def test_gpu_grain_evolution_at_128_matches_oracle(gpu, tmp_path):
             "final": np.concatenate([fin["defg_counts"], fin["rxg_counts"]]), "tsimend": t_end, "cells": d.ncells}
     t_o, vol_o, box_o = oracle.rediscr_kinetics([desc], 100)
     assert np.array_equal(t, t_o) and np.array_equal(vol, vol_o) and box == box_o
+
+
+def test_gpu_grain_evolution_odd_extents_matches_oracle(gpu, tmp_path):
+    """Odd extents (padding words in the device grid's bricks): snapshots and RX area profiles."""
+    d = sg.generate_domain(45, 51, 37, 60, 40, seed=5)
+    spec = sg.UdsSpec(nx=45, ny=51, nz=37, logpoints=["0.0", "0.3", "0.6", "0.9"], area_threshold=3)
+    p = sg.read_uds(spec.write(tmp_path / "odd.uds"))
+    sim = oracle.Sim(p, d)
+    sim.advance()
+    ref = sim.grainevo(d.nz)
+    sim.close()
+    with sg.GrowthMachine(p, device=0) as gm:
+        gm.load_domain(d)
+        gm.place_nuclei()
+        gm.run_until()
+        log = gm.grainevo()
+    assert len(log) == len(ref) == 4
+    for (info, cnt, area), r in zip(log, ref):
+        assert (info.t, info.X, info.step, info.Sv) == (r["t"], r["X"], r["step"], r["Sv"])
+        assert np.array_equal(cnt, r["counts"]) and np.array_equal(area, r["area"])

@@ -48,7 +48,8 @@ def compare(p, d, ptable=None):
     return out, ref
 
 
-@pytest.mark.parametrize("shape,ngr,nnuc,seed", [((64, 64, 64), 40, 24, 7), ((50, 72, 56), 90, 60, 3)])
+# odd extents put padding words in the device grid's 2x2x2 bricks
+@pytest.mark.parametrize("shape,ngr,nnuc,seed", [((64, 64, 64), 40, 24, 7), ((50, 72, 56), 90, 60, 3), ((45, 51, 37), 60, 40, 5)])
 def test_fp64_matches_oracle(gpu, tmp_uds, shape, ngr, nnuc, seed):
     nx, ny, nz = shape
     d = sg.generate_domain(nx, ny, nz, ngr, nnuc, seed=seed)
@@ -74,6 +75,12 @@ def test_fp64_defragmentation(gpu, tmp_uds):
 def test_fp64_periodic_boundary(gpu, tmp_uds):
     d = sg.generate_domain(56, 64, 60, 50, 30, seed=14)
     compare(sg.read_uds(tmp_uds(sg.UdsSpec(nx=56, ny=64, nz=60, boundary=1))), d)
+
+
+def test_fp64_periodic_boundary_odd_extents(gpu, tmp_uds):
+    """Periodic wrap across the padded last brick of every axis."""
+    d = sg.generate_domain(33, 47, 29, 30, 20, seed=16)
+    compare(sg.read_uds(tmp_uds(sg.UdsSpec(nx=33, ny=47, nz=29, boundary=1))), d)
 
 
 def test_fp64_border_grow_policy(gpu, tmp_uds):

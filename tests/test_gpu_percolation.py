@@ -60,3 +60,18 @@ def test_gpu_percolation_at_128_mid_run(gpu, tmp_path):
         gm.run_until()
         r, t = check(gm, d, b, tag="128^3 X=0.3")
     assert r["n_clusters"] > 20 and r["n_clusters"] >= t["n_clusters"]
+
+
+def test_gpu_percolation_odd_extents_mid_run(gpu, tmp_path):
+    """Odd extents (padding words in the device grid's bricks) mid-run, against the oracle."""
+    d = sg.generate_domain(45, 51, 37, 60, 40, seed=5)
+    p = sg.read_uds(sg.UdsSpec(nx=45, ny=51, nz=37, xmax="0.4").write(tmp_path / "odd.uds"))
+    sim = oracle.Sim(p, d)
+    sim.advance()
+    b = sim.binarize()
+    sim.close()
+    with sg.GrowthMachine(p, device=0) as gm:
+        gm.load_domain(d)
+        gm.place_nuclei()
+        gm.run_until()
+        check(gm, d, b, tag="45x51x37 X=0.4")
