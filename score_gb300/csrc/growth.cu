@@ -650,11 +650,11 @@ struct Engine {
     bool events = false;               // the sequence being launched records the phase events
     int fill_mode = kFillAny;          // ... and the grow mode of every stepping domain (kFillAny: per domain)
     // the step without / with phase events, with the general / the refresh-only grow kernel
-    // the step graphs: with or without phase events, times the fill mode (0..3 or per domain)
-    static constexpr int kGraphs = 10;
+    // the step graphs: with or without phase events, times the fill mode (0..4 or per domain)
+    static constexpr int kGraphs = 12;
     cudaGraphExec_t gexec[kGraphs] = {};
     TuneCfg gcfg[kGraphs];
-    int gndom[kGraphs] = {-1, -1, -1, -1, -1, -1, -1, -1, -1, -1};
+    int gndom[kGraphs] = {-1, -1, -1, -1, -1, -1, -1, -1, -1, -1, -1, -1};
     bool gfp32[kGraphs] = {};
     uint64_t run_steps = 0;            // steps since the run started (phase sampling)
     // 0 start, 1 end of fill, 2 end of lists, 3 end of claim, 4 end of step, 5/6 run span
@@ -1328,9 +1328,13 @@ void launch_grow(const Engine& E, int n) {
     const uint32_t g = (uint32_t)(E.sms * E.cfg.fill_bpsm);
     if (n == 1 && !FP32 && E.fill_mode == 3 && ITEMS <= 8) {  // 16 items spill in the pipelined kernel
         k_grow_fill_pf<ITEMS><<<g, kBlock, 0, E.stream>>>(E.base);
+    } else if (n == 1 && !FP32 && E.fill_mode == 0) {
+        k_grow_fill_pf0<ITEMS><<<g, kBlock, 0, E.stream>>>(E.base);
+    } else if (n == 1 && !FP32 && E.fill_mode == 4) {
+        k_grow_fill_sparse<ITEMS><<<g, kBlock, 0, E.stream>>>(E.base);
     } else if (n == 1) {
         switch (E.fill_mode) {
-            case 0: k_grow_fill<FP32, ITEMS, true, 0><<<g, kBlock, 0, E.stream>>>(E.base, n); break;
+            case 0: case 4: k_grow_fill<FP32, ITEMS, true, 0><<<g, kBlock, 0, E.stream>>>(E.base, n); break;
             case 1: k_grow_fill<FP32, ITEMS, true, 1><<<g, kBlock, 0, E.stream>>>(E.base, n); break;
             case 2: k_grow_fill<FP32, ITEMS, true, 2><<<g, kBlock, 0, E.stream>>>(E.base, n); break;
             case 3: k_grow_fill<FP32, ITEMS, true, 3><<<g, kBlock, 0, E.stream>>>(E.base, n); break;
@@ -1397,7 +1401,7 @@ cudaError_t Engine::enqueue_step(int n, bool timed, int mode) {
         launches += step_kernels(n);
         return cudaGetLastError();
     }
-    const int k = (timed ? 1 : 0) + 2 * (mode == kFillAny ? 4 : mode);
+    const int k = (timed ? 1 : 0) + 2 * (mode == kFillAny ? 5 : mode);
     if (!gexec[k] || gndom[k] != n || !(gcfg[k] == cfg) || gfp32[k] != fp32) {
         if (gexec[k]) cudaGraphExecDestroy(gexec[k]);
         gexec[k] = nullptr;
@@ -1519,7 +1523,8 @@ int Engine::step(bool timed) {
     for (int i = 0; i < n; ++i) {
         if (!dom[i]->running) continue;
         const DomainArgs& a = h_args[i];
-        const int m = a.refresh == 2 ? 2 : a.refresh == 1 ? 1 : (a.spec && !a.dt_changed) ? 3 : 0;
+        // 0 cached increments, 1 / 2 refresh, 3 as 0 with few holes and dt unchanged, 4 as 0 with many holes
+        const int m = a.refresh == 2 ? 2 : a.refresh == 1 ? 1 : !a.spec ? 4 : !a.dt_changed ? 3 : 0;
         mode = (mode == -2 || mode == m) ? m : kFillAny;
     }
     if (n > 1 && mode != 2) mode = kFillAny;  // batches: the refresh-only kernel, or the per-domain one

@@ -770,6 +770,264 @@ __global__ void __launch_bounds__(kBlock, ITEMS >= 8 ? 2 : 3) k_grow_fill_pf(int
     flush_sv(a, 1, sv1);
 }
 
+// The FP64 fill of a single domain in grow mode 0 (the cached increment, or vel when dt changed;
+// lists with many holes, so only ACTIVE slots' data is loaded), pipelined over a thread's tiles: the
+// next tile's infector bytes are in flight while this tile's increments and fills are loaded, added
+// and stored, so that a tile costs one memory round trip instead of two.  Arithmetic, stores and
+// masks are grow_tile's in mode 0.
+template <int ITEMS>
+__device__ __forceinline__ void mode0_dir(const DomainArgs& a, uint32_t u, uint32_t t0, uint32_t n0, uint32_t n1, uint8_t (&d)[ITEMS]) {
+    using S = GrowShape<ITEMS>;
+    const int L = u >= t0 ? 1 : 0;
+    const uint32_t n = L ? n1 : n0;
+    const uint32_t base = (L ? u - t0 : u) * S::kTile + (uint32_t)(threadIdx.x >> 5) * 32u * ITEMS + (threadIdx.x & 31u);
+    const uint8_t* dir = a.f[L].dir;
+#pragma unroll
+    for (int k = 0; k < ITEMS; ++k) {
+        const uint32_t slot = base + (uint32_t)(k * 32);
+        d[k] = slot < n ? dir[slot] : kInactive;
+    }
+}
+
+template <int ITEMS>
+__global__ void __launch_bounds__(kBlock, ITEMS >= 16 ? 2 : 3) k_grow_fill_pf0(int base) {
+    using S = GrowShape<ITEMS>;
+    const DomainArgs& a = c_args[base];
+    if (!a.active) return;
+    const uint32_t n0 = a.st->next_never[0], n1 = a.st->next_never[1];
+    const uint32_t t0 = (n0 + S::kTile - 1) / S::kTile, total = t0 + (n1 + S::kTile - 1) / S::kTile;
+    const bool dtc = a.dt_changed != 0;
+    uint32_t sv0 = 0, sv1 = 0;  // ACTIVE slots per list
+    uint32_t u = blockIdx.x;
+    uint8_t d[ITEMS];
+    if (u < total) mode0_dir<ITEMS>(a, u, t0, n0, n1, d);
+    while (u < total) {
+        const uint32_t un = u + gridDim.x;
+        uint8_t dn[ITEMS];
+        if (un < total) mode0_dir<ITEMS>(a, un, t0, n0, n1, dn);  // in flight during this tile's work
+        const int L = u >= t0 ? 1 : 0;
+        const DFront& fr = a.f[L];
+        const uint32_t n = L ? n1 : n0, tile = L ? u - t0 : u;
+        const uint32_t base_slot = tile * S::kTile + (uint32_t)(threadIdx.x >> 5) * 32u * ITEMS + (threadIdx.x & 31u);
+        uint32_t act = 0, fullbits = 0;
+        double w[ITEMS], fil[ITEMS];  // w: cached inc, or vel when the increment is stale or dt changed
+#pragma unroll
+        for (int k = 0; k < ITEMS; ++k) {
+            const uint32_t slot = base_slot + (uint32_t)(k * 32);
+            w[k] = -1.0; fil[k] = 0.0;
+            if (d[k] != kInactive) {
+                act |= 1u << k;
+                w[k] = dtc ? ((const double*)fr.vel)[slot] : fr.inc[slot];
+                fil[k] = ((const double*)fr.fill)[slot];
+            }
+        }
+#pragma unroll
+        for (int k = 0; k < ITEMS; ++k) {
+            if (!((act >> k) & 1u) || !(d[k] & kStale)) continue;  // nuclei, cells answered by the host: no increment yet
+            const uint32_t slot = base_slot + (uint32_t)(k * 32);
+            if (d[k] & kPend) {
+                w[k] = answered_velocity(a, fr, slot, d[k], ((const unsigned long long*)fr.vel)[slot]);
+                ((double*)fr.vel)[slot] = w[k];
+            } else if (!dtc) {
+                w[k] = ((const double*)fr.vel)[slot];
+            }
+        }
+#pragma unroll
+        for (int k = 0; k < ITEMS; ++k) {
+            if (!((act >> k) & 1u)) continue;
+            const uint32_t slot = base_slot + (uint32_t)(k * 32);
+            double inc = w[k];
+            if (dtc || (d[k] & kStale)) {
+                if (__double_as_longlong(w[k]) >= 0) inc = __dmul_rn(__dmul_rn(w[k], a.dt), a.cinv);
+                fr.inc[slot] = inc;
+                if (d[k] & kStale) fr.dir[slot] = d[k] & kCodeMask;
+            }
+            if (__double_as_longlong(inc) >= 0) {  // sign bit clear: driving force present
+                const double f = __dadd_rn(fil[k], inc);
+                ((double*)fr.fill)[slot] = f;
+                if (__double_as_longlong(f) >= 0x3FF0000000000000ll) fullbits |= 1u << k;  // f >= 1.0
+            }
+        }
+        if (L) sv1 += (uint32_t)__popc(act);
+        else sv0 += (uint32_t)__popc(act);
+        tile_masks<ITEMS>(fr, tile, base_slot, n, act, fullbits);
+        u = un;
+        if (u < total) {
+#pragma unroll
+            for (int k = 0; k < ITEMS; ++k) d[k] = dn[k];
+        }
+    }
+    flush_sv(a, 0, sv0);
+    flush_sv(a, 1, sv1);
+}
+
+// The FP64 fill of a single domain in grow mode 0 while most of the list is holes (the last step's
+// INACTIVE share above spec_holes_pct).  A block takes a whole grow tile with one vector load of
+// infector bytes per thread (ITEMS consecutive slots each); each warp gathers its ACTIVE slots into a
+// shared list, and its lanes take them up to 4 x 32 at a time with all their increment and fill
+// loads in flight together, so that a memory round trip serves up to 128 ACTIVE slots instead of the
+// few a thread's strided items hold.  The next tile's infector bytes are in flight meanwhile.
+// Arithmetic and stores are grow_tile's in mode 0; the full and INACTIVE masks and the per-warp
+// counts keep the layout k_grow_lists reads.
+template <int ITEMS>
+struct SparseDir {  // a thread's ITEMS infector bytes
+    static_assert(ITEMS == 4 || ITEMS == 8 || ITEMS == 16, "items");
+    uint32_t w[ITEMS / 4];
+};
+
+template <int ITEMS>
+__device__ __forceinline__ void sparse_dir(const DomainArgs& a, uint32_t u, uint32_t t0, uint32_t n0, uint32_t n1, SparseDir<ITEMS>& r) {
+    using S = GrowShape<ITEMS>;
+    const int L = u >= t0 ? 1 : 0;
+    const uint32_t n = L ? n1 : n0;
+    const uint32_t first = (L ? u - t0 : u) * S::kTile + threadIdx.x * (uint32_t)ITEMS;
+    const uint8_t* dir = a.f[L].dir;
+    if (first + ITEMS <= n) {  // ITEMS bytes at an ITEMS-aligned slot: one vector load
+        if (ITEMS == 4) r.w[0] = *(const uint32_t*)(dir + first);
+        else if (ITEMS == 8) { const uint2 v = *(const uint2*)(dir + first); r.w[0] = v.x; r.w[1] = v.y; }
+        else { const uint4 v = *(const uint4*)(dir + first); r.w[0] = v.x; r.w[1] = v.y; r.w[2] = v.z; r.w[3] = v.w; }
+    } else {
+#pragma unroll
+        for (int j = 0; j < ITEMS / 4; ++j) r.w[j] = 0xFFFFFFFFu;  // past the list: INACTIVE
+        for (uint32_t j = 0; first + j < n && j < (uint32_t)ITEMS; ++j) {
+            const uint32_t sh = 8u * (j & 3u);
+            r.w[j >> 2] = (r.w[j >> 2] & ~(0xFFu << sh)) | ((uint32_t)dir[first + j] << sh);
+        }
+    }
+}
+
+template <int ITEMS>
+__global__ void __launch_bounds__(kBlock, 4) k_grow_fill_sparse(int base) {
+    using S = GrowShape<ITEMS>;
+    constexpr uint32_t WS = 32u * ITEMS;  // slots of a warp's part of the tile
+    constexpr int B = 4;                  // ACTIVE slots per lane with loads in flight together
+    __shared__ uint32_t s_slot[kWarps][WS];
+    __shared__ uint8_t s_dir[kWarps][WS];
+    __shared__ uint32_t s_full[kWarps][ITEMS];  // full bits of a warp's slots
+    const DomainArgs& a = c_args[base];
+    if (!a.active) return;
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const uint32_t n0 = a.st->next_never[0], n1 = a.st->next_never[1];
+    const uint32_t t0 = (n0 + S::kTile - 1) / S::kTile, total = t0 + (n1 + S::kTile - 1) / S::kTile;
+    const bool dtc = a.dt_changed != 0;
+    uint32_t sv0 = 0, sv1 = 0;  // ACTIVE slots per list
+    uint32_t u = blockIdx.x;
+    SparseDir<ITEMS> cur;
+    if (u < total) sparse_dir<ITEMS>(a, u, t0, n0, n1, cur);
+    while (u < total) {
+        const uint32_t un = u + gridDim.x;
+        SparseDir<ITEMS> nxt;
+        if (un < total) sparse_dir<ITEMS>(a, un, t0, n0, n1, nxt);  // in flight during this tile's work
+        const int L = u >= t0 ? 1 : 0;
+        const DFront& fr = a.f[L];
+        const uint32_t n = L ? n1 : n0, tile = L ? u - t0 : u;
+        const uint32_t wfirst = tile * S::kTile + (uint32_t)warp * WS;  // the warp's first slot
+        const uint32_t first = tile * S::kTile + threadIdx.x * (uint32_t)ITEMS;  // the thread's
+        uint32_t act = 0;
+#pragma unroll
+        for (int j = 0; j < ITEMS; ++j)
+            if (((cur.w[j >> 2] >> (8 * (j & 3))) & 0xFFu) != kInactive) act |= 1u << j;
+        // the warp's ACTIVE slots into its shared list, in slot order
+        const uint32_t c = (uint32_t)__popc(act);
+        uint32_t x = c;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            const uint32_t y = __shfl_up_sync(0xFFFFFFFFu, x, o);
+            if (lane >= o) x += y;
+        }
+        const uint32_t wcnt = __shfl_sync(0xFFFFFFFFu, x, 31);
+        uint32_t pos = x - c;
+#pragma unroll
+        for (int j = 0; j < ITEMS; ++j)
+            if ((act >> j) & 1u) {
+                s_slot[warp][pos] = first + (uint32_t)j;
+                s_dir[warp][pos] = (uint8_t)((cur.w[j >> 2] >> (8 * (j & 3))) & 0xFFu);
+                ++pos;
+            }
+        if (lane < ITEMS) s_full[warp][lane] = 0u;
+        __syncwarp();
+        // the lanes take the warp's ACTIVE slots, B x 32 at a time, all their loads issued first
+        for (uint32_t i0 = 0; i0 < wcnt; i0 += 32u * B) {
+            uint32_t slot[B];
+            uint8_t d[B];
+            double w[B], fil[B];
+#pragma unroll
+            for (int b = 0; b < B; ++b) {
+                const uint32_t i = i0 + 32u * b + (uint32_t)lane;
+                d[b] = kInactive; slot[b] = 0; w[b] = -1.0; fil[b] = 0.0;
+                if (i < wcnt) {
+                    slot[b] = s_slot[warp][i];
+                    d[b] = s_dir[warp][i];
+                    w[b] = dtc ? ((const double*)fr.vel)[slot[b]] : fr.inc[slot[b]];
+                    fil[b] = ((const double*)fr.fill)[slot[b]];
+                }
+            }
+#pragma unroll
+            for (int b = 0; b < B; ++b) {
+                if (d[b] == kInactive) continue;
+                if (d[b] & kStale) {  // nuclei, cells answered by the host: no increment yet
+                    if (d[b] & kPend) {
+                        w[b] = answered_velocity(a, fr, slot[b], d[b], ((const unsigned long long*)fr.vel)[slot[b]]);
+                        ((double*)fr.vel)[slot[b]] = w[b];
+                    } else if (!dtc) {
+                        w[b] = ((const double*)fr.vel)[slot[b]];
+                    }
+                }
+                double inc = w[b];
+                if (dtc || (d[b] & kStale)) {
+                    if (__double_as_longlong(w[b]) >= 0) inc = __dmul_rn(__dmul_rn(w[b], a.dt), a.cinv);
+                    fr.inc[slot[b]] = inc;
+                    if (d[b] & kStale) fr.dir[slot[b]] = d[b] & kCodeMask;
+                }
+                if (__double_as_longlong(inc) >= 0) {  // sign bit clear: driving force present
+                    const double f = __dadd_rn(fil[b], inc);
+                    ((double*)fr.fill)[slot[b]] = f;
+                    if (__double_as_longlong(f) >= 0x3FF0000000000000ll) {  // f >= 1.0
+                        const uint32_t k = slot[b] - wfirst;
+                        atomicOr(&s_full[warp][k >> 5], 1u << (k & 31u));
+                    }
+                }
+            }
+        }
+        __syncwarp();
+        // the thread's full and INACTIVE bits into the masks: 32 / ITEMS threads share a mask word
+        const uint32_t kl = (uint32_t)lane * ITEMS;  // the thread's first slot within the warp's part
+        const uint32_t fb = (s_full[warp][kl >> 5] >> (kl & 31u)) & ((1u << ITEMS) - 1u);
+        uint32_t ib = ~act & ((1u << ITEMS) - 1u);
+        if (first + ITEMS > n) ib &= first >= n ? 0u : ((1u << (n - first)) - 1u);  // slots past the list are not INACTIVE
+        uint32_t fm = fb << (kl & 31u), im = ib << (kl & 31u);
+#pragma unroll
+        for (int o = 1; o < 32 / ITEMS; o <<= 1) {
+            fm |= __shfl_xor_sync(0xFFFFFFFFu, fm, o);
+            im |= __shfl_xor_sync(0xFFFFFFFFu, im, o);
+        }
+        if ((kl & 31u) == 0u) {
+            fr.fmask[first >> 5] = fm;  // slots 32 word .. 32 word + 31
+            fr.imask[first >> 5] = im;
+        }
+        uint32_t cf = (uint32_t)__popc(fb), ci = (uint32_t)__popc(ib);
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) {
+            cf += __shfl_xor_sync(0xFFFFFFFFu, cf, o);
+            ci += __shfl_xor_sync(0xFFFFFFFFu, ci, o);
+        }
+        if (lane == 0) {  // the warp's counts, and its share of the supertile's
+            const uint32_t wt = tile * kWarps + (uint32_t)warp;
+            fr.tcnt[2 * wt] = cf;
+            fr.tcnt[2 * wt + 1] = ci;
+            if (cf) atomicAdd(&fr.scnt[2 * (tile / kSuper)], cf);
+            if (ci) atomicAdd(&fr.scnt[2 * (tile / kSuper) + 1], ci);
+        }
+        if (L) sv1 += c;
+        else sv0 += c;
+        __syncwarp();  // the shared list is rewritten by the next tile
+        u = un;
+        if (u < total) cur = nxt;
+    }
+    flush_sv(a, 0, sv0);
+    flush_sv(a, 1, sv1);
+}
+
 // one warp per grow tile
 template <int ITEMS>
 __global__ void __launch_bounds__(kBlock) k_grow_lists(int base, int ndom) {
