@@ -239,7 +239,7 @@ typedef struct score_tune {
     int32_t spec_holes_pct;        /* k_grow_fill loads each slot's fill data together with its
                                       infector byte while the last step's INACTIVE share of the
                                       scanned slots was at most this percentage (0 never, 100
-                                      always; default 60); otherwise only for ACTIVE slots,
+                                      always; default 30); otherwise only for ACTIVE slots,
                                       after the byte */
     int32_t timing_every;          /* device phase events on every k-th step of a run (1 every
                                       step, 0 never; default 8): events cost device time */

@@ -522,7 +522,7 @@ struct TuneCfg {
     int fill_bpsm = 16;     // k_grow_fill blocks per SM
     int claim_bpsm = 2;     // k_claim blocks per SM (autotuner's choice on the 512^3 workload)
     int commit_bpsm = 8;    // k_resolve / k_commit blocks per SM (same)
-    int spec_pct = 60;      // every slot's data loaded with its infector byte up to this INACTIVE share [%]
+    int spec_pct = 30;      // every slot's data loaded with its infector byte up to this INACTIVE share [%]
     int timing_every = 8;   // phase events on every k-th step of a run (0 never): each event costs
                             // microseconds of device time, so the steps in between run without
     bool operator==(const TuneCfg& o) const {

@@ -62,7 +62,7 @@ def test_tune_values_are_checked(gpu, tmp_path):
             gm.set_tune(fill_blocks_per_sm=0)
         with pytest.raises(sg.ScoreError):
             gm.set_tune(spec_holes_pct=101)
-        assert gm.tune().spec_holes_pct == 60
+        assert gm.tune().spec_holes_pct == 30
         gm.set_tune(items=16, use_graph=0, spec_holes_pct=0)
         t = gm.tune()
         assert t.items == 16 and t.use_graph == 0 and t.spec_holes_pct == 0
