@@ -1330,8 +1330,8 @@ void launch_grow(const Engine& E, int n) {
         k_grow_fill_pf<ITEMS><<<g, kBlock, 0, E.stream>>>(E.base);
     } else if (n == 1 && !FP32 && E.fill_mode == 0) {
         k_grow_fill_pf0<ITEMS><<<g, kBlock, 0, E.stream>>>(E.base);
-    } else if (n == 1 && !FP32 && E.fill_mode == 4) {
-        k_grow_fill_sparse<ITEMS><<<g, kBlock, 0, E.stream>>>(E.base);
+    } else if (n == 1 && E.fill_mode == 4) {
+        k_grow_fill_sparse<FP32, ITEMS><<<g, kBlock, 0, E.stream>>>(E.base);
     } else if (n == 1) {
         switch (E.fill_mode) {
             case 0: case 4: k_grow_fill<FP32, ITEMS, true, 0><<<g, kBlock, 0, E.stream>>>(E.base, n); break;

@@ -861,8 +861,8 @@ __global__ void __launch_bounds__(kBlock, ITEMS >= 16 ? 2 : 3) k_grow_fill_pf0(i
     flush_sv(a, 1, sv1);
 }
 
-// The FP64 fill of a single domain in grow mode 0 while most of the list is holes (the last step's
-// INACTIVE share above spec_holes_pct).  A block takes a whole grow tile with one vector load of
+// The fill of a single domain (FP64, or FP32 + Kahan) in grow mode 0 while most of the list is holes
+// (the last step's INACTIVE share above spec_holes_pct).  A block takes a whole grow tile with one vector load of
 // infector bytes per thread (ITEMS consecutive slots each); each warp gathers its ACTIVE slots into a
 // shared list, and its lanes take them up to 4 x 32 at a time with all their increment and fill
 // loads in flight together, so that a memory round trip serves up to 128 ACTIVE slots instead of the
@@ -896,7 +896,7 @@ __device__ __forceinline__ void sparse_dir(const DomainArgs& a, uint32_t u, uint
     }
 }
 
-template <int ITEMS>
+template <bool FP32, int ITEMS>
 __global__ void __launch_bounds__(kBlock, 4) k_grow_fill_sparse(int base) {
     using S = GrowShape<ITEMS>;
     constexpr uint32_t WS = 32u * ITEMS;  // slots of a warp's part of the tile
@@ -950,42 +950,71 @@ __global__ void __launch_bounds__(kBlock, 4) k_grow_fill_sparse(int base) {
         for (uint32_t i0 = 0; i0 < wcnt; i0 += 32u * B) {
             uint32_t slot[B];
             uint8_t d[B];
-            double w[B], fil[B];
+            double w[B], fil[B];  // FP64: cached inc (or vel), fill; FP32: vel, fill
+            float cmp[B];         // FP32: Kahan compensation
 #pragma unroll
             for (int b = 0; b < B; ++b) {
                 const uint32_t i = i0 + 32u * b + (uint32_t)lane;
-                d[b] = kInactive; slot[b] = 0; w[b] = -1.0; fil[b] = 0.0;
+                d[b] = kInactive; slot[b] = 0; w[b] = -1.0; fil[b] = 0.0; cmp[b] = 0.0f;
                 if (i < wcnt) {
                     slot[b] = s_slot[warp][i];
                     d[b] = s_dir[warp][i];
-                    w[b] = dtc ? ((const double*)fr.vel)[slot[b]] : fr.inc[slot[b]];
-                    fil[b] = ((const double*)fr.fill)[slot[b]];
+                    if (!FP32) {
+                        w[b] = dtc ? ((const double*)fr.vel)[slot[b]] : fr.inc[slot[b]];
+                        fil[b] = ((const double*)fr.fill)[slot[b]];
+                    } else {
+                        w[b] = ((const float*)fr.vel)[slot[b]];
+                        fil[b] = ((const float*)fr.fill)[slot[b]];
+                        cmp[b] = fr.comp[slot[b]];
+                    }
                 }
             }
 #pragma unroll
             for (int b = 0; b < B; ++b) {
                 if (d[b] == kInactive) continue;
-                if (d[b] & kStale) {  // nuclei, cells answered by the host: no increment yet
-                    if (d[b] & kPend) {
-                        w[b] = answered_velocity(a, fr, slot[b], d[b], ((const unsigned long long*)fr.vel)[slot[b]]);
-                        ((double*)fr.vel)[slot[b]] = w[b];
-                    } else if (!dtc) {
-                        w[b] = ((const double*)fr.vel)[slot[b]];
+                bool full = false;
+                if (!FP32) {
+                    if (d[b] & kStale) {  // nuclei, cells answered by the host: no increment yet
+                        if (d[b] & kPend) {
+                            w[b] = answered_velocity(a, fr, slot[b], d[b], ((const unsigned long long*)fr.vel)[slot[b]]);
+                            ((double*)fr.vel)[slot[b]] = w[b];
+                        } else if (!dtc) {
+                            w[b] = ((const double*)fr.vel)[slot[b]];
+                        }
                     }
-                }
-                double inc = w[b];
-                if (dtc || (d[b] & kStale)) {
-                    if (__double_as_longlong(w[b]) >= 0) inc = __dmul_rn(__dmul_rn(w[b], a.dt), a.cinv);
-                    fr.inc[slot[b]] = inc;
+                    double inc = w[b];
+                    if (dtc || (d[b] & kStale)) {
+                        if (__double_as_longlong(w[b]) >= 0) inc = __dmul_rn(__dmul_rn(w[b], a.dt), a.cinv);
+                        fr.inc[slot[b]] = inc;
+                        if (d[b] & kStale) fr.dir[slot[b]] = d[b] & kCodeMask;
+                    }
+                    if (__double_as_longlong(inc) >= 0) {  // sign bit clear: driving force present
+                        const double f = __dadd_rn(fil[b], inc);
+                        ((double*)fr.fill)[slot[b]] = f;
+                        full = __double_as_longlong(f) >= 0x3FF0000000000000ll;  // f >= 1.0
+                    }
+                } else {
+                    float vel = (float)w[b];
+                    if (d[b] & kPend) {  // P from the host
+                        vel = (float)answered_velocity(a, fr, slot[b], d[b], ((const uint32_t*)fr.vel)[slot[b]]);
+                        ((float*)fr.vel)[slot[b]] = vel;
+                    }
                     if (d[b] & kStale) fr.dir[slot[b]] = d[b] & kCodeMask;
-                }
-                if (__double_as_longlong(inc) >= 0) {  // sign bit clear: driving force present
-                    const double f = __dadd_rn(fil[b], inc);
-                    ((double*)fr.fill)[slot[b]] = f;
-                    if (__double_as_longlong(f) >= 0x3FF0000000000000ll) {  // f >= 1.0
-                        const uint32_t k = slot[b] - wfirst;
-                        atomicOr(&s_full[warp][k >> 5], 1u << (k & 31u));
+                    if (vel >= 0.0f) {
+                        // Kahan-compensated accumulation of the fill
+                        const float fl = (float)fil[b];
+                        const float inc = vel * a.dtc32;
+                        const float y = inc - cmp[b];
+                        const float t = fl + y;
+                        const float c = (t - fl) - y;
+                        ((float*)fr.fill)[slot[b]] = t;
+                        fr.comp[slot[b]] = c;
+                        full = (t - c) >= 1.0f;
                     }
+                }
+                if (full) {
+                    const uint32_t k = slot[b] - wfirst;
+                    atomicOr(&s_full[warp][k >> 5], 1u << (k & 31u));
                 }
             }
         }
