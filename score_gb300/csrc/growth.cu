@@ -1330,7 +1330,8 @@ void launch_grow(const Engine& E, int n) {
         k_grow_fill_pf<ITEMS><<<g, kBlock, 0, E.stream>>>(E.base);
     } else if (n == 1 && !FP32 && E.fill_mode == 0) {
         k_grow_fill_pf0<ITEMS><<<g, kBlock, 0, E.stream>>>(E.base);
-    } else if (n == 1 && E.fill_mode == 4) {
+    } else if (n == 1 && (E.fill_mode == 4 || (FP32 && E.fill_mode == 3))) {
+        // FP32 keeps no increment (its fill step is vel dt / cellsize), so grow mode 3 is mode 0 there
         k_grow_fill_sparse<FP32, ITEMS><<<g, kBlock, 0, E.stream>>>(E.base);
     } else if (n == 1) {
         switch (E.fill_mode) {
