@@ -626,6 +626,26 @@ __device__ __forceinline__ void flush_sv(const DomainArgs& a, int L, uint32_t sv
     if ((threadIdx.x & 31) == 0 && sv) atomicAdd(&a.st->sv[L], (unsigned long long)sv);
 }
 
+// a single domain's Sv shares of the whole block into its counters: one atomic per list and block
+// (a per-warp atomic on the same two words from every block of a launch serialises at the end)
+__device__ __forceinline__ void flush_sv_block(const DomainArgs& a, uint32_t sv0, uint32_t sv1) {
+    __shared__ uint32_t s_sv[2][kWarps];
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+        sv0 += __shfl_xor_sync(0xFFFFFFFFu, sv0, o);
+        sv1 += __shfl_xor_sync(0xFFFFFFFFu, sv1, o);
+    }
+    if ((threadIdx.x & 31) == 0) { s_sv[0][threadIdx.x >> 5] = sv0; s_sv[1][threadIdx.x >> 5] = sv1; }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        uint32_t t0 = 0, t1 = 0;
+#pragma unroll
+        for (int w = 0; w < kWarps; ++w) { t0 += s_sv[0][w]; t1 += s_sv[1][w]; }
+        if (t0) atomicAdd(&a.st->sv[0], (unsigned long long)t0);
+        if (t1) atomicAdd(&a.st->sv[1], (unsigned long long)t1);
+    }
+}
+
 // slots of list L of a domain this step ( 0 for a domain that is not stepping)
 __device__ __forceinline__ uint32_t list_slots(const DomainArgs& a, int L) { return a.active ? a.st->next_never[L] : 0u; }
 
@@ -654,14 +674,14 @@ __global__ void __launch_bounds__(kBlock, ITEMS >= 16 ? 2 : 4) k_grow_fill(int b
     if (ONE) {
         const DomainArgs& a = c_args[base];
         if (!a.active) return;
-#pragma unroll 1
+        uint32_t sv[2] = {0, 0};
+#pragma unroll
         for (int L = 0; L < 2; ++L) {
             const uint32_t n = a.st->next_never[L];
             const uint32_t ntiles = (n + S::kTile - 1) / S::kTile;
-            uint32_t sv = 0;
-            for (uint32_t tile = blockIdx.x; tile < ntiles; tile += gridDim.x) sv += grow_tile_mode<FP32, ITEMS, MODE>(a, L, tile, n);
-            flush_sv(a, L, sv);
+            for (uint32_t tile = blockIdx.x; tile < ntiles; tile += gridDim.x) sv[L] += grow_tile_mode<FP32, ITEMS, MODE>(a, L, tile, n);
         }
+        flush_sv_block(a, sv[0], sv[1]);
         return;
     }
     const int nseg = 2 * ndom;
@@ -766,8 +786,7 @@ __global__ void __launch_bounds__(kBlock, ITEMS >= 8 ? 2 : 3) k_grow_fill_pf(int
         u = un;
         if (u < total) cur = nxt;
     }
-    flush_sv(a, 0, sv0);
-    flush_sv(a, 1, sv1);
+    flush_sv_block(a, sv0, sv1);
 }
 
 // The FP64 fill of a single domain in grow mode 0 (the cached increment, or vel when dt changed;
@@ -857,8 +876,7 @@ __global__ void __launch_bounds__(kBlock, ITEMS >= 16 ? 2 : 3) k_grow_fill_pf0(i
             for (int k = 0; k < ITEMS; ++k) d[k] = dn[k];
         }
     }
-    flush_sv(a, 0, sv0);
-    flush_sv(a, 1, sv1);
+    flush_sv_block(a, sv0, sv1);
 }
 
 // The fill of a single domain (FP64, or FP32 + Kahan) in grow mode 0 while most of the list is holes
@@ -1053,8 +1071,7 @@ __global__ void __launch_bounds__(kBlock, 4) k_grow_fill_sparse(int base) {
         u = un;
         if (u < total) cur = nxt;
     }
-    flush_sv(a, 0, sv0);
-    flush_sv(a, 1, sv1);
+    flush_sv_block(a, sv0, sv1);
 }
 
 // one warp per grow tile
