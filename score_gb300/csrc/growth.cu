@@ -650,11 +650,12 @@ struct Engine {
     bool events = false;               // the sequence being launched records the phase events
     int fill_mode = kFillAny;          // ... and the grow mode of every stepping domain (kFillAny: per domain)
     // the step without / with phase events, with the general / the refresh-only grow kernel
-    // the step graphs: with or without phase events, times the fill mode (0..4 or per domain)
-    static constexpr int kGraphs = 12;
+    // the step graphs: with or without phase events, times the fill mode (0..4, 5 for a batch of
+    // cached increments, or per domain)
+    static constexpr int kGraphs = 14;
     cudaGraphExec_t gexec[kGraphs] = {};
     TuneCfg gcfg[kGraphs];
-    int gndom[kGraphs] = {-1, -1, -1, -1, -1, -1, -1, -1, -1, -1, -1, -1};
+    int gndom[kGraphs] = {-1, -1, -1, -1, -1, -1, -1, -1, -1, -1, -1, -1, -1, -1};
     bool gfp32[kGraphs] = {};
     uint64_t run_steps = 0;            // steps since the run started (phase sampling)
     // 0 start, 1 end of fill, 2 end of lists, 3 end of claim, 4 end of step, 5/6 run span
@@ -1341,6 +1342,8 @@ void launch_grow(const Engine& E, int n) {
             case 3: k_grow_fill<FP32, ITEMS, true, 3><<<g, kBlock, 0, E.stream>>>(E.base, n); break;
             default: k_grow_fill<FP32, ITEMS, true, kFillAny><<<g, kBlock, 0, E.stream>>>(E.base, n); break;
         }
+    } else if (E.fill_mode == 5) {  // a batch whose domains all step from cached increments
+        k_grow_fill_sparse_batch<FP32, ITEMS><<<g, kBlock, 0, E.stream>>>(E.base, n);
     } else if (E.fill_mode == 2) {
         k_grow_fill<FP32, ITEMS, false, 2><<<g, kBlock, 0, E.stream>>>(E.base, n);
     } else {
@@ -1402,7 +1405,7 @@ cudaError_t Engine::enqueue_step(int n, bool timed, int mode) {
         launches += step_kernels(n);
         return cudaGetLastError();
     }
-    const int k = (timed ? 1 : 0) + 2 * (mode == kFillAny ? 5 : mode);
+    const int k = (timed ? 1 : 0) + 2 * (mode == kFillAny ? 6 : mode);
     if (!gexec[k] || gndom[k] != n || !(gcfg[k] == cfg) || gfp32[k] != fp32) {
         if (gexec[k]) cudaGraphExecDestroy(gexec[k]);
         gexec[k] = nullptr;
@@ -1528,7 +1531,14 @@ int Engine::step(bool timed) {
         const int m = a.refresh == 2 ? 2 : a.refresh == 1 ? 1 : !a.spec ? 4 : !a.dt_changed ? 3 : 0;
         mode = (mode == -2 || mode == m) ? m : kFillAny;
     }
-    if (n > 1 && mode != 2) mode = kFillAny;  // batches: the refresh-only kernel, or the per-domain one
+    // batches: the gathered-slot kernel when no domain refreshes, the refresh-only kernel when all
+    // refresh from cached mobilities, else the per-domain one
+    if (n > 1 && mode != 2) {
+        bool cached = true;
+        for (int i = 0; i < n; ++i)
+            if (dom[i]->running && h_args[i].refresh != 0) cached = false;
+        mode = cached ? 5 : kFillAny;
+    }
     cudaError_t e = enqueue_step(n, timed, mode);
     ++run_steps;
     // while the GPU steps: each domain's outcome-independent physics for the next step

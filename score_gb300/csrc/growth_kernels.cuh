@@ -893,12 +893,11 @@ struct SparseDir {  // a thread's ITEMS infector bytes
     uint32_t w[ITEMS / 4];
 };
 
+// the thread's ITEMS infector bytes of grow tile `tile` of list L (n slots)
 template <int ITEMS>
-__device__ __forceinline__ void sparse_dir(const DomainArgs& a, uint32_t u, uint32_t t0, uint32_t n0, uint32_t n1, SparseDir<ITEMS>& r) {
+__device__ __forceinline__ void sparse_dir(const DomainArgs& a, int L, uint32_t tile, uint32_t n, SparseDir<ITEMS>& r) {
     using S = GrowShape<ITEMS>;
-    const int L = u >= t0 ? 1 : 0;
-    const uint32_t n = L ? n1 : n0;
-    const uint32_t first = (L ? u - t0 : u) * S::kTile + threadIdx.x * (uint32_t)ITEMS;
+    const uint32_t first = tile * S::kTile + threadIdx.x * (uint32_t)ITEMS;
     const uint8_t* dir = a.f[L].dir;
     if (first + ITEMS <= n) {  // ITEMS bytes at an ITEMS-aligned slot: one vector load
         if (ITEMS == 4) r.w[0] = *(const uint32_t*)(dir + first);
@@ -914,164 +913,225 @@ __device__ __forceinline__ void sparse_dir(const DomainArgs& a, uint32_t u, uint
     }
 }
 
+template <int ITEMS>
+struct SparseShared {  // a block's shared lists: per warp its ACTIVE slots, their infector bytes, full bits
+    uint32_t slot[kWarps][32 * ITEMS];
+    uint8_t dir[kWarps][32 * ITEMS];
+    uint32_t full[kWarps][ITEMS];
+};
+
+// One grow tile of list L (n slots) by the whole block, the thread's infector bytes in `cur`:
+// returns the thread's ACTIVE slots.  Warps run apart (no block barrier).
 template <bool FP32, int ITEMS>
-__global__ void __launch_bounds__(kBlock, 4) k_grow_fill_sparse(int base) {
+__device__ __forceinline__ uint32_t sparse_tile(const DomainArgs& a, int L, uint32_t tile, uint32_t n, const SparseDir<ITEMS>& cur,
+                                                SparseShared<ITEMS>& sh) {
     using S = GrowShape<ITEMS>;
     constexpr uint32_t WS = 32u * ITEMS;  // slots of a warp's part of the tile
     constexpr int B = 4;                  // ACTIVE slots per lane with loads in flight together
-    __shared__ uint32_t s_slot[kWarps][WS];
-    __shared__ uint8_t s_dir[kWarps][WS];
-    __shared__ uint32_t s_full[kWarps][ITEMS];  // full bits of a warp's slots
+    uint32_t (&s_slot)[kWarps][WS] = sh.slot;
+    uint8_t (&s_dir)[kWarps][WS] = sh.dir;
+    uint32_t (&s_full)[kWarps][ITEMS] = sh.full;
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const DFront& fr = a.f[L];
+    const bool dtc = a.dt_changed != 0;
+    const uint32_t wfirst = tile * S::kTile + (uint32_t)warp * WS;  // the warp's first slot
+    const uint32_t first = tile * S::kTile + threadIdx.x * (uint32_t)ITEMS;  // the thread's
+    uint32_t act = 0;
+#pragma unroll
+    for (int j = 0; j < ITEMS; ++j)
+        if (((cur.w[j >> 2] >> (8 * (j & 3))) & 0xFFu) != kInactive) act |= 1u << j;
+    // the warp's ACTIVE slots into its shared list, in slot order
+    const uint32_t c = (uint32_t)__popc(act);
+    uint32_t x = c;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        const uint32_t y = __shfl_up_sync(0xFFFFFFFFu, x, o);
+        if (lane >= o) x += y;
+    }
+    const uint32_t wcnt = __shfl_sync(0xFFFFFFFFu, x, 31);
+    uint32_t pos = x - c;
+#pragma unroll
+    for (int j = 0; j < ITEMS; ++j)
+        if ((act >> j) & 1u) {
+            s_slot[warp][pos] = first + (uint32_t)j;
+            s_dir[warp][pos] = (uint8_t)((cur.w[j >> 2] >> (8 * (j & 3))) & 0xFFu);
+            ++pos;
+        }
+    if (lane < ITEMS) s_full[warp][lane] = 0u;
+    __syncwarp();
+    // the lanes take the warp's ACTIVE slots, B x 32 at a time, all their loads issued first
+    for (uint32_t i0 = 0; i0 < wcnt; i0 += 32u * B) {
+        uint32_t slot[B];
+        uint8_t d[B];
+        double w[B], fil[B];  // FP64: cached inc (or vel), fill; FP32: vel, fill
+        float cmp[B];         // FP32: Kahan compensation
+#pragma unroll
+        for (int b = 0; b < B; ++b) {
+            const uint32_t i = i0 + 32u * b + (uint32_t)lane;
+            d[b] = kInactive; slot[b] = 0; w[b] = -1.0; fil[b] = 0.0; cmp[b] = 0.0f;
+            if (i < wcnt) {
+                slot[b] = s_slot[warp][i];
+                d[b] = s_dir[warp][i];
+                if (!FP32) {
+                    w[b] = dtc ? ((const double*)fr.vel)[slot[b]] : fr.inc[slot[b]];
+                    fil[b] = ((const double*)fr.fill)[slot[b]];
+                } else {
+                    w[b] = ((const float*)fr.vel)[slot[b]];
+                    fil[b] = ((const float*)fr.fill)[slot[b]];
+                    cmp[b] = fr.comp[slot[b]];
+                }
+            }
+        }
+#pragma unroll
+        for (int b = 0; b < B; ++b) {
+            if (d[b] == kInactive) continue;
+            bool full = false;
+            if (!FP32) {
+                if (d[b] & kStale) {  // nuclei, cells answered by the host: no increment yet
+                    if (d[b] & kPend) {
+                        w[b] = answered_velocity(a, fr, slot[b], d[b], ((const unsigned long long*)fr.vel)[slot[b]]);
+                        ((double*)fr.vel)[slot[b]] = w[b];
+                    } else if (!dtc) {
+                        w[b] = ((const double*)fr.vel)[slot[b]];
+                    }
+                }
+                double inc = w[b];
+                if (dtc || (d[b] & kStale)) {
+                    if (__double_as_longlong(w[b]) >= 0) inc = __dmul_rn(__dmul_rn(w[b], a.dt), a.cinv);
+                    fr.inc[slot[b]] = inc;
+                    if (d[b] & kStale) fr.dir[slot[b]] = d[b] & kCodeMask;
+                }
+                if (__double_as_longlong(inc) >= 0) {  // sign bit clear: driving force present
+                    const double f = __dadd_rn(fil[b], inc);
+                    ((double*)fr.fill)[slot[b]] = f;
+                    full = __double_as_longlong(f) >= 0x3FF0000000000000ll;  // f >= 1.0
+                }
+            } else {
+                float vel = (float)w[b];
+                if (d[b] & kPend) {  // P from the host
+                    vel = (float)answered_velocity(a, fr, slot[b], d[b], ((const uint32_t*)fr.vel)[slot[b]]);
+                    ((float*)fr.vel)[slot[b]] = vel;
+                }
+                if (d[b] & kStale) fr.dir[slot[b]] = d[b] & kCodeMask;
+                if (vel >= 0.0f) {
+                    // Kahan-compensated accumulation of the fill
+                    const float fl = (float)fil[b];
+                    const float inc = vel * a.dtc32;
+                    const float y = inc - cmp[b];
+                    const float t = fl + y;
+                    const float c = (t - fl) - y;
+                    ((float*)fr.fill)[slot[b]] = t;
+                    fr.comp[slot[b]] = c;
+                    full = (t - c) >= 1.0f;
+                }
+            }
+            if (full) {
+                const uint32_t k = slot[b] - wfirst;
+                atomicOr(&s_full[warp][k >> 5], 1u << (k & 31u));
+            }
+        }
+    }
+    __syncwarp();
+    // the thread's full and INACTIVE bits into the masks: 32 / ITEMS threads share a mask word
+    const uint32_t kl = (uint32_t)lane * ITEMS;  // the thread's first slot within the warp's part
+    const uint32_t fb = (s_full[warp][kl >> 5] >> (kl & 31u)) & ((1u << ITEMS) - 1u);
+    uint32_t ib = ~act & ((1u << ITEMS) - 1u);
+    if (first + ITEMS > n) ib &= first >= n ? 0u : ((1u << (n - first)) - 1u);  // slots past the list are not INACTIVE
+    uint32_t fm = fb << (kl & 31u), im = ib << (kl & 31u);
+#pragma unroll
+    for (int o = 1; o < 32 / ITEMS; o <<= 1) {
+        fm |= __shfl_xor_sync(0xFFFFFFFFu, fm, o);
+        im |= __shfl_xor_sync(0xFFFFFFFFu, im, o);
+    }
+    if ((kl & 31u) == 0u) {
+        fr.fmask[first >> 5] = fm;  // slots 32 word .. 32 word + 31
+        fr.imask[first >> 5] = im;
+    }
+    uint32_t cf = (uint32_t)__popc(fb), ci = (uint32_t)__popc(ib);
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+        cf += __shfl_xor_sync(0xFFFFFFFFu, cf, o);
+        ci += __shfl_xor_sync(0xFFFFFFFFu, ci, o);
+    }
+    if (lane == 0) {  // the warp's counts, and its share of the supertile's
+        const uint32_t wt = tile * kWarps + (uint32_t)warp;
+        fr.tcnt[2 * wt] = cf;
+        fr.tcnt[2 * wt + 1] = ci;
+        if (cf) atomicAdd(&fr.scnt[2 * (tile / kSuper)], cf);
+        if (ci) atomicAdd(&fr.scnt[2 * (tile / kSuper) + 1], ci);
+    }
+    __syncwarp();  // the shared list is rewritten by the next tile
+    return c;
+}
+
+template <bool FP32, int ITEMS>
+__global__ void __launch_bounds__(kBlock, 4) k_grow_fill_sparse(int base) {
+    using S = GrowShape<ITEMS>;
+    __shared__ SparseShared<ITEMS> sh;
     const DomainArgs& a = c_args[base];
     if (!a.active) return;
-    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const uint32_t n0 = a.st->next_never[0], n1 = a.st->next_never[1];
     const uint32_t t0 = (n0 + S::kTile - 1) / S::kTile, total = t0 + (n1 + S::kTile - 1) / S::kTile;
-    const bool dtc = a.dt_changed != 0;
     uint32_t sv0 = 0, sv1 = 0;  // ACTIVE slots per list
     uint32_t u = blockIdx.x;
     SparseDir<ITEMS> cur;
-    if (u < total) sparse_dir<ITEMS>(a, u, t0, n0, n1, cur);
+    if (u < total) sparse_dir<ITEMS>(a, u >= t0 ? 1 : 0, u >= t0 ? u - t0 : u, u >= t0 ? n1 : n0, cur);
     while (u < total) {
         const uint32_t un = u + gridDim.x;
         SparseDir<ITEMS> nxt;
-        if (un < total) sparse_dir<ITEMS>(a, un, t0, n0, n1, nxt);  // in flight during this tile's work
+        if (un < total) sparse_dir<ITEMS>(a, un >= t0 ? 1 : 0, un >= t0 ? un - t0 : un, un >= t0 ? n1 : n0, nxt);  // in flight meanwhile
         const int L = u >= t0 ? 1 : 0;
-        const DFront& fr = a.f[L];
-        const uint32_t n = L ? n1 : n0, tile = L ? u - t0 : u;
-        const uint32_t wfirst = tile * S::kTile + (uint32_t)warp * WS;  // the warp's first slot
-        const uint32_t first = tile * S::kTile + threadIdx.x * (uint32_t)ITEMS;  // the thread's
-        uint32_t act = 0;
-#pragma unroll
-        for (int j = 0; j < ITEMS; ++j)
-            if (((cur.w[j >> 2] >> (8 * (j & 3))) & 0xFFu) != kInactive) act |= 1u << j;
-        // the warp's ACTIVE slots into its shared list, in slot order
-        const uint32_t c = (uint32_t)__popc(act);
-        uint32_t x = c;
-#pragma unroll
-        for (int o = 1; o < 32; o <<= 1) {
-            const uint32_t y = __shfl_up_sync(0xFFFFFFFFu, x, o);
-            if (lane >= o) x += y;
-        }
-        const uint32_t wcnt = __shfl_sync(0xFFFFFFFFu, x, 31);
-        uint32_t pos = x - c;
-#pragma unroll
-        for (int j = 0; j < ITEMS; ++j)
-            if ((act >> j) & 1u) {
-                s_slot[warp][pos] = first + (uint32_t)j;
-                s_dir[warp][pos] = (uint8_t)((cur.w[j >> 2] >> (8 * (j & 3))) & 0xFFu);
-                ++pos;
-            }
-        if (lane < ITEMS) s_full[warp][lane] = 0u;
-        __syncwarp();
-        // the lanes take the warp's ACTIVE slots, B x 32 at a time, all their loads issued first
-        for (uint32_t i0 = 0; i0 < wcnt; i0 += 32u * B) {
-            uint32_t slot[B];
-            uint8_t d[B];
-            double w[B], fil[B];  // FP64: cached inc (or vel), fill; FP32: vel, fill
-            float cmp[B];         // FP32: Kahan compensation
-#pragma unroll
-            for (int b = 0; b < B; ++b) {
-                const uint32_t i = i0 + 32u * b + (uint32_t)lane;
-                d[b] = kInactive; slot[b] = 0; w[b] = -1.0; fil[b] = 0.0; cmp[b] = 0.0f;
-                if (i < wcnt) {
-                    slot[b] = s_slot[warp][i];
-                    d[b] = s_dir[warp][i];
-                    if (!FP32) {
-                        w[b] = dtc ? ((const double*)fr.vel)[slot[b]] : fr.inc[slot[b]];
-                        fil[b] = ((const double*)fr.fill)[slot[b]];
-                    } else {
-                        w[b] = ((const float*)fr.vel)[slot[b]];
-                        fil[b] = ((const float*)fr.fill)[slot[b]];
-                        cmp[b] = fr.comp[slot[b]];
-                    }
-                }
-            }
-#pragma unroll
-            for (int b = 0; b < B; ++b) {
-                if (d[b] == kInactive) continue;
-                bool full = false;
-                if (!FP32) {
-                    if (d[b] & kStale) {  // nuclei, cells answered by the host: no increment yet
-                        if (d[b] & kPend) {
-                            w[b] = answered_velocity(a, fr, slot[b], d[b], ((const unsigned long long*)fr.vel)[slot[b]]);
-                            ((double*)fr.vel)[slot[b]] = w[b];
-                        } else if (!dtc) {
-                            w[b] = ((const double*)fr.vel)[slot[b]];
-                        }
-                    }
-                    double inc = w[b];
-                    if (dtc || (d[b] & kStale)) {
-                        if (__double_as_longlong(w[b]) >= 0) inc = __dmul_rn(__dmul_rn(w[b], a.dt), a.cinv);
-                        fr.inc[slot[b]] = inc;
-                        if (d[b] & kStale) fr.dir[slot[b]] = d[b] & kCodeMask;
-                    }
-                    if (__double_as_longlong(inc) >= 0) {  // sign bit clear: driving force present
-                        const double f = __dadd_rn(fil[b], inc);
-                        ((double*)fr.fill)[slot[b]] = f;
-                        full = __double_as_longlong(f) >= 0x3FF0000000000000ll;  // f >= 1.0
-                    }
-                } else {
-                    float vel = (float)w[b];
-                    if (d[b] & kPend) {  // P from the host
-                        vel = (float)answered_velocity(a, fr, slot[b], d[b], ((const uint32_t*)fr.vel)[slot[b]]);
-                        ((float*)fr.vel)[slot[b]] = vel;
-                    }
-                    if (d[b] & kStale) fr.dir[slot[b]] = d[b] & kCodeMask;
-                    if (vel >= 0.0f) {
-                        // Kahan-compensated accumulation of the fill
-                        const float fl = (float)fil[b];
-                        const float inc = vel * a.dtc32;
-                        const float y = inc - cmp[b];
-                        const float t = fl + y;
-                        const float c = (t - fl) - y;
-                        ((float*)fr.fill)[slot[b]] = t;
-                        fr.comp[slot[b]] = c;
-                        full = (t - c) >= 1.0f;
-                    }
-                }
-                if (full) {
-                    const uint32_t k = slot[b] - wfirst;
-                    atomicOr(&s_full[warp][k >> 5], 1u << (k & 31u));
-                }
-            }
-        }
-        __syncwarp();
-        // the thread's full and INACTIVE bits into the masks: 32 / ITEMS threads share a mask word
-        const uint32_t kl = (uint32_t)lane * ITEMS;  // the thread's first slot within the warp's part
-        const uint32_t fb = (s_full[warp][kl >> 5] >> (kl & 31u)) & ((1u << ITEMS) - 1u);
-        uint32_t ib = ~act & ((1u << ITEMS) - 1u);
-        if (first + ITEMS > n) ib &= first >= n ? 0u : ((1u << (n - first)) - 1u);  // slots past the list are not INACTIVE
-        uint32_t fm = fb << (kl & 31u), im = ib << (kl & 31u);
-#pragma unroll
-        for (int o = 1; o < 32 / ITEMS; o <<= 1) {
-            fm |= __shfl_xor_sync(0xFFFFFFFFu, fm, o);
-            im |= __shfl_xor_sync(0xFFFFFFFFu, im, o);
-        }
-        if ((kl & 31u) == 0u) {
-            fr.fmask[first >> 5] = fm;  // slots 32 word .. 32 word + 31
-            fr.imask[first >> 5] = im;
-        }
-        uint32_t cf = (uint32_t)__popc(fb), ci = (uint32_t)__popc(ib);
-#pragma unroll
-        for (int o = 16; o > 0; o >>= 1) {
-            cf += __shfl_xor_sync(0xFFFFFFFFu, cf, o);
-            ci += __shfl_xor_sync(0xFFFFFFFFu, ci, o);
-        }
-        if (lane == 0) {  // the warp's counts, and its share of the supertile's
-            const uint32_t wt = tile * kWarps + (uint32_t)warp;
-            fr.tcnt[2 * wt] = cf;
-            fr.tcnt[2 * wt + 1] = ci;
-            if (cf) atomicAdd(&fr.scnt[2 * (tile / kSuper)], cf);
-            if (ci) atomicAdd(&fr.scnt[2 * (tile / kSuper) + 1], ci);
-        }
+        const uint32_t c = sparse_tile<FP32, ITEMS>(a, L, L ? u - t0 : u, L ? n1 : n0, cur, sh);
         if (L) sv1 += c;
         else sv0 += c;
-        __syncwarp();  // the shared list is rewritten by the next tile
         u = un;
         if (u < total) cur = nxt;
     }
     flush_sv_block(a, sv0, sv1);
+}
+
+// The same for a batch whose domains all step from cached increments (no refresh this step): the
+// grow tiles of every (domain, list) form one sequence, mapped to their segment by binary search.
+template <bool FP32, int ITEMS>
+__global__ void __launch_bounds__(kBlock, 4) k_grow_fill_sparse_batch(int base, int ndom) {
+    using S = GrowShape<ITEMS>;
+    __shared__ SparseShared<ITEMS> sh;
+    __shared__ uint32_t s_pre[kMaxSegs + 1];
+    const int nseg = 2 * ndom;
+    const uint32_t total = seg_prefix(s_pre, nseg, [&](int s) {
+        return (list_slots(c_args[base + (s >> 1)], s & 1) + S::kTile - 1) / S::kTile;
+    });
+    auto locate = [&](uint32_t v, int& s, uint32_t& tile) { s = seg_find(s_pre, nseg, v); tile = v - s_pre[s]; };
+    int cur_seg = -1;   // segment whose Sv share is being accumulated
+    uint32_t sv = 0;
+    uint32_t u = blockIdx.x;
+    SparseDir<ITEMS> cur;
+    if (u < total) {
+        int s; uint32_t t;
+        locate(u, s, t);
+        sparse_dir<ITEMS>(c_args[base + (s >> 1)], s & 1, t, c_args[base + (s >> 1)].st->next_never[s & 1], cur);
+    }
+    while (u < total) {
+        const uint32_t un = u + gridDim.x;
+        SparseDir<ITEMS> nxt;
+        if (un < total) {
+            int s; uint32_t t;
+            locate(un, s, t);
+            sparse_dir<ITEMS>(c_args[base + (s >> 1)], s & 1, t, c_args[base + (s >> 1)].st->next_never[s & 1], nxt);
+        }
+        int s; uint32_t tile;
+        locate(u, s, tile);
+        if (s != cur_seg) {
+            if (cur_seg >= 0) flush_sv(c_args[base + (cur_seg >> 1)], cur_seg & 1, sv);
+            cur_seg = s;
+            sv = 0;
+        }
+        const DomainArgs& a = c_args[base + (s >> 1)];
+        sv += sparse_tile<FP32, ITEMS>(a, s & 1, tile, a.st->next_never[s & 1], cur, sh);
+        u = un;
+        if (u < total) cur = nxt;
+    }
+    if (cur_seg >= 0) flush_sv(c_args[base + (cur_seg >> 1)], cur_seg & 1, sv);
 }
 
 // one warp per grow tile
