@@ -82,6 +82,9 @@ def run_single(p, d, **tune):
     dict(items=4, fill_blocks_per_sm=4, claim_blocks_per_sm=2, commit_blocks_per_sm=16, use_graph=0, spec_holes_pct=0),
     dict(items=16, fill_blocks_per_sm=32, claim_blocks_per_sm=16, commit_blocks_per_sm=2, use_graph=1, spec_holes_pct=100),
     dict(items=8, fill_blocks_per_sm=1, claim_blocks_per_sm=1, commit_blocks_per_sm=1, use_graph=1, spec_holes_pct=100),
+    # the gathered-slot fill on every step, at 8 and 16 items
+    dict(items=8, fill_blocks_per_sm=16, claim_blocks_per_sm=2, commit_blocks_per_sm=8, use_graph=1, spec_holes_pct=0),
+    dict(items=16, fill_blocks_per_sm=8, claim_blocks_per_sm=4, commit_blocks_per_sm=4, use_graph=0, spec_holes_pct=0),
 ])
 def test_launch_configuration_does_not_change_results(gpu, tmp_path, tune):
     p, d, g = load_case("texture_bimodal", tmp_path)
