@@ -1327,24 +1327,27 @@ inline void record(const Engine& E, int k) {
 template <bool FP32, int ITEMS>
 void launch_grow(const Engine& E, int n) {
     const uint32_t g = (uint32_t)(E.sms * E.cfg.fill_bpsm);
-    if (n == 1 && !FP32 && E.fill_mode == 3 && ITEMS <= 8) {  // 16 items spill in the pipelined kernel
-        k_grow_fill_pf<ITEMS><<<g, kBlock, 0, E.stream>>>(E.base);
-    } else if (n == 1 && !FP32 && E.fill_mode == 0) {
-        k_grow_fill_pf0<ITEMS><<<g, kBlock, 0, E.stream>>>(E.base);
-    } else if (n == 1 && (E.fill_mode == 4 || (FP32 && E.fill_mode == 3))) {
-        // FP32 keeps no increment (its fill step is vel dt / cellsize), so grow mode 3 is mode 0 there
-        k_grow_fill_sparse<FP32, ITEMS><<<g, kBlock, 0, E.stream>>>(E.base);
-    } else if (n == 1) {
-        switch (E.fill_mode) {
-            case 0: case 4: k_grow_fill<FP32, ITEMS, true, 0><<<g, kBlock, 0, E.stream>>>(E.base, n); break;
-            case 1: k_grow_fill<FP32, ITEMS, true, 1><<<g, kBlock, 0, E.stream>>>(E.base, n); break;
-            case 2: k_grow_fill<FP32, ITEMS, true, 2><<<g, kBlock, 0, E.stream>>>(E.base, n); break;
-            case 3: k_grow_fill<FP32, ITEMS, true, 3><<<g, kBlock, 0, E.stream>>>(E.base, n); break;
-            default: k_grow_fill<FP32, ITEMS, true, kFillAny><<<g, kBlock, 0, E.stream>>>(E.base, n); break;
+    const int m = E.fill_mode;  // a single domain's is one of 0..4
+    if (n == 1) {
+        if (m == 4 || (FP32 && m == 3)) {
+            // FP32 keeps no increment (its fill step is vel dt / cellsize), so grow mode 3 is mode 0 there
+            k_grow_fill_sparse<FP32, ITEMS><<<g, kBlock, 0, E.stream>>>(E.base);
+        } else if (m == 1) {
+            k_grow_fill<FP32, ITEMS, true, 1><<<g, kBlock, 0, E.stream>>>(E.base, n);
+        } else if (m == 2) {
+            k_grow_fill<FP32, ITEMS, true, 2><<<g, kBlock, 0, E.stream>>>(E.base, n);
+        } else if constexpr (FP32) {
+            k_grow_fill<true, ITEMS, true, 0><<<g, kBlock, 0, E.stream>>>(E.base, n);
+        } else if (m == 0) {
+            k_grow_fill_pf0<ITEMS><<<g, kBlock, 0, E.stream>>>(E.base);
+        } else if constexpr (ITEMS <= 8) {
+            k_grow_fill_pf<ITEMS><<<g, kBlock, 0, E.stream>>>(E.base);
+        } else {
+            k_grow_fill<false, ITEMS, true, 3><<<g, kBlock, 0, E.stream>>>(E.base, n);  // 16 items spill in the pipelined kernel
         }
-    } else if (E.fill_mode == 5) {  // a batch whose domains all step from cached increments
+    } else if (m == 5) {  // a batch whose domains all step from cached increments
         k_grow_fill_sparse_batch<FP32, ITEMS><<<g, kBlock, 0, E.stream>>>(E.base, n);
-    } else if (E.fill_mode == 2) {
+    } else if (m == 2) {
         k_grow_fill<FP32, ITEMS, false, 2><<<g, kBlock, 0, E.stream>>>(E.base, n);
     } else {
         k_grow_fill<FP32, ITEMS, false, kFillAny><<<g, kBlock, 0, E.stream>>>(E.base, n);
